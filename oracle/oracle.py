@@ -1,0 +1,209 @@
+"""ctypes front end of the CPU oracle (oracle/pwd_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py``, always as the checker or the timed CPU
+baseline, never by the product package.
+
+Each function mirrors the low-level reference entry point it restates
+(pyseistr/src/dip_cfuns.c ``dipc``, sof_cfuns.c ``csomean2d``/``csomf2d``,
+sof3d_cfuns.c ``csomean3d``/``csomf3d``, soint3d_cfuns.c ``csoint3d``) on
+column-major (Fortran-order) float32 or float64 arrays.  ``precision='f32'``
+reproduces the reference arithmetic, ``'f64'`` is the FP64 oracle.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "build", "libpwd_oracle.so")
+_lib = None
+
+USUM_DOUBLE = 1
+FILTER_REAL = 2
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_L = ctypes.c_long
+_F = ctypes.c_float
+_D = ctypes.c_double
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (seconds); returns the .so path."""
+    src = os.path.join(_HERE, "pwd_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        for pre, R in (("f32", _F), ("f64", _D)):
+            getattr(L, f"orc_dip_{pre}").argtypes = [_P, _P, _P] + [_I] * 10 + [_P]
+            getattr(L, f"orc_somean2d_{pre}").argtypes = [_P, _P, _P, _I, _I, _I, _I, _I, R, _I]
+            getattr(L, f"orc_somf2d_{pre}").argtypes = [_P, _P, _P] + [_I] * 7 + [R]
+            getattr(L, f"orc_somean3d_{pre}").argtypes = [_P, _P, _P, _P] + [_I] * 6
+            getattr(L, f"orc_somf3d_{pre}").argtypes = [_P, _P, _P, _P] + [_I] * 8
+            getattr(L, f"orc_soint3d_{pre}").argtypes = [_P] * 5 + [_I] * 10 + [R]
+        L.orc_pwspray2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
+        L.orc_pwspray3d_f32.argtypes = [_P, _P, _P, _P] + [_I] * 6
+        L.orc_spray_median_f32.argtypes = [_P, _P, _I, _I, _L, _I, _I]
+        _lib = L
+    return _lib
+
+
+def _dt(precision):
+    if precision not in ("f32", "f64"):
+        raise ValueError("precision must be 'f32' or 'f64'")
+    return np.float32 if precision == "f32" else np.float64
+
+
+def _flat(a, dt):
+    return np.ascontiguousarray(np.asarray(a, dtype=dt).flatten(order="F"))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _check(rc, name):
+    if rc != 0:
+        raise ValueError(f"{name}: invalid arguments (status {rc})")
+
+
+def dipc(din, n1, n2, n3, niter, liter, order, r1, r2, r3, mask=None, flags=0,
+         precision="f32", return_ls=False):
+    """Restatement of ``dipc``: returns n (n3==1) or 2n slopes, flat."""
+    dt = _dt(precision)
+    u = _flat(din, dt)
+    n = n1 * n2 * n3
+    if u.size != n:
+        raise ValueError("data size mismatch")
+    m = _flat(mask, dt) if mask is not None else None
+    nout = n if n3 == 1 else 2 * n
+    out = np.empty(nout, dtype=dt)
+    ls = np.zeros(2 * max(niter, 1), dtype=np.int32)
+    rc = getattr(lib(), f"orc_dip_{precision}")(
+        _ptr(u), _ptr(m), _ptr(out), n1, n2, n3, niter, liter, order, r1, r2, r3, flags, _ptr(ls))
+    _check(rc, "dipc")
+    return (out, ls) if return_ls else out
+
+
+def dip2d(din, niter=5, liter=20, order=2, rect=(10, 10, 1), mask=None, flags=0, precision="f32",
+          return_ls=False):
+    n1, n2 = din.shape
+    r = dipc(din, n1, n2, 1, niter, liter, order, rect[0], rect[1], rect[2], mask, flags,
+             precision, return_ls)
+    if return_ls:
+        return r[0].reshape(n1, n2, order="F"), r[1]
+    return r.reshape(n1, n2, order="F")
+
+
+def dip3d(din, niter=5, liter=10, order=2, rect=(5, 5, 5), mask=None, flags=0, precision="f32"):
+    n1, n2, n3 = din.shape
+    p = dipc(din, n1, n2, n3, niter, liter, order, rect[0], rect[1], rect[2], mask, flags,
+             precision)
+    p = p.reshape(n1, n2, n3, 2, order="F")
+    return p[..., 0], p[..., 1]
+
+
+def _shape3(dn):
+    if dn.ndim == 2:
+        return dn.shape[0], dn.shape[1], 1
+    return dn.shape
+
+
+def somean2d(dn, dip, ns, order, eps, adj=0, precision="f32"):
+    dt = _dt(precision)
+    n1, n2, n3 = _shape3(dn)
+    d, p = _flat(dn, dt), _flat(dip, dt)
+    out = np.empty(n1 * n2 * n3, dtype=dt)
+    rc = getattr(lib(), f"orc_somean2d_{precision}")(_ptr(d), _ptr(p), _ptr(out), n1, n2, n3, ns,
+                                                      order, eps, adj)
+    _check(rc, "somean2d")
+    return out.reshape(dn.shape, order="F")
+
+
+def somf2d(dn, dip, ns, order, eps, option=1, nmf=None, precision="f32"):
+    dt = _dt(precision)
+    n1, n2, n3 = _shape3(dn)
+    d, p = _flat(dn, dt), _flat(dip, dt)
+    out = np.empty(n1 * n2 * n3, dtype=dt)
+    nmf = 2 * ns + 1 if nmf is None else nmf
+    rc = getattr(lib(), f"orc_somf2d_{precision}")(_ptr(d), _ptr(p), _ptr(out), n1, n2, n3, ns,
+                                                    nmf, option, order, eps)
+    _check(rc, "somf2d")
+    return out.reshape(dn.shape, order="F")
+
+
+def somean3d(dn, dipi, dipx, r1, r2, order, precision="f32"):
+    dt = _dt(precision)
+    n1, n2, n3 = _shape3(dn)
+    d, p1, p2 = _flat(dn, dt), _flat(dipi, dt), _flat(dipx, dt)
+    out = np.empty(n1 * n2 * n3, dtype=dt)
+    rc = getattr(lib(), f"orc_somean3d_{precision}")(_ptr(d), _ptr(p1), _ptr(p2), _ptr(out), n1,
+                                                      n2, n3, r1, r2, order)
+    _check(rc, "somean3d")
+    return out.reshape(dn.shape, order="F")
+
+
+def somf3d(dn, dipi, dipx, r1, r2, order, option=1, nmf=None, precision="f32"):
+    dt = _dt(precision)
+    n1, n2, n3 = _shape3(dn)
+    d, p1, p2 = _flat(dn, dt), _flat(dipi, dt), _flat(dipx, dt)
+    out = np.empty(n1 * n2 * n3, dtype=dt)
+    nmf = 2 * r1 * r2 + 1 if nmf is None else nmf
+    rc = getattr(lib(), f"orc_somf3d_{precision}")(_ptr(d), _ptr(p1), _ptr(p2), _ptr(out), n1,
+                                                    n2, n3, r1, r2, nmf, option, order)
+    _check(rc, "somf3d")
+    return out.reshape(dn.shape, order="F")
+
+
+def soint3d(din, mask, dipi, dipx, order=1, niter=100, njs=(1, 1), drift=0, seed=202223,
+            hasmask=1, var=0.0, precision="f32"):
+    dt = _dt(precision)
+    n1, n2, n3 = din.shape
+    d, m = _flat(din, dt), _flat(mask, dt)
+    p, q = _flat(dipi, dt), _flat(dipx, dt)
+    out = np.empty(n1 * n2 * n3, dtype=dt)
+    rc = getattr(lib(), f"orc_soint3d_{precision}")(
+        _ptr(d), _ptr(m), _ptr(p), _ptr(q), _ptr(out), n1, n2, n3, order, njs[0], njs[1], niter,
+        drift, seed, hasmask, var)
+    _check(rc, "soint3d")
+    return out.reshape(n1, n2, n3, order="F")
+
+
+def pwspray2d(dn, dip, ns, order, eps):
+    """Sprayed panels u[n2][2ns+1][n1] (C order) of one 2-D section."""
+    n1, n2 = dn.shape
+    d, p = _flat(dn, np.float32), _flat(dip, np.float32)
+    u = np.empty((n2, 2 * ns + 1, n1), dtype=np.float32)
+    _check(lib().orc_pwspray2d_f32(_ptr(d), _ptr(p), _ptr(u), n1, n2, ns, order, eps), "pwspray2d")
+    return u
+
+
+def pwspray3d(dn, dipi, dipx, r1, r2, order):
+    """Sprayed panels u[n2*n3][np][n1] (C order) of one 3-D cube."""
+    n1, n2, n3 = dn.shape
+    npp = (2 * r1 + 1) * (2 * r2 + 1)
+    d, p1, p2 = (_flat(a, np.float32) for a in (dn, dipi, dipx))
+    u = np.empty((n2 * n3, npp, n1), dtype=np.float32)
+    _check(lib().orc_pwspray3d_f32(_ptr(d), _ptr(p1), _ptr(p2), _ptr(u), n1, n2, n3, r1, r2, order),
+           "pwspray3d")
+    return u
+
+
+def spray_median(u, nmf, option=1):
+    """Median row (np-1)/2 of sprayed panels u[ntr][np][n1] -> out[ntr][n1]."""
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    ntr, npp, n1 = u.shape
+    out = np.empty((ntr, n1), dtype=np.float32)
+    _check(lib().orc_spray_median_f32(_ptr(u), _ptr(out), n1, npp, ntr, nmf, option), "median")
+    return out
