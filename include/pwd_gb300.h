@@ -1,0 +1,144 @@
+/*
+ * pwd_gb300.h -- C ABI of the GB300 plane-wave-destruction library
+ * (libpwd_gb300.so).
+ *
+ * Drop-in boundary for pyseistr's structural hot path.  Each entry point
+ * replaces one low-level CPython entry of the reference and takes the same
+ * arguments with the same meaning, but on device memory:
+ *
+ *   - arrays are float32, column-major (Fortran order, time axis n1
+ *     fastest: i = i1 + n1*(i2 + n2*i3)), exactly as the reference's Python
+ *     wrappers flatten them before calling C;
+ *   - every pointer is a device pointer the caller allocated; the library
+ *     never allocates, its scratch is the caller's `workspace` of at least
+ *     the size the matching *_workspace_size() returns (256-byte aligned);
+ *   - work is enqueued on `stream` (NULL = legacy default stream) and the
+ *     call returns without synchronising; results are ready once the
+ *     stream has been synchronised;
+ *   - the library holds no global state: calls on different streams with
+ *     different workspaces may run concurrently;
+ *   - errors are returned as pwd_status codes (the reference prints and
+ *     returns NULL, which surfaces as SystemError).
+ *
+ * The plain path reproduces the reference's float arithmetic operation by
+ * operation, including its quirks (effective divne/CG eps = 1, eps forced
+ * to 0.01 in the 3-D filters, the triangle-weighted 2-D mean).
+ */
+#ifndef PWD_GB300_H
+#define PWD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *pwd_stream_t; /* same object as cudaStream_t */
+
+typedef enum {
+  PWD_OK = 0,
+  PWD_EINVAL = 1,      /* bad size or parameter (reference: "Dimension mismatch") */
+  PWD_EWORKSPACE = 2,  /* workspace missing, too small or misaligned */
+  PWD_ECUDA = 3,       /* a CUDA launch or runtime call failed */
+  PWD_ENOTSUP = 4      /* valid for the reference but not built here (order > 4) */
+} pwd_status;
+
+/* Library version as 10000*major + 100*minor + patch. */
+int pwd_version(void);
+/* Static description of a status code. */
+const char *pwd_status_string(int status);
+
+/* ------------------------------------------------------------------------
+ * Local slope by plane-wave destruction.
+ * Replaces dipc, pyseistr/src/dip_cfuns.c:1694-1989 (called by dip2dc,
+ * dip2d.py:115, and dip3dc, dip3d.py:59).
+ *   data     [n1*n2*n3]; mask [n1*n2*n3] or NULL (the reference appends the
+ *            mask to the data array and sets hasmask=1)
+ *   dip_out  n3 == 1: [n1*n2] inline slope;
+ *            n3 > 1 : [2*n1*n2*n3] inline slope, then crossline slope
+ *   niter    nonlinear (Gauss-Newton) iterations; liter: CG iterations of
+ *            the shaping division; order: PWD accuracy order (1..4);
+ *   rect     triangle smoothing radius per axis (1 = no smoothing)
+ * eps_dv / eps_cg / tol_cg of the reference are accepted by the Python
+ * layer and ignored there, as the reference C ignores them.
+ */
+size_t pwd_dip_workspace_size(int n1, int n2, int n3, int order, const int rect[3],
+                              int has_mask);
+int pwd_dip(const float *data, const float *mask, float *dip_out, int n1, int n2, int n3,
+            int niter, int liter, int order, const int rect[3], void *workspace,
+            size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 2-D structure-oriented mean, slice by slice over n3.
+ * Replaces csomean2d, pyseistr/src/sof_cfuns.c:1433-1531 (somean2dc,
+ * somean2d.py:36): triangle-weighted spray mean normalised by the spray of
+ * ones; adj != 0 applies the adjoint.
+ */
+size_t pwd_somean2d_workspace_size(int n1, int n2, int n3, int ns, int order);
+int pwd_somean2d(const float *data, const float *dip, float *out, int n1, int n2, int n3,
+                 int ns, int order, int adj, float eps, void *workspace,
+                 size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 2-D structure-oriented median filter, slice by slice over n3.
+ * Replaces csomf2d, pyseistr/src/sof_cfuns.c:1534-1678 (somf2dc,
+ * somf2d.py:60).  nmf: median window (somf2dc passes 2*ns+1);
+ * option 1 = median filter, otherwise space-varying median (svmf).
+ */
+size_t pwd_somf2d_workspace_size(int n1, int n2, int n3, int ns, int nmf, int option,
+                                 int order);
+int pwd_somf2d(const float *data, const float *dip, float *out, int n1, int n2, int n3, int ns,
+               int nmf, int option, int order, float eps, void *workspace,
+               size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 3-D structure-oriented mean over the (2*r1+1)*(2*r2+1) spray.
+ * Replaces csomean3d, pyseistr/src/sof3d_cfuns.c:1355-1551 (somean3dc,
+ * somean3d.py:36).  eps is accepted and replaced by 0.01 as the reference.
+ */
+size_t pwd_somean3d_workspace_size(int n1, int n2, int n3, int r1, int r2, int order);
+int pwd_somean3d(const float *data, const float *dip_inline, const float *dip_xline,
+                 float *out, int n1, int n2, int n3, int r1, int r2, int order, float eps,
+                 void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 3-D structure-oriented median filter.
+ * Replaces csomf3d, pyseistr/src/sof3d_cfuns.c:1554-1753 (somf3dc,
+ * somf3d.py:54).  nmf: median length (somf3dc passes 2*r1*r2+1), taken
+ * over raster-ordered spray slots centred on the centre slot.
+ */
+size_t pwd_somf3d_workspace_size(int n1, int n2, int n3, int r1, int r2, int nmf, int option,
+                                 int order);
+int pwd_somf3d(const float *data, const float *dip_inline, const float *dip_xline, float *out,
+               int n1, int n2, int n3, int r1, int r2, int nmf, int option, int order,
+               float eps, void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Median along the spray axis of given sprayed panels, centre row only.
+ * Replaces mf / svmf (pyseistr/src/sof_cfuns.c:1294-1332, :1334-1431, with
+ * mf_init/svmf_init axis=2 ifbound=1) as csomf2d/csomf3d apply them:
+ *   panels [ntr][np][n1] (each source trace's np sprayed traces),
+ *   out    [ntr][n1]     row (np-1)/2 of the filtered panel.
+ */
+size_t pwd_panel_median_workspace_size(int n1, int np, long ntr, int nmf, int option);
+int pwd_panel_median(const float *panels, float *out, int n1, int np, long ntr, int nmf,
+                     int option, void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * 3-D structure-oriented interpolation (PWD-regularised CG).
+ * Replaces csoint3d, pyseistr/src/soint3d_cfuns.c:2405-2507 (soint3dc,
+ * soint3d.py:65).  known = (mask != 0) if hasmask == 1, else (data != 0);
+ * var > 0 adds the reference's seeded MT19937/Box-Muller noise to the
+ * zero data of the PWD residual.
+ */
+size_t pwd_soint3d_workspace_size(int n1, int n2, int n3, int order);
+int pwd_soint3d(const float *data, const float *mask, const float *dip_inline,
+                const float *dip_xline, float *out, int n1, int n2, int n3, int order, int nj1,
+                int nj2, int niter, int drift, int seed, int hasmask, float var,
+                void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PWD_GB300_H */

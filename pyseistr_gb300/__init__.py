@@ -1,0 +1,31 @@
+"""pyseistr_gb300: GB300-native plane-wave-destruction hot path of pyseistr.
+
+Drop-in replacements of pyseistr's C-path entry points, computed by the
+sm_103a kernels of libpwd_gb300.so:
+
+    dip2dc, dip3dc                 local slopes (PWD + shaping division)
+    somean2dc, somf2dc             2-D structure-oriented mean / median
+    somean3dc, somf3dc             3-D structure-oriented mean / median
+    soint3dc                       3-D structure-oriented interpolation
+    dipc, csomean2d, csomf2d,      the reference's low-level positional
+    csomean3d, csomf3d, csoint3d   entries
+
+`pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
+"""
+from .api import (  # noqa: F401
+    csoint3d,
+    csomean2d,
+    csomean3d,
+    csomf2d,
+    csomf3d,
+    dip2dc,
+    dip3dc,
+    dipc,
+    soint3dc,
+    somean2dc,
+    somean3dc,
+    somf2dc,
+    somf3dc,
+)
+
+__version__ = "0.1.0"

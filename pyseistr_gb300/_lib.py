@@ -1,0 +1,70 @@
+"""ctypes binding of libpwd_gb300.so (the C ABI declared in include/pwd_gb300.h).
+
+The library is the only compute path: if it cannot be loaded, every entry
+point raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpwd_gb300.so")
+
+PWD_OK, PWD_EINVAL, PWD_EWORKSPACE, PWD_ECUDA, PWD_ENOTSUP = range(5)
+
+# Every symbol the header declares, with its ctypes signature.
+_P, _I, _F, _S = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+SIGNATURES = {
+    "pwd_version": ([], _I),
+    "pwd_status_string": ([_I], ctypes.c_char_p),
+    "pwd_dip_workspace_size": ([_I, _I, _I, _I, _P, _I], _S),
+    "pwd_dip": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _S, _P], _I),
+    "pwd_somean2d_workspace_size": ([_I, _I, _I, _I, _I], _S),
+    "pwd_somean2d": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_somf2d_workspace_size": ([_I, _I, _I, _I, _I, _I, _I], _S),
+    "pwd_somf2d": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_somean3d_workspace_size": ([_I, _I, _I, _I, _I, _I], _S),
+    "pwd_somean3d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_somf3d_workspace_size": ([_I, _I, _I, _I, _I, _I, _I, _I], _S),
+    "pwd_somf3d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_panel_median_workspace_size": ([_I, _I, ctypes.c_long, _I, _I], _S),
+    "pwd_panel_median": ([_P, _P, _I, _I, ctypes.c_long, _I, _I, _P, _S, _P], _I),
+    "pwd_soint3d_workspace_size": ([_I, _I, _I, _I], _S),
+    "pwd_soint3d": ([_P, _P, _P, _P, _P] + [_I] * 10 + [_F, _P, _S, _P], _I),
+}
+
+_lib = None
+
+
+class PwdError(RuntimeError):
+    """A library call failed (status other than PWD_OK / PWD_EINVAL)."""
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) and return the ctypes library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        from . import build as _build
+
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise PwdError(f"CUDA extension {LIB_PATH} is missing: run pyseistr_gb300.build.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str) -> None:
+    if status == PWD_OK:
+        return
+    msg = f"{what}: {load().pwd_status_string(status).decode()} (status {status})"
+    if status == PWD_EINVAL:
+        raise ValueError(msg)
+    raise PwdError(msg)

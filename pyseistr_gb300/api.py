@@ -1,0 +1,199 @@
+"""pyseistr-compatible host API on the GB300 kernels.
+
+Same names, signatures, defaults and return types as the reference's C-path
+wrappers (pyseistr/dip2d.py:115 dip2dc, dip3d.py:59 dip3dc,
+somean2d.py:36 somean2dc, somf2d.py:60 somf2dc, somean3d.py:36 somean3dc,
+somf3d.py:54 somf3dc, soint3d.py:65 soint3dc) and low-level entries (dipc,
+csomean2d, csomf2d, csomean3d, csomf3d, csoint3d with the reference's
+positional argument tuples).  NumPy inputs are flattened in Fortran order to
+float32, copied to the GPU, processed and copied back as NumPy float32;
+CUDA tensors stay on the device and CUDA tensors are returned.
+
+Arguments the reference C ignores are accepted and ignored here too
+(eps_dv, eps_cg, tol_cg of dip*; eps of the 3-D filters is replaced by 0.01;
+verb, runc).  Bad sizes raise ValueError where the reference prints
+"Dimension mismatch" and returns NULL.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import device as D
+
+
+def _dev():
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyseistr_gb300 needs a CUDA GPU; no CPU fallback exists")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _to_dev_flat(a):
+    """(array, was_tensor): a flat float32 CUDA tensor in Fortran order."""
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=_dev(), dtype=torch.float32)
+        t = t.permute(*reversed(range(t.dim()))).contiguous().view(-1)
+        return t, True
+    arr = np.asarray(a, dtype=np.float32)
+    flat = np.ascontiguousarray(arr.reshape(-1, order="F"))
+    pinned = torch.from_numpy(flat).pin_memory()
+    return pinned.to(_dev(), non_blocking=True), False
+
+
+def _from_dev_flat(t, shape, as_tensor):
+    if as_tensor:
+        return t.view(*reversed(shape)).permute(*reversed(range(len(shape))))
+    host = t.cpu().numpy()
+    return host.reshape(shape, order="F")
+
+
+# --------------------------------------------------------------------------
+# low-level entries (reference positional tuples)
+# --------------------------------------------------------------------------
+def dipc(din, n1, n2, n3, niter, liter, order, eps_dv, eps_cg, tol_cg, r1, r2, r3, hasmask,
+         verb):
+    """dipc "Oiiiiiifffiiiii" (dip_cfuns.c:1708): din is [data] or [data, mask]."""
+    t, as_t = _to_dev_flat(din)
+    n = n1 * n2 * n3
+    if hasmask:
+        if t.numel() != 2 * n:
+            raise ValueError(f"Dimension mismatch, N_input = {t.numel()}, N_data = {2 * n}")
+        data, mask = t[:n], t[n:]
+    else:
+        if t.numel() != n:
+            raise ValueError(f"Dimension mismatch, N_input = {t.numel()}, N_data = {n}")
+        data, mask = t, None
+    out = D.dip(data, n1, n2, n3, niter, liter, order, (r1, r2, r3), mask)
+    return out if as_t else out.cpu().numpy()
+
+
+def csomean2d(dn, dip, n1, n2, n3, ns, order, adj, eps, verb):
+    d, as_t = _to_dev_flat(dn)
+    p, _ = _to_dev_flat(dip)
+    out = D.somean2d(d, p, n1, n2, n3, ns, order, eps, adj)
+    return out if as_t else out.cpu().numpy()
+
+
+def csomf2d(dn, dip, n1, n2, n3, ns, nmf, option, order, eps, verb):
+    d, as_t = _to_dev_flat(dn)
+    p, _ = _to_dev_flat(dip)
+    out = D.somf2d(d, p, n1, n2, n3, ns, nmf, option, order, eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def csomean3d(dn, dipi, dipx, n1, n2, n3, r1, r2, order, eps, verb):
+    d, as_t = _to_dev_flat(dn)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.somean3d(d, pi, px, n1, n2, n3, r1, r2, order, eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def csomf3d(dn, dipi, dipx, n1, n2, n3, r1, r2, nmf, option, order, eps, verb):
+    d, as_t = _to_dev_flat(dn)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.somf3d(d, pi, px, n1, n2, n3, r1, r2, nmf, option, order, eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def csoint3d(din, mask, dipi, dipx, n1, n2, n3, nw, nj1, nj2, niter, drift, seed, hasmask, var,
+             verb):
+    d, as_t = _to_dev_flat(din)
+    m, _ = _to_dev_flat(mask)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.soint3d(d, m, pi, px, n1, n2, n3, nw, nj1, nj2, niter, drift, seed, hasmask, var)
+    return out if as_t else out.cpu().numpy()
+
+
+# --------------------------------------------------------------------------
+# high-level entries
+# --------------------------------------------------------------------------
+def dip2dc(din, niter=5, liter=20, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.000001,
+           rect=[10, 10, 1], verb=1, mask=None):
+    """2-D slope by shaping-regularised PWD (dip2d.py:115)."""
+    n1, n2 = din.shape[0], din.shape[1]
+    d, as_t = _to_dev_flat(din)
+    m = None
+    if mask is not None:
+        if int(np.prod(mask.shape)) != n1 * n2:
+            raise ValueError("Mask and Data should have the same dimension")
+        m, _ = _to_dev_flat(mask)
+    out = D.dip(d, n1, n2, 1, niter, liter, order, rect, m)
+    return _from_dev_flat(out, (n1, n2), as_t)
+
+
+def dip3dc(din, niter=5, liter=10, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.000001,
+           rect=[5, 5, 5], verb=1, runc=1, mask=None):
+    """3-D inline and crossline slopes (dip3d.py:59)."""
+    n1, n2, n3 = din.shape
+    d, as_t = _to_dev_flat(din)
+    m = None
+    if mask is not None:
+        if int(np.prod(mask.shape)) != n1 * n2 * n3:
+            raise ValueError("Mask and Data should have the same dimension")
+        m, _ = _to_dev_flat(mask)
+    out = D.dip(d, n1, n2, n3, niter, liter, order, rect, m)
+    n = n1 * n2 * n3
+    return (_from_dev_flat(out[:n], (n1, n2, n3), as_t),
+            _from_dev_flat(out[n:], (n1, n2, n3), as_t))
+
+
+def _shape3(dn):
+    if dn.ndim == 2:
+        return dn.shape[0], dn.shape[1], 1
+    return tuple(dn.shape)
+
+
+def somean2dc(dn, dip, ns, order, eps, adj=0, verb=1):
+    """Structure-oriented (triangle-weighted) mean, 2-D slices (somean2d.py:36)."""
+    n1, n2, n3 = _shape3(dn)
+    d, as_t = _to_dev_flat(dn)
+    p, _ = _to_dev_flat(dip)
+    out = D.somean2d(d, p, n1, n2, n3, ns, order, eps, adj)
+    res = _from_dev_flat(out, (n1, n2, n3), as_t)
+    return res.squeeze() if n3 == 1 else res
+
+
+def somf2dc(dn, dip, ns, order, eps, option=1, verb=1):
+    """Structure-oriented median filter, 2-D slices (somf2d.py:60)."""
+    n1, n2, n3 = _shape3(dn)
+    d, as_t = _to_dev_flat(dn)
+    p, _ = _to_dev_flat(dip)
+    out = D.somf2d(d, p, n1, n2, n3, ns, 2 * ns + 1, option, order, eps)
+    res = _from_dev_flat(out, (n1, n2, n3), as_t)
+    return res.squeeze() if n3 == 1 else res
+
+
+def somean3dc(dn, dipi, dipx, r1, r2, eps, order, verb=0):
+    """3-D structure-oriented mean (somean3d.py:36)."""
+    n1, n2, n3 = _shape3(dn)
+    d, as_t = _to_dev_flat(dn)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.somean3d(d, pi, px, n1, n2, n3, r1, r2, order, eps)
+    return _from_dev_flat(out, (n1, n2, n3), as_t)
+
+
+def somf3dc(dn, dipi, dipx, r1, r2, eps, order, option=1, verb=1):
+    """3-D structure-oriented median filter (somf3d.py:54)."""
+    n1, n2, n3 = _shape3(dn)
+    d, as_t = _to_dev_flat(dn)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.somf3d(d, pi, px, n1, n2, n3, r1, r2, 2 * r1 * r2 + 1, option, order, eps)
+    return _from_dev_flat(out, (n1, n2, n3), as_t)
+
+
+def soint3dc(din, mask, dipi, dipx, order=1, niter=100, njs=[1, 1], drift=0, seed=202223,
+             hasmask=1, var=0, verb=1):
+    """3-D structure-oriented interpolation (soint3d.py:65)."""
+    n1, n2, n3 = din.shape
+    d, as_t = _to_dev_flat(din)
+    m, _ = _to_dev_flat(mask)
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    out = D.soint3d(d, m, pi, px, n1, n2, n3, order, njs[0], njs[1], niter, drift, seed, hasmask,
+                    var)
+    return _from_dev_flat(out, (n1, n2, n3), as_t)

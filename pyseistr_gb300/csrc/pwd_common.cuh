@@ -1,0 +1,259 @@
+// Shared device code of the GB300 plane-wave-destruction (PWD) library.
+//
+// Arithmetic contract of the plain FP32 path: every float operation of the
+// reference (pyseistr/src/*_cfuns.c) is reproduced in the same order with
+// the same rounding.  The library is compiled with -fmad=false so that no
+// multiply-add is contracted (the reference is FMA-free x86-64 SSE code);
+// FMAs appear only where written explicitly (__fmaf_rn), i.e. inside the
+// error-free transformations below.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pwd_gb300.h"
+
+#ifndef PWD_MAX_ORDER
+#define PWD_MAX_ORDER 4
+#endif
+#define PWD_MAX_NF (2 * PWD_MAX_ORDER)
+#define PWD_MAX_NA (2 * PWD_MAX_ORDER + 1)
+
+namespace pwd {
+
+// ---------------------------------------------------------------------------
+// All-pass filter constants (apfilt_init, dip_cfuns.c:835-855): b[k] as a
+// double and as a float-float pair.
+// ---------------------------------------------------------------------------
+struct ApCoef {
+  int nw, nf;
+  double b[PWD_MAX_NA];
+  float bh[PWD_MAX_NA], bl[PWD_MAX_NA];
+};
+
+inline ApCoef make_apcoef(int nw) {
+  ApCoef c;
+  c.nw = nw;
+  c.nf = 2 * nw;
+  for (int k = 0; k <= c.nf; k++) {
+    double bk = 1.0;
+    for (int j = 0; j < c.nf; j++) {
+      if (j < c.nf - k)
+        bk *= (k + j + 1.0) / (2 * (2 * j + 1) * (j + 1));
+      else
+        bk *= 1.0 / (2 * (2 * j + 1));
+    }
+    c.b[k] = bk;
+    c.bh[k] = (float)bk;
+    c.bl[k] = (float)(bk - (double)c.bh[k]);
+  }
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Float-float arithmetic (Dekker 1971, Knuth TAOCP vol. 2 "TwoSum").
+// ---------------------------------------------------------------------------
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  float p = __fmul_rn(a.h, b);
+  float pl = __fmaf_rn(a.h, b, -p);
+  float e = __fmaf_rn(a.l, b, pl);
+  float s = __fadd_rn(p, e);
+  return {s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  float p = __fmul_rn(a.h, b.h);
+  float pl = __fmaf_rn(a.h, b.h, -p);
+  float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, pl));
+  float s = __fadd_rn(p, e);
+  return {s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = ff_two_sum(a.h, b.h);
+  float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+  return ff_two_sum(s.h, e);
+}
+
+// True when rounding the float-float value (h,l) to float could differ from
+// rounding the exact value, given an absolute error bound tol of the pair:
+// i.e. (h+l) lies within tol of the midpoint between h and its neighbour on
+// the side of l.  Also true for zero, tiny or non-finite h (handled exactly).
+__device__ __forceinline__ bool ff_near_tie(float h, float l, float tol) {
+  uint32_t bits = __float_as_uint(h) & 0x7fffffffu;
+  if (bits < (30u << 23) || bits >= 0x7f800000u) return true;
+  float ulp = __uint_as_float((bits & 0x7f800000u) - (23u << 23));
+  bool toward_zero = (l != 0.f) && ((l < 0.f) != (h < 0.f));
+  float half = ((bits & 0x007fffffu) == 0u && toward_zero) ? 0.25f * ulp : 0.5f * ulp;
+  return __fsub_rn(half, fabsf(l)) <= tol;
+}
+
+// Factor j of tap k: (nf-j-p) or ((p+j)+1), in float as the C expression.
+__device__ __forceinline__ float ap_factor(int nf, int k, int j, float p) {
+  if (j < nf - k) return __fsub_rn((float)(nf - j), p);
+  return __fadd_rn(__fadd_rn(p, (float)j), 1.0f);
+}
+
+// passfilter tap k (dip_cfuns.c:863-881): double product rounded to float,
+// evaluated in float-float and redone in FP64 only near a rounding tie.
+__device__ __forceinline__ float pass_tap(const ApCoef& c, int k, float p) {
+  ff a = {c.bh[k], c.bl[k]};
+  for (int j = 0; j < c.nf; j++) a = ff_mul_f(a, ap_factor(c.nf, k, j, p));
+  if (!ff_near_tie(a.h, a.l, fabsf(a.h) * 0x1p-40f)) return a.h;
+  double ak = c.b[k];
+  for (int j = 0; j < c.nf; j++) ak = __dmul_rn(ak, (double)ap_factor(c.nf, k, j, p));
+  return __double2float_rn(ak);
+}
+
+// aderfilter tap k (dip_cfuns.c:883-910), same scheme.
+__device__ __forceinline__ float ader_tap(const ApCoef& c, int k, float p) {
+  ff s = {0.f, 0.f};
+  float sabs = 0.f;
+  for (int i = 0; i < c.nf; i++) {
+    ff ai = {-1.f, 0.f};
+    for (int j = 0; j < c.nf; j++) {
+      if (j != i)
+        ai = ff_mul_f(ai, ap_factor(c.nf, k, j, p));
+      else if (j < c.nf - k)
+        ai = {-ai.h, -ai.l};
+    }
+    s = ff_add(s, ai);
+    sabs = __fadd_rn(sabs, fabsf(ai.h));
+  }
+  ff r = ff_mul(s, ff{c.bh[k], c.bl[k]});
+  if (!ff_near_tie(r.h, r.l, sabs * fabsf(c.bh[k]) * 0x1p-38f)) return r.h;
+  double ak = 0.0;
+  for (int i = 0; i < c.nf; i++) {
+    double ai = -1.0;
+    for (int j = 0; j < c.nf; j++) {
+      if (j != i)
+        ai = __dmul_rn(ai, (double)ap_factor(c.nf, k, j, p));
+      else if (j < c.nf - k)
+        ai = __dmul_rn(ai, -1.0);
+    }
+    ak = __dadd_rn(ak, ai);
+  }
+  return __double2float_rn(__dmul_rn(ak, c.b[k]));
+}
+
+template <int NW>
+__device__ __forceinline__ void passfilter(const ApCoef& c, float p, float* a) {
+#pragma unroll
+  for (int k = 0; k <= 2 * NW; k++) a[k] = pass_tap(c, k, p);
+}
+template <int NW>
+__device__ __forceinline__ void aderfilter(const ApCoef& c, float p, float* a) {
+#pragma unroll
+  for (int k = 0; k <= 2 * NW; k++) a[k] = ader_tap(c, k, p);
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions: per-block partials, summed in a fixed order by
+// the last block to finish (no floating-point atomics).
+// ---------------------------------------------------------------------------
+constexpr int kRedBlock = 256;
+constexpr int kRedGridMax = 1184;  // 8 x 148: a fixed, size-independent cap
+
+inline int red_grid(long n) {
+  long g = (n + kRedBlock - 1) / kRedBlock;
+  if (g > kRedGridMax) g = kRedGridMax;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+template <int K>
+struct dvec {
+  double v[K];
+};
+
+template <int K>
+__device__ __forceinline__ dvec<K> block_sum(dvec<K> x) {
+  __shared__ double sh[K][32];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x.v[k] += __shfl_down_sync(0xffffffffu, x.v[k], o);
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) sh[k][w] = x.v[k];
+  }
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double t = lane < nw ? sh[k][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      x.v[k] = t;
+    }
+  }
+  return x;  // valid in thread 0
+}
+
+// Publishes this block's partial sums; returns true (in every thread of the
+// block) for the last block, which then holds the grid totals in tot.
+template <int K>
+__device__ __forceinline__ bool grid_sum_last(dvec<K> x, double* partials, unsigned* counter,
+                                              dvec<K>& tot) {
+  __shared__ bool s_last;
+  dvec<K> b = block_sum<K>(x);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) partials[(size_t)k * gridDim.x + blockIdx.x] = b.v[k];
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  dvec<K> y;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      t += __ldcg(partials + (size_t)k * gridDim.x + i);
+    y.v[k] = t;
+  }
+  tot = block_sum<K>(y);
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Workspace carving (256-byte aligned slices of the caller's buffer).
+// ---------------------------------------------------------------------------
+struct Carver {
+  char* base;
+  size_t off = 0;
+  explicit Carver(void* b) : base((char*)b) {}
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = base ? (T*)(base + off) : nullptr;
+    off += count * sizeof(T);
+    return p;
+  }
+  size_t size() const { return (off + 255) & ~(size_t)255; }
+};
+
+inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? PWD_OK : PWD_ECUDA; }
+
+}  // namespace pwd
+
+#define PWD_LAUNCH_CHECK()                            \
+  do {                                                \
+    cudaError_t e_ = cudaGetLastError();              \
+    if (e_ != cudaSuccess) return PWD_ECUDA;          \
+  } while (0)

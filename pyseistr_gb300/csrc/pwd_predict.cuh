@@ -1,0 +1,404 @@
+// One plane-wave-destruction trace prediction, streamed along the trace by
+// one thread.
+//
+// Restates predict_step(adj=false) (pyseistr/src/sof_cfuns.c:622-649),
+// predict1_step and predict2_step (sof3d_cfuns.c:596-661) and the adjoint
+// predict_step(adj=true): regularization (:603-620), pwd_define (:453-497),
+// sf_banded_define (:161-186), pwd_set (:499-555) and sf_banded_solve
+// (:287-307), with the same float operations in the same order.
+//
+// The ascending pass keeps sliding windows (registers) of the filter
+// columns, the pwd_set intermediate and the last `band` LDL' columns, and
+// fuses the band accumulation, the factorisation, the filter application
+// and the forward substitution; the descending pass does the back
+// substitution.  The factor (o, d) and the forward-substituted trace (y)
+// go to a per-thread, thread-interleaved scratch (element k at k*ss).
+#pragma once
+
+#include "pwd_common.cuh"
+
+namespace pwd {
+
+struct PredictScratch {
+  float* o;  // [NB][n1] interleaved: o[m][k] at (m*n1 + k)*ss
+  float* d;  // [n1]
+  float* y;  // [n1]
+  long ss;   // interleave stride (number of threads sharing the scratch)
+};
+
+template <int NW>
+struct FilterWin {
+  // a[c][j]: filter tap j of column (i - NW + c), c = 0..2NW
+  float a[2 * NW + 1][2 * NW + 1];
+};
+
+template <int NW>
+__device__ __forceinline__ void filter_column(const ApCoef& c, float p, bool reversed, float* col) {
+  float b[2 * NW + 1];
+  passfilter<NW>(c, p, b);
+#pragma unroll
+  for (int j = 0; j <= 2 * NW; j++) col[j] = reversed ? b[2 * NW - j] : b[j];
+}
+
+template <int NW>
+__device__ __forceinline__ void shift_win(FilterWin<NW>& w) {
+#pragma unroll
+  for (int c = 0; c < 2 * NW; c++)
+#pragma unroll
+    for (int j = 0; j <= 2 * NW; j++) w.a[c][j] = w.a[c + 1][j];
+}
+
+// Band entries of row i from the filter window (pwd_define :475-495): adds
+// to diag and offd[0..NB) in the reference's j order.
+template <int NW>
+__device__ __forceinline__ void band_add(const FilterWin<NW>& w, int i, int n1, float& diag,
+                                         float* offd) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+#pragma unroll
+  for (int j = 0; j < NA; j++) {
+    int k = i + j - NW;
+    if (k >= NW && k < n1 - NW) {
+      float aj = w.a[j][j];
+      diag = __fadd_rn(diag, __fmul_rn(aj, aj));
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+#pragma unroll
+    for (int j = m + 1; j < NA; j++) {
+      int k = i + j - NW;
+      if (k >= NW && k < n1 - NW) {
+        float aj = w.a[j][j];
+        float am = w.a[j][j - m - 1];
+        offd[m] = __fadd_rn(offd[m], __fmul_rn(am, aj));
+      }
+    }
+  }
+}
+
+// regularization() values of row i.
+template <int NB>
+__device__ __forceinline__ void reg_row(int i, int n1, float eps, float eps2, float& diag,
+                                        float* offd) {
+  diag = __double2float_rn(6. * (double)eps);
+  if (i == 0 || i == n1 - 1) diag = __fadd_rn(eps2, eps);
+  if (i == 1 || i == n1 - 2) diag = __double2float_rn((double)eps2 + 5. * (double)eps);
+  offd[0] = __double2float_rn(-4. * (double)eps);
+  if (i == 0 || i == n1 - 2) offd[0] = __double2float_rn(-2. * (double)eps);
+  offd[1] = eps;
+#pragma unroll
+  for (int b = 2; b < NB; b++) offd[b] = 0.f;
+}
+
+// sf_banded_define step at row k with the window of previous columns:
+// O[c][m] = o[m][k-1-c], D[c] = d[k-1-c].  Returns d[k] and o[0..NB)[k].
+template <int NB>
+__device__ __forceinline__ void ldl_row(int k, int n1, float diag, const float* offd,
+                                        const float (&O)[NB][NB], const float (&D)[NB],
+                                        float& dk, float* ok) {
+  float t = diag;
+#pragma unroll
+  for (int m = 0; m < NB; m++)
+    if (m < k) t = __fsub_rn(t, __fmul_rn(__fmul_rn(O[m][m], O[m][m]), D[m]));
+  dk = t;
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    if (q < n1 - k - 1) {
+      float s = offd[q];
+#pragma unroll
+      for (int m = 0; m < NB - q - 1; m++)
+        if (m < k) s = __fsub_rn(s, __fmul_rn(__fmul_rn(O[m][m], O[m][q + m + 1]), D[m]));
+      ok[q] = __fdiv_rn(s, dk);
+    } else {
+      ok[q] = 0.f;
+    }
+  }
+}
+
+// Forward prediction into `out` (predict_step adj=false, predict1_step,
+// predict2_step).  in1/in2 input traces, pp1/pp2 slope traces, contiguous.
+// forw1/forw2 select the reversed filter (pwd_define adj flag).
+template <int NW, bool TWO>
+__device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
+                            const float* __restrict__ in1, const float* __restrict__ pp1,
+                            bool forw1, const float* __restrict__ in2,
+                            const float* __restrict__ pp2, bool forw2, float* __restrict__ out,
+                            const PredictScratch& sc) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  FilterWin<NW> w1, w2;
+  float x1[NA], x2[NA];    // input window in[i .. i+2NW]
+  float t1[NA], t2[NA];    // pwd_set intermediate tmp[i-NW .. i+NW]
+  float O[NB][NB], D[NB];  // previous LDL' columns
+  float Y[NB];             // previous forward-substituted values y[k-1-c]
+
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++)
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      w1.a[cc][j] = 0.f;
+      if (TWO) w2.a[cc][j] = 0.f;
+    }
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++) {
+    t1[cc] = 0.f;
+    t2[cc] = 0.f;
+  }
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    D[m] = 0.f;
+    Y[m] = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[m][q] = 0.f;
+  }
+  // prefill: filter columns 0..NW-1 go to window slots NW+1..2NW (for i=0 the
+  // window holds columns -NW..NW); inputs in[0..2NW-1] to x slots 1..2NW.
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++) {
+    if (cc < n1) {
+      filter_column<NW>(c, pp1[cc], forw1, w1.a[NW + 1 + cc]);
+      if (TWO) filter_column<NW>(c, pp2[cc], forw2, w2.a[NW + 1 + cc]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    x1[q + 1] = q < n1 ? in1[q] : 0.f;
+    if (TWO) x2[q + 1] = q < n1 ? in2[q] : 0.f;
+  }
+  // pwd_set intermediate for columns < NW is zero; columns NW.. are made
+  // when the column enters the window.
+  float b0, b1, b2, b3;  // boundary values t0..t3
+  if (TWO) {
+    b0 = __fmul_rn(0.5f, __fadd_rn(in1[0], in2[0]));
+    b1 = __fmul_rn(0.5f, __fadd_rn(in1[1], in2[1]));
+    b2 = __fmul_rn(0.5f, __fadd_rn(in1[n1 - 2], in2[n1 - 2]));
+    b3 = __fmul_rn(0.5f, __fadd_rn(in1[n1 - 1], in2[n1 - 1]));
+  } else {
+    b0 = in1[0];
+    b1 = in1[1];
+    b2 = in1[n1 - 2];
+    b3 = in1[n1 - 1];
+  }
+
+  for (int i = 0; i < n1; i++) {
+    // advance: column i+NW enters the windows
+    const int cn = i + NW;
+    shift_win<NW>(w1);
+    if (TWO) shift_win<NW>(w2);
+#pragma unroll
+    for (int q = 0; q < NA - 1; q++) {
+      x1[q] = x1[q + 1];
+      if (TWO) x2[q] = x2[q + 1];
+      t1[q] = t1[q + 1];
+      if (TWO) t2[q] = t2[q + 1];
+    }
+    const int ln = i + 2 * NW;  // newest input sample
+    x1[NA - 1] = ln < n1 ? in1[ln] : 0.f;
+    if (TWO) x2[NA - 1] = ln < n1 ? in2[ln] : 0.f;
+    if (cn < n1) {
+      filter_column<NW>(c, pp1[cn], forw1, w1.a[2 * NW]);
+      if (TWO) filter_column<NW>(c, pp2[cn], forw2, w2.a[2 * NW]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < NA; j++) {
+        w1.a[2 * NW][j] = 0.f;
+        if (TWO) w2.a[2 * NW][j] = 0.f;
+      }
+    }
+    // pwd_set forward, first loop: tmp[cn] = sum_j a[j][cn] * in[cn+j-NW]
+    float s1 = 0.f, s2 = 0.f;
+    if (cn >= NW && cn < n1 - NW) {
+#pragma unroll
+      for (int j = 0; j < NA; j++) {
+        s1 = __fadd_rn(s1, __fmul_rn(w1.a[2 * NW][j], x1[j]));
+        if (TWO) s2 = __fadd_rn(s2, __fmul_rn(w2.a[2 * NW][j], x2[j]));
+      }
+    }
+    t1[NA - 1] = s1;
+    if (TWO) t2[NA - 1] = s2;
+
+    // band row i: regularization + pwd_define of each filter
+    float diag, offd[NB];
+    reg_row<NB>(i, n1, eps, eps2, diag, offd);
+    band_add<NW>(w1, i, n1, diag, offd);
+    if (TWO) band_add<NW>(w2, i, n1, diag, offd);
+
+    // pwd_set forward, second loop: out[i] = sum_j a[j][k] tmp[k], k=i+j-NW
+    float o1 = 0.f, o2 = 0.f;
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      int k = i + j - NW;
+      if (k >= NW && k < n1 - NW) {
+        o1 = __fadd_rn(o1, __fmul_rn(w1.a[j][j], t1[j]));
+        if (TWO) o2 = __fadd_rn(o2, __fmul_rn(w2.a[j][j], t2[j]));
+      }
+    }
+    float b = TWO ? __fadd_rn(o1, o2) : o1;
+    if (i == 0) b = __fadd_rn(b, __fmul_rn(eps2, b0));
+    if (i == 1) b = __fadd_rn(b, __fmul_rn(eps2, b1));
+    if (i == n1 - 2) b = __fadd_rn(b, __fmul_rn(eps2, b2));
+    if (i == n1 - 1) b = __fadd_rn(b, __fmul_rn(eps2, b3));
+
+    // LDL' row and forward substitution
+    float dk, ok[NB];
+    ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);
+    float y = b;
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < i) y = __fsub_rn(y, __fmul_rn(O[m][m], Y[m]));
+    // store the factor column and y for the descending pass
+#pragma unroll
+    for (int m = 0; m < NB; m++) sc.o[((long)m * n1 + i) * sc.ss] = ok[m];
+    sc.d[(long)i * sc.ss] = dk;
+    sc.y[(long)i * sc.ss] = y;
+    // shift the LDL' windows: column i becomes c=0
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) {
+      D[m] = D[m - 1];
+      Y[m] = Y[m - 1];
+#pragma unroll
+      for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
+    }
+    D[0] = dk;
+    Y[0] = y;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[0][q] = ok[q];
+  }
+
+  // back substitution: x[k] = y[k]/d[k] - sum_m o[m][k] x[k+m+1]
+  float X[NB];
+#pragma unroll
+  for (int m = 0; m < NB; m++) X[m] = 0.f;
+  for (int k = n1 - 1; k >= 0; k--) {
+    float t = __fdiv_rn(sc.y[(long)k * sc.ss], sc.d[(long)k * sc.ss]);
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < n1 - k - 1) t = __fsub_rn(t, __fmul_rn(sc.o[((long)m * n1 + k) * sc.ss], X[m]));
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) X[m] = X[m - 1];
+    X[0] = t;
+    out[k] = t;
+  }
+}
+
+// Adjoint prediction in place (predict_step adj=true, sof_cfuns.c:622-649):
+// solve, then the adjoint pwd_set, then the boundary terms.  `tr` is the
+// trace (contiguous), `xs` a per-thread interleaved scratch of n1 floats.
+template <int NW>
+__device__ void predict_adj(int n1, float eps, float eps2, const ApCoef& c, float* __restrict__ tr,
+                            const float* __restrict__ pp, bool forw, const PredictScratch& sc,
+                            float* __restrict__ xs) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  FilterWin<NW> w1;
+  float O[NB][NB], D[NB], Y[NB];
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++)
+#pragma unroll
+    for (int j = 0; j < NA; j++) w1.a[cc][j] = 0.f;
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    D[m] = 0.f;
+    Y[m] = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[m][q] = 0.f;
+  }
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++)
+    if (cc < n1) filter_column<NW>(c, pp[cc], forw, w1.a[NW + 1 + cc]);
+  // pass 1: factor + forward substitution of the trace itself
+  for (int i = 0; i < n1; i++) {
+    const int cn = i + NW;
+    shift_win<NW>(w1);
+    if (cn < n1)
+      filter_column<NW>(c, pp[cn], forw, w1.a[2 * NW]);
+    else
+#pragma unroll
+      for (int j = 0; j < NA; j++) w1.a[2 * NW][j] = 0.f;
+    float diag, offd[NB];
+    reg_row<NB>(i, n1, eps, eps2, diag, offd);
+    band_add<NW>(w1, i, n1, diag, offd);
+    float dk, ok[NB];
+    ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);
+    float y = tr[i];
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < i) y = __fsub_rn(y, __fmul_rn(O[m][m], Y[m]));
+#pragma unroll
+    for (int m = 0; m < NB; m++) sc.o[((long)m * n1 + i) * sc.ss] = ok[m];
+    sc.d[(long)i * sc.ss] = dk;
+    sc.y[(long)i * sc.ss] = y;
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) {
+      D[m] = D[m - 1];
+      Y[m] = Y[m - 1];
+#pragma unroll
+      for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
+    }
+    D[0] = dk;
+    Y[0] = y;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[0][q] = ok[q];
+  }
+  // pass 2: back substitution into xs
+  float X[NB];
+#pragma unroll
+  for (int m = 0; m < NB; m++) X[m] = 0.f;
+  for (int k = n1 - 1; k >= 0; k--) {
+    float t = __fdiv_rn(sc.y[(long)k * sc.ss], sc.d[(long)k * sc.ss]);
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < n1 - k - 1) t = __fsub_rn(t, __fmul_rn(sc.o[((long)m * n1 + k) * sc.ss], X[m]));
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) X[m] = X[m - 1];
+    X[0] = t;
+    xs[(long)k * sc.ss] = t;
+  }
+  const float b0 = xs[0], b1 = xs[sc.ss], b2 = xs[(long)(n1 - 2) * sc.ss],
+              b3 = xs[(long)(n1 - 1) * sc.ss];
+  // pass 3: adjoint pwd_set.  tmp[k] = sum_{j=NA-1..0} a[j][k] x[k+NW-j]
+  // (k in [NW, n1-NW)), then out[q] = sum_{j=NA-1..0} a[j][i] tmp[i] with
+  // i = q+NW-j in [NW, n1-NW); both in the reference's accumulation order.
+  FilterWin<NW> w;
+  float tw[NA];  // tw[c] = tmp[q-NW+c], aligned with the filter window
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++) {
+    tw[cc] = 0.f;
+#pragma unroll
+    for (int j = 0; j < NA; j++) w.a[cc][j] = 0.f;
+  }
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++)
+    if (cc < n1) filter_column<NW>(c, pp[cc], forw, w.a[NW + 1 + cc]);
+  for (int q = 0; q < n1; q++) {
+    const int cn = q + NW;
+    shift_win<NW>(w);
+#pragma unroll
+    for (int cc = 0; cc < NA - 1; cc++) tw[cc] = tw[cc + 1];
+    if (cn < n1)
+      filter_column<NW>(c, pp[cn], forw, w.a[2 * NW]);
+    else
+#pragma unroll
+      for (int j = 0; j < NA; j++) w.a[2 * NW][j] = 0.f;
+    float tk = 0.f;
+    if (cn >= NW && cn < n1 - NW) {
+#pragma unroll
+      for (int j = NA - 1; j >= 0; j--) {
+        int ii = cn + NW - j;
+        if (ii >= 0 && ii < n1) tk = __fadd_rn(tk, __fmul_rn(w.a[2 * NW][j], xs[(long)ii * sc.ss]));
+      }
+    }
+    tw[NA - 1] = tk;
+    float o = 0.f;
+#pragma unroll
+    for (int j = NA - 1; j >= 0; j--) {
+      int ii = q + NW - j;  // window slot of column ii is ii - (q - NW) = 2NW - j
+      if (ii >= NW && ii < n1 - NW) o = __fadd_rn(o, __fmul_rn(w.a[2 * NW - j][j], tw[2 * NW - j]));
+    }
+    if (q == 0) o = __fadd_rn(o, __fmul_rn(eps2, b0));
+    if (q == 1) o = __fadd_rn(o, __fmul_rn(eps2, b1));
+    if (q == n1 - 2) o = __fadd_rn(o, __fmul_rn(eps2, b2));
+    if (q == n1 - 1) o = __fadd_rn(o, __fmul_rn(eps2, b3));
+    tr[q] = o;
+  }
+}
+
+}  // namespace pwd

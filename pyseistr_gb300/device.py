@@ -1,0 +1,147 @@
+"""Device-resident entry points: flat, column-major float32 CUDA tensors in,
+CUDA tensors out, enqueued on the current torch stream without host
+synchronisation.
+
+These are thin wrappers of the C ABI (include/pwd_gb300.h); each mirrors the
+low-level reference entry it replaces (dipc, csomean2d, csomf2d, csomean3d,
+csomf3d, csoint3d) with the sizes passed explicitly.  Workspaces come from
+torch's caching allocator unless the caller passes one.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _as_flat(t, n, name):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != torch.float32:
+        raise TypeError(f"{name} must be float32, got {t.dtype}")
+    if t.numel() != n:
+        raise ValueError(f"{name}: size {t.numel()} does not match the section size {n}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous (flat column-major)")
+    return t.view(-1)
+
+
+def _workspace(nbytes, device, ws=None):
+    if nbytes == 0:
+        raise ValueError("invalid sizes or parameters (workspace query returned 0)")
+    if ws is not None:
+        if ws.numel() * ws.element_size() < nbytes or ws.data_ptr() % 256:
+            raise ValueError(f"workspace must be >= {nbytes} bytes and 256-byte aligned")
+        return ws
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+def dip(data, n1, n2, n3, niter=5, liter=20, order=2, rect=(10, 10, 1), mask=None, out=None,
+        workspace=None):
+    """Slopes of a section (n3 == 1, [n]) or cube (n3 > 1, [2n]: inline then crossline)."""
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data = _as_flat(data, n, "data")
+    if mask is not None:
+        mask = _as_flat(mask, n, "mask")
+    rc = (ctypes.c_int * 3)(*[int(r) for r in rect])
+    nbytes = L.pwd_dip_workspace_size(n1, n2, n3, order, rc, int(mask is not None))
+    ws = _workspace(nbytes, data.device, workspace)
+    nout = n if n3 == 1 else 2 * n
+    if out is None:
+        out = torch.empty(nout, dtype=torch.float32, device=data.device)
+    _lib.check(L.pwd_dip(_ptr(data), _ptr(mask), _ptr(out), n1, n2, n3, niter, liter, order, rc,
+                         _ptr(ws), ws.numel(), _stream()), "dip")
+    return out
+
+
+def somean2d(data, dip_, n1, n2, n3, ns, order, eps, adj=0, out=None, workspace=None):
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data, dip_ = _as_flat(data, n, "data"), _as_flat(dip_, n, "dip")
+    ws = _workspace(L.pwd_somean2d_workspace_size(n1, n2, n3, ns, order), data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_somean2d(_ptr(data), _ptr(dip_), _ptr(out), n1, n2, n3, ns, order, int(adj),
+                              float(eps), _ptr(ws), ws.numel(), _stream()), "somean2d")
+    return out
+
+
+def somf2d(data, dip_, n1, n2, n3, ns, nmf, option, order, eps, out=None, workspace=None):
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data, dip_ = _as_flat(data, n, "data"), _as_flat(dip_, n, "dip")
+    ws = _workspace(L.pwd_somf2d_workspace_size(n1, n2, n3, ns, nmf, option, order), data.device,
+                    workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_somf2d(_ptr(data), _ptr(dip_), _ptr(out), n1, n2, n3, ns, nmf, option, order,
+                            float(eps), _ptr(ws), ws.numel(), _stream()), "somf2d")
+    return out
+
+
+def somean3d(data, dipi, dipx, n1, n2, n3, r1, r2, order, eps=0.01, out=None, workspace=None):
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data = _as_flat(data, n, "data")
+    dipi, dipx = _as_flat(dipi, n, "dipi"), _as_flat(dipx, n, "dipx")
+    ws = _workspace(L.pwd_somean3d_workspace_size(n1, n2, n3, r1, r2, order), data.device,
+                    workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_somean3d(_ptr(data), _ptr(dipi), _ptr(dipx), _ptr(out), n1, n2, n3, r1, r2,
+                              order, float(eps), _ptr(ws), ws.numel(), _stream()), "somean3d")
+    return out
+
+
+def somf3d(data, dipi, dipx, n1, n2, n3, r1, r2, nmf, option, order, eps=0.01, out=None,
+           workspace=None):
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data = _as_flat(data, n, "data")
+    dipi, dipx = _as_flat(dipi, n, "dipi"), _as_flat(dipx, n, "dipx")
+    ws = _workspace(L.pwd_somf3d_workspace_size(n1, n2, n3, r1, r2, nmf, option, order),
+                    data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_somf3d(_ptr(data), _ptr(dipi), _ptr(dipx), _ptr(out), n1, n2, n3, r1, r2, nmf,
+                            option, order, float(eps), _ptr(ws), ws.numel(), _stream()), "somf3d")
+    return out
+
+
+def soint3d(data, mask, dipi, dipx, n1, n2, n3, order=1, nj1=1, nj2=1, niter=100, drift=0,
+            seed=202223, hasmask=1, var=0.0, out=None, workspace=None):
+    L = _lib.load()
+    n = n1 * n2 * n3
+    data = _as_flat(data, n, "data")
+    mask = _as_flat(mask, n, "mask") if mask is not None else None
+    dipi, dipx = _as_flat(dipi, n, "dipi"), _as_flat(dipx, n, "dipx")
+    ws = _workspace(L.pwd_soint3d_workspace_size(n1, n2, n3, order), data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_soint3d(_ptr(data), _ptr(mask), _ptr(dipi), _ptr(dipx), _ptr(out), n1, n2, n3,
+                             order, nj1, nj2, niter, int(drift), int(seed), int(hasmask),
+                             float(var), _ptr(ws), ws.numel(), _stream()), "soint3d")
+    return out
+
+
+def panel_median(panels, nmf, option=1, out=None, workspace=None):
+    """Median row (np-1)/2 of sprayed panels [ntr][np][n1] -> [ntr][n1]
+    (the reference's mf/svmf as the somf filters use them)."""
+    L = _lib.load()
+    if not isinstance(panels, torch.Tensor) or not panels.is_cuda or panels.dim() != 3:
+        raise TypeError("panels must be a 3-D CUDA tensor [ntr][np][n1]")
+    if panels.dtype != torch.float32 or not panels.is_contiguous():
+        raise TypeError("panels must be contiguous float32")
+    ntr, npn, n1 = panels.shape
+    ws = _workspace(L.pwd_panel_median_workspace_size(n1, npn, ntr, nmf, option), panels.device,
+                    workspace)
+    out = torch.empty((ntr, n1), dtype=torch.float32, device=panels.device) if out is None else out
+    _lib.check(L.pwd_panel_median(_ptr(panels), _ptr(out), n1, npn, ntr, nmf, option, _ptr(ws),
+                                  ws.numel(), _stream()), "panel_median")
+    return out

@@ -1,0 +1,74 @@
+"""The C-ABI library loads and exports every entry point include/pwd_gb300.h
+declares; host-side argument checks and workspace queries (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pyseistr_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "pwd_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pwd_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for n in ("pwd_dip", "pwd_somean2d", "pwd_somf2d", "pwd_somean3d", "pwd_somf3d",
+              "pwd_soint3d"):
+        assert n in names and n + "_workspace_size" in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings_and_version():
+    lib = _lib.load()
+    assert lib.pwd_version() >= 100
+    for s in range(5):
+        assert lib.pwd_status_string(s)
+    with pytest.raises(ValueError):
+        _lib.check(_lib.PWD_EINVAL, "x")
+    with pytest.raises(_lib.PwdError):
+        _lib.check(_lib.PWD_EWORKSPACE, "x")
+
+
+def test_workspace_queries():
+    lib = _lib.load()
+    rect = (ctypes.c_int * 3)(10, 10, 1)
+    a = lib.pwd_dip_workspace_size(501, 100, 1, 2, rect, 0)
+    b = lib.pwd_dip_workspace_size(501, 100, 1, 2, rect, 1)
+    assert a >= 11 * 501 * 100 * 4 and b > a
+    assert lib.pwd_dip_workspace_size(0, 100, 1, 2, rect, 0) == 0
+    assert lib.pwd_somean2d_workspace_size(501, 100, 1, 8, 2) >= 17 * 501 * 100 * 4
+    assert lib.pwd_somf2d_workspace_size(501, 100, 1, 8, 17, 1, 2) > 0
+    assert lib.pwd_somf2d_workspace_size(501, 100, 1, 8, 0, 1, 2) == 0   # empty window
+    assert lib.pwd_somf2d_workspace_size(501, 100, 1, 1, 3, 2, 2) == 0   # svmf needs nmf >= 5
+    assert lib.pwd_somean3d_workspace_size(201, 60, 60, 4, 4, 2) >= 81 * 201 * 3600 * 4
+    assert lib.pwd_somean3d_workspace_size(201, 60, 60, 11, 4, 2) == 0   # radius cap
+    assert lib.pwd_soint3d_workspace_size(64, 32, 32, 2) > 0
+    assert lib.pwd_soint3d_workspace_size(64, 32, 32, 9) == 0
+
+
+def test_calls_reject_bad_arguments_before_touching_the_gpu():
+    lib = _lib.load()
+    rect = (ctypes.c_int * 3)(10, 10, 1)
+    fake = ctypes.c_void_p(256)  # never dereferenced: rejected by the host checks
+    assert lib.pwd_dip(None, None, fake, 10, 10, 1, 5, 10, 2, rect, fake, 1 << 20, None) == _lib.PWD_EINVAL
+    assert lib.pwd_dip(fake, None, fake, 10, 10, 1, 5, 10, 9, rect, fake, 1 << 20, None) == _lib.PWD_ENOTSUP
+    assert lib.pwd_dip(fake, None, fake, 4, 10, 1, 5, 10, 2, rect, fake, 1 << 20, None) == _lib.PWD_EINVAL
+    assert lib.pwd_dip(fake, None, fake, 100, 10, 1, 5, 10, 2, rect, fake, 16, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_dip(fake, None, fake, 100, 10, 1, 5, 10, 2, rect, ctypes.c_void_p(300), 1 << 30, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_somean2d(fake, fake, fake, 3, 10, 1, 2, 2, 0, 0.01, fake, 1 << 20, None) == _lib.PWD_EINVAL
+    assert lib.pwd_somf2d(fake, fake, fake, 50, 10, 1, 2, 5, 1, 2, 0.01, fake, 16, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_somf3d(fake, fake, fake, fake, 50, 10, 10, 2, 2, 200, 1, 2, 0.01, fake, 1 << 30, None) == _lib.PWD_ENOTSUP
+    assert lib.pwd_soint3d(fake, None, fake, fake, fake, 8, 8, 8, 2, 1, 1, 5, 0, 1, 1, 0.0, fake, 1 << 30, None) == _lib.PWD_EINVAL

@@ -1,0 +1,76 @@
+"""GPU results against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference C)."""
+import numpy as np
+import pytest
+
+from golden_cases import ids, load
+from gpu_util import DIP_TOL, need_gpu, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+CASES = load("2d") + load("3d")
+
+
+def run_gpu(fn, p, a):
+    import pyseistr_gb300 as ps
+
+    if fn == "dip":
+        d = a["d"]
+        mask = a.get("mask")
+        if d.ndim == 2:
+            return (ps.dip2dc(d, p["niter"], p["liter"], p["order"], rect=p["rect"], mask=mask),)
+        return ps.dip3dc(d, p["niter"], p["liter"], p["order"], rect=p["rect"], mask=mask)
+    if fn == "somean2d":
+        return (ps.somean2dc(a["d"], a["p"], p["ns"], p["order"], p["eps"], p["adj"]),)
+    if fn == "somf2d":
+        d = a["d"]
+        n1, n2 = d.shape[0], d.shape[1]
+        n3 = d.shape[2] if d.ndim == 3 else 1
+        out = ps.csomf2d(d.flatten(order="F"), a["p"].flatten(order="F"), n1, n2, n3, p["ns"],
+                         p["nmf"], p["option"], p["order"], p["eps"], 0)
+        return (out.reshape(d.shape, order="F"),)
+    if fn == "somean3d":
+        return (ps.somean3dc(a["d"], a["pi"], a["px"], p["r1"], p["r2"], 0.01, p["order"]),)
+    if fn == "somf3d":
+        d = a["d"]
+        n1, n2, n3 = d.shape
+        out = ps.csomf3d(d.flatten(order="F"), a["pi"].flatten(order="F"),
+                         a["px"].flatten(order="F"), n1, n2, n3, p["r1"], p["r2"], p["nmf"],
+                         p["option"], p["order"], 0.01, 0)
+        return (out.reshape(d.shape, order="F"),)
+    if fn == "soint3d":
+        return (ps.soint3dc(a["d"], a["mask"], a["pi"], a["px"], order=p["order"],
+                            niter=p["niter"], drift=p["drift"], seed=p["seed"], var=p["var"]),)
+    raise KeyError(fn)
+
+
+def expected(a):
+    return (a["out"],) if "out" in a else (a["out_i"], a["out_x"])
+
+
+@pytest.mark.parametrize("case", CASES, ids=ids(CASES))
+def test_matches_reference(case):
+    need_gpu()
+    _, fn, p, a = case
+    for got, want in zip(run_gpu(fn, p, a), expected(a)):
+        got = np.asarray(got)
+        assert got.shape == want.shape and got.dtype == np.float32
+        if fn == "dip":
+            assert rel_l2(got, want) <= DIP_TOL
+        else:
+            assert np.array_equal(got, want), f"max |diff| {np.abs(got - want).max():.3e}"
+
+
+def test_dip_golden_bit_exact_count():
+    """Report how many slope cases reproduce the reference bit for bit."""
+    need_gpu()
+    exact = 0
+    total = 0
+    for _, fn, p, a in CASES:
+        if fn != "dip":
+            continue
+        for got, want in zip(run_gpu(fn, p, a), expected(a)):
+            total += 1
+            exact += int(np.array_equal(np.asarray(got), want))
+    print(f"dip cases bit-exact: {exact}/{total}")
+    assert exact >= 1
