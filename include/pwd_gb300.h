@@ -69,6 +69,27 @@ int pwd_dip(const float *data, const float *mask, float *dip_out, int n1, int n2
             size_t workspace_bytes, pwd_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Batched slope estimation over many independent sections of uneven size
+ * (the patch / DAS-window workflows), in one fixed launch sequence: every
+ * kernel covers all sections.  Same results as one pwd_dip call per
+ * section.  The section table is read from host memory during the call.
+ * No single reference entry point: it replaces a loop of dipc calls
+ * (dip_cfuns.c:1694) over the sections.
+ */
+typedef struct {
+  long offset;     /* element offset of the section in data (and mask) */
+  long out_offset; /* element offset of its slopes in dip_out (2n for 3-D) */
+  int n1, n2, n3;
+} pwd_section;
+
+size_t pwd_dip_batch_workspace_size(const pwd_section *sections, int nsec, int order,
+                                    const int rect[3], int has_mask);
+int pwd_dip_batch(const float *data, const float *mask, float *dip_out,
+                  const pwd_section *sections, int nsec, int niter, int liter, int order,
+                  const int rect[3], void *workspace, size_t workspace_bytes,
+                  pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * 2-D structure-oriented mean, slice by slice over n3.
  * Replaces csomean2d, pyseistr/src/sof_cfuns.c:1433-1531 (somean2dc,
  * somean2d.py:36): triangle-weighted spray mean normalised by the spray of
@@ -90,6 +111,21 @@ size_t pwd_somf2d_workspace_size(int n1, int n2, int n3, int ns, int nmf, int op
 int pwd_somf2d(const float *data, const float *dip, float *out, int n1, int n2, int n3, int ns,
                int nmf, int option, int order, float eps, void *workspace,
                size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Batched 2-D structure-oriented filters over many sections of uneven size
+ * in one launch sequence: filter 1 = mean (csomean2d adj=0), 2 = adjoint
+ * mean (adj=1), 3 = median (csomf2d with nmf, option).  data and dip share
+ * the sections' offsets; the filtered output of section k is written at
+ * sections[k].out_offset.  Same results as one call per section; replaces
+ * a loop of csomean2d / csomf2d calls (sof_cfuns.c:1433, :1534).
+ */
+size_t pwd_sofilter2d_batch_workspace_size(const pwd_section *sections, int nsec, int ns,
+                                           int order, int filter, int nmf, int option);
+int pwd_sofilter2d_batch(const float *data, const float *dip, float *out,
+                         const pwd_section *sections, int nsec, int ns, int order, int filter,
+                         int nmf, int option, float eps, void *workspace,
+                         size_t workspace_bytes, pwd_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * 3-D structure-oriented mean over the (2*r1+1)*(2*r2+1) spray.
@@ -136,6 +172,30 @@ int pwd_soint3d(const float *data, const float *mask, const float *dip_inline,
                 const float *dip_xline, float *out, int n1, int n2, int n3, int order, int nj1,
                 int nj2, int niter, int drift, int seed, int hasmask, float var,
                 void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Launch accounting and kernel timing (no counterpart in the reference,
+ * which has no GPU code).  Kernel families:
+ */
+enum {
+  PWD_FAM_PWD = 0,      /* PWD residual / derivative / line-search trials  */
+  PWD_FAM_CG = 1,       /* shaping-CG vector updates and reductions        */
+  PWD_FAM_TRIANGLE = 2, /* triangle-smoothing line sweeps                  */
+  PWD_FAM_SPRAY = 3,    /* plane-wave spray chains / trees                 */
+  PWD_FAM_FILTER = 4,   /* spray mean / median reductions                  */
+  PWD_FAM_SOINT = 5,    /* interpolation operator and CG                   */
+  PWD_FAM_OTHER = 6,
+  PWD_NFAM = 7
+};
+/* Number of kernels the library has launched since it was loaded. */
+unsigned long long pwd_launch_count(void);
+/* Start recording a CUDA event pair around every launch (process-wide; for
+ * benchmarks, not for concurrent use from several threads). */
+void pwd_profile_start(void);
+/* Stop recording; synchronises the recorded events and writes, per family,
+ * the summed kernel time in ms and the number of launches (arrays of
+ * `nfam` entries).  Returns the number of launches recorded. */
+int pwd_profile_stop(double *ms, int *launches, int nfam);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,9 @@ sm_103a kernels of libpwd_gb300.so:
     soint3dc                       3-D structure-oriented interpolation
     dipc, csomean2d, csomf2d,      the reference's low-level positional
     csomean3d, csomf3d, csoint3d   entries
+    dip2dc_batch, somean2dc_batch, many sections of uneven size in one
+    somf2dc_batch,                 launch sequence (same results as one
+    dip_somean2d_batch             call per section)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -19,12 +22,16 @@ from .api import (  # noqa: F401
     csomf2d,
     csomf3d,
     dip2dc,
+    dip2dc_batch,
+    dip_somean2d_batch,
     dip3dc,
     dipc,
     soint3dc,
     somean2dc,
+    somean2dc_batch,
     somean3dc,
     somf2dc,
+    somf2dc_batch,
     somf3dc,
 )
 

@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpwd_gb300.so")
 
 PWD_OK, PWD_EINVAL, PWD_EWORKSPACE, PWD_ECUDA, PWD_ENOTSUP = range(5)
+FAMILIES = ["pwd", "cg", "triangle", "spray", "filter", "soint", "other"]
 
 # Every symbol the header declares, with its ctypes signature.
 _P, _I, _F, _S = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
@@ -20,6 +21,10 @@ SIGNATURES = {
     "pwd_status_string": ([_I], ctypes.c_char_p),
     "pwd_dip_workspace_size": ([_I, _I, _I, _I, _P, _I], _S),
     "pwd_dip": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _S, _P], _I),
+    "pwd_dip_batch_workspace_size": ([_P, _I, _I, _P, _I], _S),
+    "pwd_dip_batch": ([_P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _S, _P], _I),
+    "pwd_sofilter2d_batch_workspace_size": ([_P, _I, _I, _I, _I, _I, _I], _S),
+    "pwd_sofilter2d_batch": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_somean2d_workspace_size": ([_I, _I, _I, _I, _I], _S),
     "pwd_somean2d": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_somf2d_workspace_size": ([_I, _I, _I, _I, _I, _I, _I], _S),
@@ -30,11 +35,20 @@ SIGNATURES = {
     "pwd_somf3d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_panel_median_workspace_size": ([_I, _I, ctypes.c_long, _I, _I], _S),
     "pwd_panel_median": ([_P, _P, _I, _I, ctypes.c_long, _I, _I, _P, _S, _P], _I),
+    "pwd_launch_count": ([], ctypes.c_ulonglong),
+    "pwd_profile_start": ([], None),
+    "pwd_profile_stop": ([_P, _P, _I], _I),
     "pwd_soint3d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_soint3d": ([_P, _P, _P, _P, _P] + [_I] * 10 + [_F, _P, _S, _P], _I),
 }
 
 _lib = None
+
+
+class Section(ctypes.Structure):
+    """pwd_section: one section of a batch."""
+    _fields_ = [("offset", ctypes.c_long), ("out_offset", ctypes.c_long), ("n1", ctypes.c_int),
+                ("n2", ctypes.c_int), ("n3", ctypes.c_int)]
 
 
 class PwdError(RuntimeError):
@@ -68,3 +82,26 @@ def check(status: int, what: str) -> None:
     if status == PWD_EINVAL:
         raise ValueError(msg)
     raise PwdError(msg)
+
+
+def launch_count() -> int:
+    """Kernels the library has launched since it was loaded."""
+    return int(load().pwd_launch_count())
+
+
+class profile:
+    """Context manager timing every library launch with CUDA events:
+    ``with profile() as p: ...`` then ``p.ms[family]``, ``p.launches[family]``."""
+
+    def __enter__(self):
+        load().pwd_profile_start()
+        return self
+
+    def __exit__(self, *exc):
+        n = len(FAMILIES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int * n)()
+        load().pwd_profile_stop(ms, cnt, n)
+        self.ms = {f: ms[i] for i, f in enumerate(FAMILIES)}
+        self.launches = {f: cnt[i] for i, f in enumerate(FAMILIES)}
+        return False

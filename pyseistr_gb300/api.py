@@ -197,3 +197,61 @@ def soint3dc(din, mask, dipi, dipx, order=1, niter=100, njs=[1, 1], drift=0, see
     out = D.soint3d(d, m, pi, px, n1, n2, n3, order, njs[0], njs[1], niter, drift, seed, hasmask,
                     var)
     return _from_dev_flat(out, (n1, n2, n3), as_t)
+
+
+# --------------------------------------------------------------------------
+# batched entries: many sections of uneven size in one launch sequence
+# --------------------------------------------------------------------------
+def _pack(sections):
+    flat = np.concatenate([np.asarray(s, np.float32).reshape(-1, order="F") for s in sections])
+    t = torch.from_numpy(flat).pin_memory().to(_dev(), non_blocking=True)
+    return t
+
+
+def _unpack(t, shapes):
+    host = t.cpu().numpy()
+    out, k = [], 0
+    for sh in shapes:
+        n = int(np.prod(sh))
+        out.append(host[k:k + n].reshape(sh, order="F"))
+        k += n
+    return out
+
+
+def dip2dc_batch(sections, niter=5, liter=20, order=2, rect=[10, 10, 1]):
+    """dip2dc over a list of 2-D sections, all in one launch sequence;
+    returns the list of slopes (each equal to dip2dc of its section)."""
+    shapes = [tuple(s.shape) for s in sections]
+    out = D.dip_batch(_pack(sections), shapes, niter, liter, order, rect)
+    return _unpack(out, shapes)
+
+
+def somean2dc_batch(sections, dips, ns, order, eps, adj=0):
+    """somean2dc over a list of 2-D sections and their slopes."""
+    shapes = [tuple(s.shape) for s in sections]
+    out = D.sofilter2d_batch(_pack(sections), _pack(dips), shapes, ns, order, eps,
+                             filter=D.FILTER_MEAN_ADJ if adj else D.FILTER_MEAN)
+    return _unpack(out, shapes)
+
+
+def somf2dc_batch(sections, dips, ns, order, eps, option=1):
+    """somf2dc over a list of 2-D sections and their slopes."""
+    shapes = [tuple(s.shape) for s in sections]
+    out = D.sofilter2d_batch(_pack(sections), _pack(dips), shapes, ns, order, eps,
+                             filter=D.FILTER_MEDIAN, nmf=2 * ns + 1, option=option)
+    return _unpack(out, shapes)
+
+
+def dip_somean2d_batch(sections, niter=5, liter=10, order=2, rect=[10, 10, 1], ns=6, eps=0.01,
+                       median=False):
+    """Slope estimation followed by the structure-oriented mean (or median)
+    of many sections: one upload, both stages on the device, one download.
+    Returns (slopes, filtered) lists."""
+    shapes = [tuple(s.shape) for s in sections]
+    d = _pack(sections)
+    p = D.dip_batch(d, shapes, niter, liter, order, rect)
+    if median:
+        f = D.sofilter2d_batch(d, p, shapes, ns, order, eps, filter=D.FILTER_MEDIAN)
+    else:
+        f = D.sofilter2d_batch(d, p, shapes, ns, order, eps, filter=D.FILTER_MEAN)
+    return _unpack(p, shapes), _unpack(f, shapes)

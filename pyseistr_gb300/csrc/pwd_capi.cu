@@ -1,5 +1,68 @@
-// Library-wide entry points of the C ABI (version and status strings).
+// Library-wide entry points of the C ABI: version, status strings, launch
+// accounting and kernel-family timing with CUDA events.
+#include <atomic>
+#include <mutex>
+#include <vector>
+
 #include "pwd_common.cuh"
+
+namespace pwd {
+namespace {
+
+std::atomic<unsigned long long> g_launches{0};
+
+struct Rec {
+  int fam;
+  cudaEvent_t a, b;
+};
+
+struct Profiler {
+  std::mutex mu;
+  bool on = false;
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+
+Profiler& prof() {
+  static Profiler p;
+  return p;
+}
+
+thread_local cudaEvent_t t_pending = nullptr;
+
+}  // namespace
+
+void prof_begin(int fam, cudaStream_t st) {
+  (void)fam;
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  Profiler& p = prof();
+  if (!p.on) return;
+  std::lock_guard<std::mutex> lk(p.mu);
+  t_pending = p.get();
+  cudaEventRecord(t_pending, st);
+}
+
+void prof_end(int fam, cudaStream_t st) {
+  Profiler& p = prof();
+  if (!p.on || !t_pending) return;
+  std::lock_guard<std::mutex> lk(p.mu);
+  cudaEvent_t b = p.get();
+  cudaEventRecord(b, st);
+  p.recs.push_back({fam, t_pending, b});
+  t_pending = nullptr;
+}
+
+}  // namespace pwd
 
 extern "C" int pwd_version(void) { return 100; }  // 0.1.0
 
@@ -12,4 +75,37 @@ extern "C" const char* pwd_status_string(int status) {
     case PWD_ENOTSUP: return "parameter outside what this build supports";
   }
   return "unknown status";
+}
+
+extern "C" unsigned long long pwd_launch_count(void) { return pwd::g_launches.load(); }
+
+extern "C" void pwd_profile_start(void) {
+  pwd::Profiler& p = pwd::prof();
+  std::lock_guard<std::mutex> lk(p.mu);
+  p.on = true;
+}
+
+extern "C" int pwd_profile_stop(double* ms, int* launches, int nfam) {
+  pwd::Profiler& p = pwd::prof();
+  std::lock_guard<std::mutex> lk(p.mu);
+  p.on = false;
+  for (int f = 0; f < nfam; f++) {
+    if (ms) ms[f] = 0.0;
+    if (launches) launches[f] = 0;
+  }
+  int n = 0;
+  for (auto& r : p.recs) {
+    cudaEventSynchronize(r.b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    if (r.fam >= 0 && r.fam < nfam) {
+      if (ms) ms[r.fam] += t;
+      if (launches) launches[r.fam] += 1;
+    }
+    p.pool.push_back(r.a);
+    p.pool.push_back(r.b);
+    n++;
+  }
+  p.recs.clear();
+  return n;
 }

@@ -250,7 +250,19 @@ struct Carver {
 
 inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? PWD_OK : PWD_ECUDA; }
 
+// Launch accounting (pwd_capi.cu): every kernel launch goes through
+// PWD_KERNEL so that it is counted and, while profiling, timed.
+void prof_begin(int fam, cudaStream_t st);
+void prof_end(int fam, cudaStream_t st);
+
 }  // namespace pwd
+
+#define PWD_KERNEL(fam, st, ...)   \
+  do {                             \
+    pwd::prof_begin((fam), (st));  \
+    __VA_ARGS__;                   \
+    pwd::prof_end((fam), (st));    \
+  } while (0)
 
 #define PWD_LAUNCH_CHECK()                            \
   do {                                                \

@@ -2,41 +2,107 @@
 //
 // Restates dipc / dip3 / ps_divne / ps_conjgrad / ps_trianglen_lop of
 // pyseistr/src/dip_cfuns.c (:1694-1989, :1619-1691, :796-827, :257-383,
-// :672-712) as stream-ordered kernels.  All scalar control (CG convergence,
-// line-search acceptance) lives on the device, so a call enqueues a fixed
-// launch sequence and never synchronises with the host; kernels after a
-// decided exit read a device flag and return at once.
+// :672-712) as stream-ordered kernels over a batch of independent sections.
+// Every launch covers all sections of the batch: elementwise work is split
+// into tiles that never straddle a section, reductions are summed per
+// section in a fixed tile order (deterministic, no floating-point atomics),
+// and all scalar control (CG convergence, line-search acceptance) is per
+// section on the device.  A call therefore enqueues a fixed launch sequence
+// that depends only on (niter, liter, the smoothed axes), never synchronises
+// with the host and can be captured in a CUDA graph; launches for a section
+// that has left a loop return at once.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <vector>
 
+#include "pwd_batch.cuh"
 #include "pwd_common.cuh"
 
 namespace pwd {
 namespace {
 
-constexpr int kBlock = 256;
-
-struct Geo {
-  int n1, n2, n3;
-  long n;
-  long ip;   // neighbour offset: n1 (inline) or n1*n2 (crossline)
-  int dip;   // 1 inline, 2 crossline
-};
+constexpr int kTile = 2048;  // samples per elementwise tile
+constexpr int kTileThreads = 256;
 
 struct DipScalars {
-  double usum, usum2, den2, norm2, r0;
+  double usum, usum2, r0, norm2;
   double gn, gnp, g0, alpha, step;
   int zero, cg_done, ls_done, ls_trials, cg_iters;
   unsigned cnt[8];
 };
 
-__device__ __forceinline__ bool pwd_valid(const Geo& g, long i, int nw) {
-  int i1 = (int)(i % g.n1);
-  long r = i / g.n1;
-  if (i1 < nw || i1 >= g.n1 - nw) return false;
-  if (g.dip == 1) return (int)(r % g.n2) < g.n2 - 1;
-  return (int)(r / g.n2) < g.n3 - 1;
+struct DipBatch {
+  const SecDesc* secs;
+  const int* tile_sec;
+  int nsec, ntiles;
+  DipScalars* S;
+  double* partials;  // [ntiles][3]
+};
+
+struct DipArrays {
+  const float* u;  // data
+  float* p;        // slopes (output)
+  const uint8_t* mask;
+  float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
+};
+
+struct TileRange {
+  int sec;
+  long lo, hi;
+};
+
+__device__ __forceinline__ TileRange tile_range(const DipBatch& b, int t) {
+  TileRange r;
+  r.sec = b.tile_sec[t];
+  const SecDesc& s = b.secs[r.sec];
+  r.lo = (long)(t - s.tile0) * kTile;
+  r.hi = min(s.n, r.lo + kTile);
+  return r;
+}
+
+// Offset of the slopes being estimated: inline ones first, crossline after.
+__device__ __forceinline__ long pout_of(const SecDesc& s, int dip) {
+  return s.pout + (dip == 2 ? s.n : 0);
+}
+
+// Sum of K doubles over the tiles of one section; true in the block of the
+// section's last tile to finish, which receives the totals (summed over the
+// section's tiles in tile order).
+template <int K>
+__device__ __forceinline__ bool sec_sum_last(dvec<K> x, const DipBatch& b, int t, const SecDesc& s,
+                                             unsigned* counter, dvec<K>& tot) {
+  __shared__ bool s_last;
+  dvec<K> blk = block_sum<K>(x);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) b.partials[(size_t)t * 3 + k] = blk.v[k];
+    __threadfence();
+    unsigned tk = atomicAdd(counter, 1u);
+    s_last = (tk == (unsigned)(s.ntile - 1));
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  dvec<K> y;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < s.ntile; i += blockDim.x)
+      v += __ldcg(b.partials + (size_t)(s.tile0 + i) * 3 + k);
+    y.v[k] = v;
+  }
+  tot = block_sum<K>(y);
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+__device__ __forceinline__ bool pwd_valid(const SecDesc& s, long i, int nw, int dip) {
+  int i1 = (int)(i % s.n1);
+  long r = i / s.n1;
+  if (i1 < nw || i1 >= s.n1 - nw) return false;
+  if (dip == 1) return (int)(r % s.n2) < s.n2 - 1;
+  return (int)(r / s.n2) < s.n3 - 1;
 }
 
 // allpass1/allpass2 at one sample (dip_cfuns.c:1135-1200, :1399-1465).
@@ -57,27 +123,44 @@ __device__ __forceinline__ float pwd_at(const float* __restrict__ u, long i, lon
   return y;
 }
 
+__device__ __forceinline__ long nb_offset(const SecDesc& s, int dip) {
+  return dip == 1 ? (long)s.n1 : (long)s.n1 * s.n2;
+}
+
+// 2-D sections of a batch that also holds cubes have no crossline slope.
+__device__ __forceinline__ bool no_pass(const SecDesc& s, int dip) { return dip == 2 && s.n3 == 1; }
+
 template <int NW>
-__global__ void k_residual(const float* __restrict__ u, const float* __restrict__ p,
-                           float* __restrict__ u2, Geo g, ApCoef c) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < g.n;
-       i += (long)gridDim.x * blockDim.x)
-    u2[i] = pwd_valid(g, i, NW) ? pwd_at<NW, false>(u, i, g.ip, c, p[i]) : 0.f;
+__global__ void k_residual(DipArrays a, DipBatch b, ApCoef c, int dip) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  if (no_pass(s, dip)) return;
+  const float* u = a.u + s.off;
+  const float* p = a.p + pout_of(s, dip);
+  float* u2 = a.u2 + s.off;
+  const long ip = nb_offset(s, dip);
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
+    u2[i] = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false>(u, i, ip, c, p[i]) : 0.f;
 }
 
 // One Gauss-Newton linearisation (dip3 :1645-1665 up to ps_divne's first
 // normalisation, ps_divne :796-815): derivative filter, residual energy,
-// mask, 1/hypot(den,1) scaling and sum of den^2.
+// mask, 1/hypot(den,1) scaling and the sum of den^2.
 template <int NW>
-__global__ void k_prep(const float* __restrict__ u, const float* __restrict__ p,
-                       float* __restrict__ u2, float* __restrict__ u1, float* __restrict__ p0,
-                       const uint8_t* __restrict__ mask, Geo g, ApCoef c, DipScalars* S,
-                       double* partials) {
+__global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  if (no_pass(s, dip)) return;
+  const float* u = a.u + s.off;
+  const float* p = a.p + pout_of(s, dip);
+  float *u2 = a.u2 + s.off, *u1 = a.u1 + s.off, *p0 = a.p0 + s.off;
+  const uint8_t* mask = a.mask ? a.mask + s.off : nullptr;
+  const long ip = nb_offset(s, dip);
   dvec<2> acc = {{0.0, 0.0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < g.n;
-       i += (long)gridDim.x * blockDim.x) {
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float pi = p[i];
-    float d = pwd_valid(g, i, NW) ? pwd_at<NW, true>(u, i, g.ip, c, pi) : 0.f;
+    float d = pwd_valid(s, i, NW, dip) ? pwd_at<NW, true>(u, i, ip, c, pi) : 0.f;
     float r = u2[i];
     acc.v[0] += (double)r * (double)r;
     p0[i] = pi;
@@ -92,12 +175,12 @@ __global__ void k_prep(const float* __restrict__ u, const float* __restrict__ p,
     u1[i] = den;
     acc.v[1] += (double)den * (double)den;
   }
+  DipScalars* S = b.S + tr.sec;
   dvec<2> tot;
-  if (grid_sum_last<2>(acc, partials, &S->cnt[0], tot) && threadIdx.x == 0) {
+  if (sec_sum_last<2>(acc, b, t, s, &S->cnt[0], tot) && threadIdx.x == 0) {
     S->usum = tot.v[0];
-    S->den2 = tot.v[1];
     S->zero = (tot.v[1] == 0.0);
-    S->norm2 = S->zero ? 0.0 : sqrt((double)g.n / tot.v[1]);
+    S->norm2 = S->zero ? 0.0 : sqrt((double)s.n / tot.v[1]);
     S->cg_done = S->zero;
     S->ls_done = 0;
     S->ls_trials = 0;
@@ -106,57 +189,94 @@ __global__ void k_prep(const float* __restrict__ u, const float* __restrict__ p,
 }
 
 // ps_divne :817-826 second scaling, and ps_conjgrad :267-303 start.
-__global__ void k_scale(float* __restrict__ num, float* __restrict__ den, float* __restrict__ r,
-                        float* __restrict__ pcg, float* __restrict__ x, long n, DipScalars* S,
-                        double* partials) {
-  dvec<1> acc = {{0.0}};
+__global__ void k_scale(DipArrays a, DipBatch b, int dip) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  if (no_pass(s, dip)) return;
+  DipScalars* S = b.S + tr.sec;
   const bool zero = S->zero;
   const double nrm = S->norm2;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
+  float *num = a.u2 + s.off, *den = a.u1 + s.off, *r = a.r + s.off, *pcg = a.pcg + s.off,
+        *x = a.dp + s.off;
+  dvec<1> acc = {{0.0}};
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     x[i] = 0.f;
     if (zero) continue;
-    float a = __double2float_rn(__dmul_rn((double)num[i], nrm));
-    float b = __double2float_rn(__dmul_rn((double)den[i], nrm));
-    num[i] = a;
-    den[i] = b;
-    float ri = -a;
+    float va = __double2float_rn(__dmul_rn((double)num[i], nrm));
+    float vb = __double2float_rn(__dmul_rn((double)den[i], nrm));
+    num[i] = va;
+    den[i] = vb;
+    float ri = -va;
     r[i] = ri;
     pcg[i] = 0.f;
     acc.v[0] += (double)ri * (double)ri;
   }
   dvec<1> tot;
-  if (grid_sum_last<1>(acc, partials, &S->cnt[1], tot) && threadIdx.x == 0) {
+  if (sec_sum_last<1>(acc, b, t, s, &S->cnt[1], tot) && threadIdx.x == 0) {
     S->r0 = tot.v[0];
     if (!S->zero && tot.v[0] == 0.0) S->cg_done = 1;
   }
 }
 
-// gx = -eps*x + W' r with eps = 1 (ps_conjgrad :306-317); written to tmp.
-__global__ void k_cg_grad(const float* __restrict__ x, const float* __restrict__ r,
-                          const float* __restrict__ w, float* __restrict__ tmp, long n,
-                          const DipScalars* S) {
+// The previous iteration's step p += a sp, x += a sx, r += a sr (:364-368),
+// then gx = -eps*x + W' r with eps = 1 (:306-317), written to tmp.  A
+// section whose CG stopped skips both (the reference breaks before the step).
+__global__ void k_cg_stepgrad(DipArrays a, DipBatch b, int iter) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const DipScalars* S = b.S + tr.sec;
   if (S->cg_done) return;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x)
-    tmp[i] = __fadd_rn(-x[i], __fmul_rn(r[i], w[i]));
+  const float st = __double2float_rn(S->step);
+  float *pcg = a.pcg + s.off, *x = a.dp + s.off, *r = a.r + s.off, *tmp = a.tmp + s.off;
+  const float *w = a.u1 + s.off, *sp = a.sp + s.off, *sx = a.sx + s.off, *sr = a.sr + s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    float xi = x[i], ri = r[i];
+    if (iter > 0) {
+      pcg[i] = __fadd_rn(pcg[i], __fmul_rn(st, sp[i]));
+      xi = __fadd_rn(xi, __fmul_rn(st, sx[i]));
+      ri = __fadd_rn(ri, __fmul_rn(st, sr[i]));
+      x[i] = xi;
+      r[i] = ri;
+    }
+    tmp[i] = __fadd_rn(-xi, __fmul_rn(ri, w[i]));
+  }
+}
+
+// The step of the last iteration when the CG ran all liter iterations.
+__global__ void k_cg_step(DipArrays a, DipBatch b) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const DipScalars* S = b.S + tr.sec;
+  if (S->cg_done) return;
+  const float st = __double2float_rn(S->step);
+  float *pcg = a.pcg + s.off, *x = a.dp + s.off, *r = a.r + s.off;
+  const float *sp = a.sp + s.off, *sx = a.sx + s.off, *sr = a.sr + s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    pcg[i] = __fadd_rn(pcg[i], __fmul_rn(st, sp[i]));
+    x[i] = __fadd_rn(x[i], __fmul_rn(st, sx[i]));
+    r[i] = __fadd_rn(r[i], __fmul_rn(st, sr[i]));
+  }
 }
 
 // gp = eps*p + S' gx; gn = gp.gp; convergence test (:319, :328-345).
-__global__ void k_cg_gp(const float* __restrict__ pcg, float* __restrict__ tmp,
-                        float* __restrict__ gp, long n, int iter, DipScalars* S,
-                        double* partials) {
+__global__ void k_cg_gp(DipArrays a, DipBatch b, int iter) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  DipScalars* S = b.S + tr.sec;
   if (S->cg_done) return;
+  const float* pcg = a.pcg + s.off;
+  float *tmp = a.tmp + s.off, *gp = a.gp + s.off;
   dvec<1> acc = {{0.0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float v = __fadd_rn(pcg[i], tmp[i]);
     gp[i] = v;
     tmp[i] = v;
     acc.v[0] += (double)v * (double)v;
   }
   dvec<1> tot;
-  if (grid_sum_last<1>(acc, partials, &S->cnt[2], tot) && threadIdx.x == 0) {
+  if (sec_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0) {
     double gn = tot.v[0];
     S->gn = gn;
     if (iter == 0) {
@@ -172,22 +292,24 @@ __global__ void k_cg_gp(const float* __restrict__ pcg, float* __restrict__ tmp,
 }
 
 // gx = S gp (in tmp), gr = W gx, conjugate directions and beta (:320-359).
-__global__ void k_cg_update(const float* __restrict__ gp, const float* __restrict__ tmp,
-                            const float* __restrict__ w, float* __restrict__ sp,
-                            float* __restrict__ sx, float* __restrict__ sr, long n, int iter,
-                            DipScalars* S, double* partials) {
+__global__ void k_cg_update(DipArrays a, DipBatch b, int iter) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  DipScalars* S = b.S + tr.sec;
   if (S->cg_done) return;
-  const float a = __double2float_rn(S->alpha);
+  const float al = __double2float_rn(S->alpha);
+  const float *gp = a.gp + s.off, *tmp = a.tmp + s.off, *w = a.u1 + s.off;
+  float *sp = a.sp + s.off, *sx = a.sx + s.off, *sr = a.sr + s.off;
   dvec<3> acc = {{0.0, 0.0, 0.0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float gx = tmp[i];
     float gr = __fadd_rn(0.f, __fmul_rn(gx, w[i]));
     float vp = gp[i], vx = gx, vr = gr;
     if (iter > 0) {
-      vp = __fadd_rn(vp, __fmul_rn(a, sp[i]));
-      vx = __fadd_rn(vx, __fmul_rn(a, sx[i]));
-      vr = __fadd_rn(vr, __fmul_rn(a, sr[i]));
+      vp = __fadd_rn(vp, __fmul_rn(al, sp[i]));
+      vx = __fadd_rn(vx, __fmul_rn(al, sx[i]));
+      vr = __fadd_rn(vr, __fmul_rn(al, sr[i]));
     }
     sp[i] = vp;
     sx[i] = vx;
@@ -197,7 +319,7 @@ __global__ void k_cg_update(const float* __restrict__ gp, const float* __restric
     acc.v[2] += (double)vx * (double)vx;
   }
   dvec<3> tot;
-  if (grid_sum_last<3>(acc, partials, &S->cnt[3], tot) && threadIdx.x == 0) {
+  if (sec_sum_last<3>(acc, b, t, s, &S->cnt[3], tot) && threadIdx.x == 0) {
     double beta = tot.v[0] + 1.0 * (tot.v[1] - tot.v[2]);
     S->step = -S->gn / beta;
     S->gnp = S->gn;
@@ -205,100 +327,141 @@ __global__ void k_cg_update(const float* __restrict__ gp, const float* __restric
   }
 }
 
-// p += alpha sp; x += alpha sx; r += alpha sr (:364-368).
-__global__ void k_cg_step(float* __restrict__ pcg, float* __restrict__ x, float* __restrict__ r,
-                          const float* __restrict__ sp, const float* __restrict__ sx,
-                          const float* __restrict__ sr, long n, const DipScalars* S) {
-  if (S->cg_done) return;
-  const float a = __double2float_rn(S->step);
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
-    pcg[i] = __fadd_rn(pcg[i], __fmul_rn(a, sp[i]));
-    x[i] = __fadd_rn(x[i], __fmul_rn(a, sx[i]));
-    r[i] = __fadd_rn(r[i], __fmul_rn(a, sr[i]));
-  }
-}
-
-// Triangle smoothing of every line along one axis, in place
-// (ps_smooth2 :616-625 = triple2 :564 + doubint2 :508 + fold2 :458), one
-// thread per line with its running sums in a line-interleaved scratch.
-struct TriAxis {
-  int axis, len, nb;
-  long nlines, stride;
-  int n1, n2;
+// Triangle smoothing of every line along one axis of every section, in
+// place (ps_smooth2 :616-625 = triple2 :564 + doubint2 :508 + fold2 :458).
+// One thread per line, serial running sums as the reference; the forward
+// sums go to a line-interleaved scratch and the backward pass folds the
+// reflections straight into the output when the triangle is not longer than
+// the line (the general fold2 loops otherwise).
+struct TriParams {
+  int axis, nb;
+  long nlines;  // lines of this axis over the batch
   float wt, w2;
 };
 
-__device__ __forceinline__ long tri_origin(const TriAxis& t, long line) {
-  if (t.axis == 0) return line * t.n1;
-  if (t.axis == 1) return (line % t.n1) + (line / t.n1) * (long)t.n1 * t.n2;
-  return line;
+__device__ __forceinline__ int sec_of_line(const SecDesc* secs, int nsec, int axis, long g) {
+  int lo = 0, hi = nsec - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (secs[mid].line0[axis] <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
 }
 
-__global__ void k_tri_line(float* __restrict__ x, float* __restrict__ scr, TriAxis t,
-                           const DipScalars* S) {
-  if (S && S->cg_done) return;
-  long line = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (line >= t.nlines) return;
-  const long o = tri_origin(t, line), d = t.stride, ss = t.nlines;
-  const int L = t.len, nb = t.nb, np = L + 2 * nb;
-  const float mw = -t.wt, w2 = t.w2;
-  float* s = scr + line;
+constexpr int kMaxRect = 64;
+
+__global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
+  long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= tp.nlines) return;
+  const int si = sec_of_line(b.secs, b.nsec, tp.axis, g);
+  if (b.S[si].cg_done) return;
+  const SecDesc& s = b.secs[si];
+  const long line = g - s.line0[tp.axis];
+  const int L = tp.axis == 0 ? s.n1 : (tp.axis == 1 ? s.n2 : s.n3);
+  const long nl = s.n / L;
+  long o, d;
+  if (tp.axis == 0) {
+    o = line * s.n1;
+    d = 1;
+  } else if (tp.axis == 1) {
+    o = (line % s.n1) + (line / s.n1) * (long)s.n1 * s.n2;
+    d = s.n1;
+  } else {
+    o = line;
+    d = (long)s.n1 * s.n2;
+  }
+  float* x = a.tmp + s.off + o;
+  float* sc = a.tri + s.scr0[tp.axis] + line;
+  const long ss = nl;
+  const int nb = tp.nb, np = L + 2 * nb;
+  const float mw = -tp.wt, w2 = tp.w2;
   float acc = 0.f;
   for (int m = 0; m < np; m++) {
     float v = 0.f;
-    if (m < L) v = __fadd_rn(v, __fmul_rn(mw, x[o + m * d]));
+    if (m < L) v = __fadd_rn(v, __fmul_rn(mw, x[m * d]));
     int q = m - nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(w2, x[o + q * d]));
+    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(w2, x[q * d]));
     q = m - 2 * nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(mw, x[o + q * d]));
+    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(mw, x[q * d]));
     acc = __fadd_rn(acc, v);
-    s[m * ss] = acc;
+    sc[m * ss] = acc;
   }
   acc = 0.f;
-  for (int m = np - 1; m >= 0; m--) {
-    acc = __fadd_rn(acc, s[m * ss]);
-    s[m * ss] = acc;
-  }
-  int i, j;
-  for (i = 0; i < L; i++) x[o + i * d] = s[(i + nb) * ss];
-  for (j = nb + L; j < np; j += L) {
-    for (i = 0; i < L && i < np - j; i++)
-      x[o + (L - 1 - i) * d] = __fadd_rn(x[o + (L - 1 - i) * d], s[(j + i) * ss]);
-    j += L;
-    for (i = 0; i < L && i < np - j; i++) x[o + i * d] = __fadd_rn(x[o + i * d], s[(j + i) * ss]);
-  }
-  for (j = nb; j >= 0; j -= L) {
-    for (i = 0; i < L && i < j; i++) x[o + i * d] = __fadd_rn(x[o + i * d], s[(j - 1 - i) * ss]);
-    j -= L;
-    for (i = 0; i < L && i < j; i++)
-      x[o + (L - 1 - i) * d] = __fadd_rn(x[o + (L - 1 - i) * d], s[(j - 1 - i) * ss]);
+  if (nb <= L) {
+    // fold2 with one reflection per side: x[i] = B[i+nb], then
+    // + B[2L+nb-1-i] for i >= L-nb, then + B[nb-1-i] for i < nb.  The right
+    // reflections are met first in the descending pass and kept; outputs
+    // i < nb wait for their left reflection.
+    float right[kMaxRect];
+    float left_main[kMaxRect];
+    for (int m = np - 1; m >= 0; m--) {
+      acc = __fadd_rn(acc, sc[m * ss]);
+      if (m >= L + nb) {
+        right[m - (L + nb)] = acc;
+      } else if (m >= nb) {
+        const int i = m - nb;
+        float v = acc;
+        if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
+        if (i < nb)
+          left_main[i] = v;
+        else
+          x[i * d] = v;
+      } else {
+        const int i = nb - 1 - m;
+        x[i * d] = __fadd_rn(left_main[i], acc);
+      }
+    }
+  } else {
+    for (int m = np - 1; m >= 0; m--) {
+      acc = __fadd_rn(acc, sc[m * ss]);
+      sc[m * ss] = acc;
+    }
+    int i, j;
+    for (i = 0; i < L; i++) x[i * d] = sc[(i + nb) * ss];
+    for (j = nb + L; j < np; j += L) {
+      for (i = 0; i < L && i < np - j; i++)
+        x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j + i) * ss]);
+      j += L;
+      for (i = 0; i < L && i < np - j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j + i) * ss]);
+    }
+    for (j = nb; j >= 0; j -= L) {
+      for (i = 0; i < L && i < j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j - 1 - i) * ss]);
+      j -= L;
+      for (i = 0; i < L && i < j; i++)
+        x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j - 1 - i) * ss]);
+    }
   }
 }
 
 // One backtracking trial of dip3 :1666-1687: p = clip(p0 + lam*dp), new
 // residual and its energy; accepted when it decreases.
 template <int NW>
-__global__ void k_ls_trial(const float* __restrict__ u, const float* __restrict__ p0,
-                           const float* __restrict__ dp, float* __restrict__ p,
-                           float* __restrict__ u2, Geo g, ApCoef c, int k, DipScalars* S,
-                           double* partials) {
-  if (S->ls_done) return;
+__global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  DipScalars* S = b.S + tr.sec;
+  if (S->ls_done || no_pass(s, dip)) return;
   const float lam = ldexpf(1.0f, -k);
   const float pmin = -FLT_MAX, pmax = FLT_MAX;
+  const float *u = a.u + s.off, *p0 = a.p0 + s.off, *dp = a.dp + s.off;
+  float *p = a.p + pout_of(s, dip), *u2 = a.u2 + s.off;
+  const long ip = nb_offset(s, dip);
   dvec<1> acc = {{0.0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < g.n;
-       i += (long)gridDim.x * blockDim.x) {
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float pi = __fadd_rn(p0[i], __fmul_rn(lam, dp[i]));
     if (pi < pmin) pi = pmin;
     if (pi > pmax) pi = pmax;
     p[i] = pi;
-    float r = pwd_valid(g, i, NW) ? pwd_at<NW, false>(u, i, g.ip, c, pi) : 0.f;
+    float r = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false>(u, i, ip, c, pi) : 0.f;
     u2[i] = r;
     acc.v[0] += (double)r * (double)r;
   }
   dvec<1> tot;
-  if (grid_sum_last<1>(acc, partials, &S->cnt[4], tot) && threadIdx.x == 0) {
+  if (sec_sum_last<1>(acc, b, t, s, &S->cnt[4], tot) && threadIdx.x == 0) {
     S->usum2 = tot.v[0];
     S->ls_trials = k + 1;
     if (tot.v[0] < S->usum) S->ls_done = 1;
@@ -306,146 +469,221 @@ __global__ void k_ls_trial(const float* __restrict__ u, const float* __restrict_
 }
 
 // mask32 (dip_cfuns.c:914-997, both=false, nj=1): flags samples whose PWD
-// stencil touches a zero of the mask data.
-__global__ void k_mask32(const float* __restrict__ yy, uint8_t* __restrict__ m0,
-                         uint8_t* __restrict__ m1, int n1, int n2, int n3, int nw) {
-  long n = (long)n1 * n2 * n3;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
+// stencil touches a zero of the mask data.  m0 inline, m1 crossline.
+__global__ void k_mask32(const float* __restrict__ mdata, uint8_t* __restrict__ m0,
+                         uint8_t* __restrict__ m1, DipBatch b, int nw) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const float* yy = mdata + s.off;
+  const int n1 = s.n1, n2 = s.n2, n3 = s.n3;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     int ix = (int)(i % n1);
     long r = i / n1;
     int iy = (int)(r % n2), iz = (int)(r / n2);
-    bool a = false, b = false;
+    bool ma = false, mb = false;
     if (ix >= nw && ix < n1 - nw) {
       if (iy < n2 - 1)
         for (int iw = 0; iw <= 2 * nw; iw++) {
           int is = iw - nw;
-          a = a || (yy[i - is] == 0.f) || (yy[i + n1 + is] == 0.f);
+          ma = ma || (yy[i - is] == 0.f) || (yy[i + n1 + is] == 0.f);
         }
       if (iz < n3 - 1)
         for (int iw = 0; iw <= 2 * nw; iw++) {
           int is = iw - nw;
-          b = b || (yy[i - is] == 0.f) || (yy[i + (long)n1 * n2 + is] == 0.f);
+          mb = mb || (yy[i - is] == 0.f) || (yy[i + (long)n1 * n2 + is] == 0.f);
         }
     }
-    m0[i] = a;
-    m1[i] = b;
+    m0[s.off + i] = ma;
+    m1[s.off + i] = mb;
   }
 }
 
+__global__ void k_zero_slopes(float* __restrict__ p, DipBatch b) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    p[s.pout + i] = 0.f;
+    if (s.n3 > 1) p[s.pout + s.n + i] = 0.f;
+  }
+}
+
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsec) return;
+  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
+}
+
+__global__ void k_put_single(SecDesc* dst, SecDesc v) { *dst = v; }
+
+// Marks the loops of 2-D sections done before the crossline pass.
+__global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsec || secs[s].n3 > 1) return;
+  S[s].cg_done = 1;
+  S[s].ls_done = 1;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct DipLayout {
+  long ntot;  // elements spanned by the input arrays
+  int ntiles;
+  long scr_total;
+  long nlines[3];
+  bool any3d;
+};
+
+// Completes the section table (tiles, triangle line numbering and scratch).
+DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
+  DipLayout L{};
+  long scr[3] = {0, 0, 0}, lines[3] = {0, 0, 0};
+  int tiles = 0;
+  for (auto& s : secs) {
+    s.n = (long)s.n1 * s.n2 * s.n3;
+    L.ntot = std::max(L.ntot, s.off + s.n);
+    L.any3d |= s.n3 > 1;
+    s.tile0 = tiles;
+    s.ntile = (int)((s.n + kTile - 1) / kTile);
+    tiles += s.ntile;
+    const int len[3] = {s.n1, s.n2, s.n3};
+    for (int a = 0; a < 3; a++) {
+      s.line0[a] = lines[a];
+      s.scr0[a] = scr[a];
+      if (rect[a] > 1) {
+        long nl = s.n / len[a];
+        lines[a] += nl;
+        scr[a] += nl * (len[a] + 2L * rect[a]);
+      }
+    }
+  }
+  L.ntiles = tiles;
+  L.scr_total = std::max(std::max(scr[0], scr[1]), std::max(scr[2], 1L));
+  for (int a = 0; a < 3; a++) L.nlines[a] = lines[a];
+  return L;
+}
+
 struct DipWork {
-  float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
+  DipArrays a;
   uint8_t *m0, *m1;
+  SecDesc* secs;
+  int* tile_sec;
   DipScalars* S;
   double* partials;
 };
 
-long tri_scratch_elems(int n1, int n2, int n3, const int rect[3]) {
-  long n = (long)n1 * n2 * n3, best = 0;
-  const int len[3] = {n1, n2, n3};
-  for (int a = 0; a < 3; a++)
-    if (rect[a] > 1) {
-      long nl = n / len[a];
-      long e = nl * (len[a] + 2L * rect[a]);
-      if (e > best) best = e;
-    }
-  return best > 0 ? best : 1;
-}
-
-DipWork carve_dip(void* ws, int n1, int n2, int n3, const int rect[3], int has_mask,
-                  size_t* total) {
-  long n = (long)n1 * n2 * n3;
+DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t* total) {
   Carver cv(ws);
-  DipWork w;
-  w.u1 = cv.take<float>(n);
-  w.u2 = cv.take<float>(n);
-  w.dp = cv.take<float>(n);
-  w.p0 = cv.take<float>(n);
-  w.pcg = cv.take<float>(n);
-  w.r = cv.take<float>(n);
-  w.gp = cv.take<float>(n);
-  w.tmp = cv.take<float>(n);
-  w.sp = cv.take<float>(n);
-  w.sx = cv.take<float>(n);
-  w.sr = cv.take<float>(n);
-  w.tri = cv.take<float>(tri_scratch_elems(n1, n2, n3, rect));
+  DipWork w{};
+  const long n = L.ntot;
+  w.a.u1 = cv.take<float>(n);
+  w.a.u2 = cv.take<float>(n);
+  w.a.dp = cv.take<float>(n);
+  w.a.p0 = cv.take<float>(n);
+  w.a.pcg = cv.take<float>(n);
+  w.a.r = cv.take<float>(n);
+  w.a.gp = cv.take<float>(n);
+  w.a.tmp = cv.take<float>(n);
+  w.a.sp = cv.take<float>(n);
+  w.a.sx = cv.take<float>(n);
+  w.a.sr = cv.take<float>(n);
+  w.a.tri = cv.take<float>(L.scr_total);
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.m1 = has_mask ? cv.take<uint8_t>(n) : nullptr;
-  w.S = cv.take<DipScalars>(1);
-  w.partials = cv.take<double>(4 * (size_t)kRedGridMax);
+  w.secs = cv.take<SecDesc>(nsec);
+  w.tile_sec = cv.take<int>(L.ntiles);
+  w.S = cv.take<DipScalars>(nsec);
+  w.partials = cv.take<double>((size_t)L.ntiles * 3);
   *total = cv.size();
   return w;
 }
 
 template <int NW>
-int dip3_run(const float* u, float* p, const uint8_t* mask, int dip, int n1, int n2, int n3,
-             int niter, int liter, const int rect[3], const DipWork& w, cudaStream_t st) {
-  Geo g;
-  g.n1 = n1;
-  g.n2 = n2;
-  g.n3 = n3;
-  g.n = (long)n1 * n2 * n3;
-  g.dip = dip;
-  g.ip = dip == 1 ? n1 : (long)n1 * n2;
+int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], const DipLayout& L,
+             const DipBatch& b, cudaStream_t st) {
   const ApCoef c = make_apcoef(NW);
-  const int gr = red_grid(g.n);
-  const int ge = (int)std::min<long>((g.n + kBlock - 1) / kBlock, 65535L * 8);
-
-  TriAxis ax[3];
+  TriParams tp[3];
   int nax = 0;
-  const int len[3] = {n1, n2, n3};
-  const long str[3] = {1, n1, (long)n1 * n2};
-  for (int a = 0; a < 3; a++) {
-    if (rect[a] <= 1) continue;
-    TriAxis t;
-    t.axis = a;
-    t.len = len[a];
-    t.nb = rect[a];
-    t.nlines = g.n / len[a];
-    t.stride = str[a];
-    t.n1 = n1;
-    t.n2 = n2;
-    t.wt = (float)(1.0 / (rect[a] * rect[a]));
+  for (int ax = 0; ax < 3; ax++) {
+    if (rect[ax] <= 1 || L.nlines[ax] == 0) continue;
+    TriParams t;
+    t.axis = ax;
+    t.nb = rect[ax];
+    t.nlines = L.nlines[ax];
+    t.wt = (float)(1.0 / (rect[ax] * rect[ax]));
     t.w2 = (float)(2. * t.wt);
-    ax[nax++] = t;
+    tp[nax++] = t;
   }
+  const unsigned gt = (unsigned)L.ntiles;
   auto sweeps = [&]() {
-    for (int a = 0; a < nax; a++) {
-      int gl = (int)((ax[a].nlines + 127) / 128);
-      k_tri_line<<<gl, 128, 0, st>>>(w.tmp, w.tri, ax[a], w.S);
+    for (int k = 0; k < nax; k++) {
+      const int bs = 128;
+      PWD_KERNEL(PWD_FAM_TRIANGLE, st,
+                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, 0, st>>>(a, b, tp[k]));
     }
   };
-
-  k_residual<NW><<<ge, kBlock, 0, st>>>(u, p, w.u2, g, c);
+  PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
   for (int iter = 0; iter < niter; iter++) {
-    k_prep<NW><<<gr, kRedBlock, 0, st>>>(u, p, w.u2, w.u1, w.p0, mask, g, c, w.S, w.partials);
-    k_scale<<<gr, kRedBlock, 0, st>>>(w.u2, w.u1, w.r, w.pcg, w.dp, g.n, w.S, w.partials);
+    PWD_KERNEL(PWD_FAM_PWD, st, k_prep<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
+    PWD_KERNEL(PWD_FAM_CG, st, k_scale<<<gt, kTileThreads, 0, st>>>(a, b, dip));
     for (int it = 0; it < liter; it++) {
-      k_cg_grad<<<ge, kBlock, 0, st>>>(w.dp, w.r, w.u1, w.tmp, g.n, w.S);
+      PWD_KERNEL(PWD_FAM_CG, st, k_cg_stepgrad<<<gt, kTileThreads, 0, st>>>(a, b, it));
       sweeps();
-      k_cg_gp<<<gr, kRedBlock, 0, st>>>(w.pcg, w.tmp, w.gp, g.n, it, w.S, w.partials);
+      PWD_KERNEL(PWD_FAM_CG, st, k_cg_gp<<<gt, kTileThreads, 0, st>>>(a, b, it));
       sweeps();
-      k_cg_update<<<gr, kRedBlock, 0, st>>>(w.gp, w.tmp, w.u1, w.sp, w.sx, w.sr, g.n, it, w.S,
-                                            w.partials);
-      k_cg_step<<<ge, kBlock, 0, st>>>(w.pcg, w.dp, w.r, w.sp, w.sx, w.sr, g.n, w.S);
+      PWD_KERNEL(PWD_FAM_CG, st, k_cg_update<<<gt, kTileThreads, 0, st>>>(a, b, it));
     }
+    if (liter > 0) PWD_KERNEL(PWD_FAM_CG, st, k_cg_step<<<gt, kTileThreads, 0, st>>>(a, b));
     for (int k = 0; k < 8; k++)
-      k_ls_trial<NW><<<gr, kRedBlock, 0, st>>>(u, w.p0, w.dp, p, w.u2, g, c, k, w.S, w.partials);
+      PWD_KERNEL(PWD_FAM_PWD, st, k_ls_trial<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip, k));
   }
-  PWD_LAUNCH_CHECK();
-  return PWD_OK;
+  return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
-int dip_dispatch(int order, const float* u, float* p, const uint8_t* mask, int dip, int n1,
-                 int n2, int n3, int niter, int liter, const int rect[3], const DipWork& w,
-                 cudaStream_t st) {
+int dip_dispatch(int order, DipArrays a, int dip, int niter, int liter, const int rect[3],
+                 const DipLayout& L, const DipBatch& b, cudaStream_t st) {
   switch (order) {
-    case 1: return dip3_run<1>(u, p, mask, dip, n1, n2, n3, niter, liter, rect, w, st);
-    case 2: return dip3_run<2>(u, p, mask, dip, n1, n2, n3, niter, liter, rect, w, st);
-    case 3: return dip3_run<3>(u, p, mask, dip, n1, n2, n3, niter, liter, rect, w, st);
-    case 4: return dip3_run<4>(u, p, mask, dip, n1, n2, n3, niter, liter, rect, w, st);
+    case 1: return dip3_run<1>(a, dip, niter, liter, rect, L, b, st);
+    case 2: return dip3_run<2>(a, dip, niter, liter, rect, L, b, st);
+    case 3: return dip3_run<3>(a, dip, niter, liter, rect, L, b, st);
+    case 4: return dip3_run<4>(a, dip, niter, liter, rect, L, b, st);
   }
   return PWD_ENOTSUP;
+}
+
+// Enqueues the estimation of a batch whose section table is in w.secs.
+int dip_enqueue(const float* data, const float* mask, float* out, const DipLayout& L,
+                const DipWork& w, int nsec, int niter, int liter, int order, const int rect[3],
+                cudaStream_t st) {
+  PWD_KERNEL(PWD_FAM_OTHER, st,
+             k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
+  if (cudaMemsetAsync(w.S, 0, sizeof(DipScalars) * nsec, st) != cudaSuccess) return PWD_ECUDA;
+  DipBatch b{w.secs, w.tile_sec, nsec, L.ntiles, w.S, w.partials};
+  DipArrays a = w.a;
+  a.u = data;
+  a.p = out;
+  PWD_KERNEL(PWD_FAM_OTHER, st, k_zero_slopes<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(out, b));
+  if (mask)
+    PWD_KERNEL(PWD_FAM_OTHER, st,
+               k_mask32<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(mask, w.m0, w.m1, b, order));
+  a.mask = mask ? w.m0 : nullptr;
+  int rc = dip_dispatch(order, a, 1, niter, liter, rect, L, b, st);
+  if (rc != PWD_OK || !L.any3d) return rc;
+  // crossline slopes (dipc :1926); 2-D sections of a mixed batch skip them
+  // because their crossline residual region is empty (n3 = 1).
+  a.mask = mask ? w.m1 : nullptr;
+  PWD_KERNEL(PWD_FAM_OTHER, st, k_skip_2d<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.S));
+  return dip_dispatch(order, a, 2, niter, liter, rect, L, b, st);
+}
+
+int check_dip_args(int niter, int liter, int order, const int rect[3]) {
+  if (!rect || niter < 0 || liter < 0 || order < 1) return PWD_EINVAL;
+  for (int a = 0; a < 3; a++) {
+    if (rect[a] < 0) return PWD_EINVAL;
+    if (rect[a] > kMaxRect) return PWD_ENOTSUP;
+  }
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  return PWD_OK;
 }
 
 }  // namespace
@@ -457,38 +695,86 @@ extern "C" size_t pwd_dip_workspace_size(int n1, int n2, int n3, int order, cons
                                          int has_mask) {
   (void)order;
   if (n1 < 1 || n2 < 1 || n3 < 1 || !rect) return 0;
-  size_t total = 0;
-  carve_dip(nullptr, n1, n2, n3, rect, has_mask, &total);
-  return total;
+  std::vector<SecDesc> secs(1, SecDesc{});
+  secs[0].n1 = n1;
+  secs[0].n2 = n2;
+  secs[0].n3 = n3;
+  DipLayout L = layout(secs, rect);
+  size_t need = 0;
+  carve_dip(nullptr, L, 1, has_mask != 0, &need);
+  return need;
 }
 
 extern "C" int pwd_dip(const float* data, const float* mask, float* dip_out, int n1, int n2,
                        int n3, int niter, int liter, int order, const int rect[3],
                        void* workspace, size_t workspace_bytes, pwd_stream_t stream) {
-  if (!data || !dip_out || !rect || n1 < 1 || n2 < 1 || n3 < 1 || niter < 0 || liter < 0 ||
-      order < 1)
-    return PWD_EINVAL;
-  for (int a = 0; a < 3; a++)
-    if (rect[a] < 0) return PWD_EINVAL;
-  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
-  if (2 * order >= n1) return PWD_EINVAL;
-  size_t need = 0;
-  carve_dip(nullptr, n1, n2, n3, rect, mask != nullptr, &need);
-  if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  DipWork w = carve_dip(workspace, n1, n2, n3, rect, mask != nullptr, &need);
-  cudaStream_t st = (cudaStream_t)stream;
-  const long n = (long)n1 * n2 * n3;
-  const bool three = n3 > 1;
-  if (cudaMemsetAsync(dip_out, 0, sizeof(float) * n * (three ? 2 : 1), st) != cudaSuccess)
-    return PWD_ECUDA;
-  if (cudaMemsetAsync(w.S, 0, sizeof(DipScalars), st) != cudaSuccess) return PWD_ECUDA;
-  if (mask) {
-    int gb = (int)std::min<long>((n + 255) / 256, 65535L * 8);
-    k_mask32<<<gb, 256, 0, st>>>(mask, w.m0, w.m1, n1, n2, n3, order);
-  }
-  int rc = dip_dispatch(order, data, dip_out, w.m0, 1, n1, n2, n3, niter, liter, rect, w, st);
+  int rc = check_dip_args(niter, liter, order, rect);
   if (rc != PWD_OK) return rc;
-  if (three)
-    rc = dip_dispatch(order, data, dip_out + n, w.m1, 2, n1, n2, n3, niter, liter, rect, w, st);
-  return rc;
+  if (!data || !dip_out || n1 < 1 || n2 < 1 || n3 < 1 || 2 * order >= n1) return PWD_EINVAL;
+  std::vector<SecDesc> secs(1, SecDesc{});
+  secs[0].n1 = n1;
+  secs[0].n2 = n2;
+  secs[0].n3 = n3;
+  DipLayout L = layout(secs, rect);
+  size_t need = 0;
+  carve_dip(nullptr, L, 1, mask != nullptr, &need);
+  if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
+  DipWork w = carve_dip(workspace, L, 1, mask != nullptr, &need);
+  cudaStream_t st = (cudaStream_t)stream;
+  PWD_KERNEL(PWD_FAM_OTHER, st, k_put_single<<<1, 1, 0, st>>>(w.secs, secs[0]));
+  return dip_enqueue(data, mask, dip_out, L, w, 1, niter, liter, order, rect, st);
+}
+
+// ---------------------------------------------------------------------------
+// batched entry point
+// ---------------------------------------------------------------------------
+namespace {
+
+int batch_table(const pwd_section* in, int nsec, int order, std::vector<SecDesc>& secs) {
+  if (!in || nsec < 1) return PWD_EINVAL;
+  secs.assign(nsec, SecDesc{});
+  for (int i = 0; i < nsec; i++) {
+    if (in[i].n1 < 1 || in[i].n2 < 1 || in[i].n3 < 1 || 2 * order >= in[i].n1 ||
+        in[i].offset < 0 || in[i].out_offset < 0)
+      return PWD_EINVAL;
+    secs[i].off = in[i].offset;
+    secs[i].pout = in[i].out_offset;
+    secs[i].n1 = in[i].n1;
+    secs[i].n2 = in[i].n2;
+    secs[i].n3 = in[i].n3;
+  }
+  return PWD_OK;
+}
+
+}  // namespace
+
+extern "C" size_t pwd_dip_batch_workspace_size(const pwd_section* sections, int nsec, int order,
+                                               const int rect[3], int has_mask) {
+  std::vector<SecDesc> secs;
+  if (!rect || batch_table(sections, nsec, std::max(order, 1), secs) != PWD_OK) return 0;
+  DipLayout L = layout(secs, rect);
+  size_t need = 0;
+  carve_dip(nullptr, L, nsec, has_mask != 0, &need);
+  return need;
+}
+
+extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_out,
+                             const pwd_section* sections, int nsec, int niter, int liter,
+                             int order, const int rect[3], void* workspace,
+                             size_t workspace_bytes, pwd_stream_t stream) {
+  int rc = check_dip_args(niter, liter, order, rect);
+  if (rc != PWD_OK) return rc;
+  if (!data || !dip_out) return PWD_EINVAL;
+  std::vector<SecDesc> secs;
+  if ((rc = batch_table(sections, nsec, order, secs)) != PWD_OK) return rc;
+  DipLayout L = layout(secs, rect);
+  size_t need = 0;
+  carve_dip(nullptr, L, nsec, mask != nullptr, &need);
+  if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
+  DipWork w = carve_dip(workspace, L, nsec, mask != nullptr, &need);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PWD_ECUDA;
+  return dip_enqueue(data, mask, dip_out, L, w, nsec, niter, liter, order, rect, st);
 }

@@ -119,12 +119,12 @@ inline int launch_panel_median(const float* u, float* out, float* v2, float* avg
   const long nout = ntr * n1;
   const int b = 128;
   if (option == 1) {
-    k_median_centre<<<(unsigned)((nout + b - 1) / b), b, 0, st>>>(u, out, n1, np, ntr, nmf);
+    PWD_KERNEL(PWD_FAM_FILTER, st, k_median_centre<<<(unsigned)((nout + b - 1) / b), b, 0, st>>>(u, out, n1, np, ntr, nmf));
   } else {
     const long nv = ntr * np * (long)n1;
-    k_svmf_pass1<<<(unsigned)((nv + b - 1) / b), b, 0, st>>>(u, v2, n1, np, ntr, nmf);
-    k_svmf_avg<<<(unsigned)((ntr + b - 1) / b), b, 0, st>>>(v2, avg, n1, np, ntr);
-    k_svmf_pass2<<<(unsigned)((nout + b - 1) / b), b, 0, st>>>(u, avg, out, n1, np, ntr, nmf);
+    PWD_KERNEL(PWD_FAM_FILTER, st, k_svmf_pass1<<<(unsigned)((nv + b - 1) / b), b, 0, st>>>(u, v2, n1, np, ntr, nmf));
+    PWD_KERNEL(PWD_FAM_FILTER, st, k_svmf_avg<<<(unsigned)((ntr + b - 1) / b), b, 0, st>>>(v2, avg, n1, np, ntr));
+    PWD_KERNEL(PWD_FAM_FILTER, st, k_svmf_pass2<<<(unsigned)((nout + b - 1) / b), b, 0, st>>>(u, avg, out, n1, np, ntr, nmf));
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }

@@ -403,9 +403,9 @@ int soint3_run(const float* data, const float* mask, const float* pp, const floa
   // ps_cgstep's restart zeroes the step vectors (:838-839)
   if (cudaMemsetAsync(w.S, 0, sizeof(float) * n, st) != cudaSuccess) return PWD_ECUDA;
   if (cudaMemsetAsync(w.Ss, 0, sizeof(float) * ny, st) != cudaSuccess) return PWD_ECUDA;
-  k_ap3_coef<NW><<<gn, b, 0, st>>>(pp, qq, g, make_apcoef(NW), cf);
-  if (g.drift) k_max_shift<<<gr, kRedBlock, 0, st>>>(w.id1, w.id2, n, &w.sc->dmax);
-  k_init_x<<<gn, b, 0, st>>>(data, mask, x, w.known, n, hasmask);
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_coef<NW><<<gn, b, 0, st>>>(pp, qq, g, make_apcoef(NW), cf));
+  if (g.drift) PWD_KERNEL(PWD_FAM_SOINT, st, k_max_shift<<<gr, kRedBlock, 0, st>>>(w.id1, w.id2, n, &w.sc->dmax));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_init_x<<<gn, b, 0, st>>>(data, mask, x, w.known, n, hasmask));
   if (var != 0.f) {
     std::vector<float> dd((size_t)ny);
     make_noise(dd, seed, var);
@@ -414,15 +414,15 @@ int soint3_run(const float* data, const float* mask, const float* pp, const floa
       return PWD_ECUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return PWD_ECUDA;
   }
-  k_init_rr<<<g2, b, 0, st>>>(w.rr, var != 0.f ? w.dd : nullptr, ny);
-  k_ap3_fwd<NW><<<gn, b, 0, st>>>(x, w.rr, g, cf, 1, nullptr);
-  k_rr0<<<gr2, kRedBlock, 0, st>>>(w.rr, ny, w.sc, w.partials);
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_init_rr<<<g2, b, 0, st>>>(w.rr, var != 0.f ? w.dd : nullptr, ny));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gn, b, 0, st>>>(x, w.rr, g, cf, 1, nullptr));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_rr0<<<gr2, kRedBlock, 0, st>>>(w.rr, ny, w.sc, w.partials));
   for (int iter = 0; iter < niter; iter++) {
-    k_ap3_adj<NW><<<gr, kRedBlock, 0, st>>>(w.g, w.rr, g, cf, w.known, &w.sc->dmax, &w.sc->done,
-                                            w.partials, &w.sc->cnt[0], &w.sc->gsum);
-    k_ap3_fwd<NW><<<gn, b, 0, st>>>(w.g, w.gg, g, cf, 0, &w.sc->done);
-    k_cg3_dots<<<gr2, kRedBlock, 0, st>>>(w.gg, w.Ss, w.rr, ny, iter, w.sc, w.partials);
-    k_cg3_update<<<g2, b, 0, st>>>(x, w.S, w.g, w.rr, w.Ss, w.gg, n, iter, w.sc);
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_adj<NW><<<gr, kRedBlock, 0, st>>>(w.g, w.rr, g, cf, w.known, &w.sc->dmax, &w.sc->done,
+                                            w.partials, &w.sc->cnt[0], &w.sc->gsum));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gn, b, 0, st>>>(w.g, w.gg, g, cf, 0, &w.sc->done));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_dots<<<gr2, kRedBlock, 0, st>>>(w.gg, w.Ss, w.rr, ny, iter, w.sc, w.partials));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_update<<<g2, b, 0, st>>>(x, w.S, w.g, w.rr, w.Ss, w.gg, n, iter, w.sc));
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }

@@ -1,67 +1,115 @@
 // 2-D plane-wave spray with the structure-oriented mean and median.
 //
 // Restates csomean2d / csomf2d (pyseistr/src/sof_cfuns.c:1433-1678) with
-// pwsmooth_* (:1036-1122) and pwspray_lop (:948-1033).  The spray of a
-// section is two independent prediction chains per source trace (towards
-// lower and higher trace numbers); every chain is one GPU thread, every
-// slice of an n3 > 1 volume is processed in the same launch.
+// pwsmooth_* (:1036-1122) and pwspray_lop (:948-1033), for one section or a
+// batch of sections of uneven size in one launch.  The spray of a section is
+// two independent prediction chains per source trace (towards lower and
+// higher trace numbers); every chain is one GPU thread.  For the mean, the
+// trace of ones (the normalisation spray of pwsmooth_set) and the data are
+// predicted through the same factorisation in the same chain.
 #include <algorithm>
+#include <vector>
 
+#include "pwd_batch.cuh"
 #include "pwd_median.cuh"
 #include "pwd_predict.cuh"
 
 namespace pwd {
 namespace {
 
-struct Spray2 {
-  int n1, n2, n3, ns, np;
+constexpr int kTile = 2048;
+constexpr int kTileThreads = 256;
+
+struct SprayB {
+  const SecDesc* secs;
+  const int* tile_sec;
+  int nsec, ntiles;
+  long ntr;  // traces over the batch (n2*n3 per section)
+  int ns, np;
   float eps, eps2;
 };
 
-// Forward spray (pwspray_lop adj=false): u[tr][np][n1], tr = i3*n2 + i2.
-// Thread (i3, source i, dir).  in == nullptr sprays a trace of ones.
-template <int NW>
+struct SprayBufs {
+  float* u;     // data panels [trace][np][n1] per section
+  float* u1;    // ones panels (mean only)
+  float* w1;    // normalisation weights, one per sample (adjoint mean only)
+  float* scr;   // per-chain prediction scratch
+  float* tbuf;  // adjoint chain traces
+};
+
+__device__ __forceinline__ const SecDesc& trace_section(const SprayB& b, long g, long& q) {
+  const int si = find_section(b.nsec, g, [&](int k) { return b.secs[k].tr0; });
+  q = g - b.secs[si].tr0;
+  return b.secs[si];
+}
+
+template <int NB>
+__device__ __forceinline__ PredictScratch chain_scratch(float* scr, const SecDesc& s, long tl,
+                                                        long nthr_s, float** y2) {
+  PredictScratch my;
+  float* base = scr + s.sc0;
+  const long stride = (long)s.n1 * nthr_s;
+  my.o = base + tl;
+  my.d = base + NB * stride + tl;
+  my.y = base + (NB + 1) * stride + tl;
+  if (y2) *y2 = base + (NB + 2) * stride + tl;
+  my.ss = nthr_s;
+  return my;
+}
+
+// Forward spray (pwspray_lop adj=false).  Thread (trace g, dir).  MODE 0:
+// data only; MODE 1: data and ones together (u and u1); MODE 2: ones only
+// into u1.
+template <int NW, int MODE>
 __global__ void k_spray2_chains(const float* __restrict__ in, const float* __restrict__ ones,
-                                const float* __restrict__ dip, float* __restrict__ u, Spray2 s,
-                                ApCoef c, PredictScratch sc) {
-  const long nthr = 2L * s.n2 * s.n3;
+                                const float* __restrict__ dip, SprayBufs bf, SprayB b, ApCoef c) {
   long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= nthr) return;
+  if (t >= 2 * b.ntr) return;
   const int dir = (int)(t & 1);
-  const long q = t >> 1;
-  const int i = (int)(q % s.n2);
-  const long i3 = q / s.n2;
-  const long n12 = (long)s.n1 * s.n2;
-  const float* pp = dip + i3 * n12;
-  float* U = u + i3 * s.n2 * (long)s.np * s.n1;
-  const float* src = in ? in + i3 * n12 + (long)i * s.n1 : ones;
-  PredictScratch my = sc;
-  my.o += t;
-  my.d += t;
-  my.y += t;
-  auto slot = [&](int k, int sl) { return U + ((long)k * s.np + sl) * s.n1; };
+  long q;
+  const SecDesc& s = trace_section(b, t >> 1, q);
+  const int n1 = s.n1, n2 = s.n2;
+  const int i = (int)(q % n2);
+  const long i3 = q / n2;
+  const long n12 = (long)n1 * n2;
+  const float* pp = dip + s.off + i3 * n12;
+  const long slice_u = s.u0 + i3 * n2 * (long)b.np * n1;
+  float* U = (MODE == 2 ? bf.u1 : bf.u) + slice_u;
+  float* U1 = MODE == 1 ? bf.u1 + slice_u : nullptr;
+  const float* src = MODE == 2 ? ones : in + s.off + i3 * n12 + (long)i * n1;
+  float* y2 = nullptr;
+  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, t - 2 * s.tr0, 2L * n2 * s.n3,
+                                            MODE == 1 ? &y2 : nullptr);
+  auto slot = [&](float* base, int k, int sl) { return base + ((long)k * b.np + sl) * n1; };
+  const int ns = b.ns;
   if (dir == 0) {
-    float* cen = slot(i, s.ns);
-    for (int i1 = 0; i1 < s.n1; i1++) cen[i1] = src[i1];
-    const float* prev = src;
-    for (int is = 0; is < s.ns; is++) {  // predict forward: to trace i-is-1
-      int ip = i - is - 1;
-      if (ip < 0) break;
-      float* out = slot(ip, s.ns - is - 1);
-      predict_fwd<NW, false>(s.n1, s.eps, s.eps2, c, prev, pp + (long)ip * s.n1, false, nullptr,
-                             nullptr, false, out, my);
-      prev = out;
+    float* cen = slot(U, i, ns);
+    for (int i1 = 0; i1 < n1; i1++) cen[i1] = src[i1];
+    if (MODE == 1) {
+      float* cen1 = slot(U1, i, ns);
+      for (int i1 = 0; i1 < n1; i1++) cen1[i1] = 1.0f;
     }
-  } else {
-    const float* prev = src;
-    for (int is = 0; is < s.ns; is++) {  // predict backward: to trace i+is+1
-      int ip = i + is + 1;
-      if (ip >= s.n2) break;
-      float* out = slot(ip, s.ns + is + 1);
-      predict_fwd<NW, false>(s.n1, s.eps, s.eps2, c, prev, pp + (long)(ip - 1) * s.n1, true,
-                             nullptr, nullptr, false, out, my);
-      prev = out;
+  }
+  const float* prev = src;
+  const float* prevb = ones;
+  for (int is = 0; is < ns; is++) {
+    // dir 0 predicts forward to trace i-is-1 with its own slopes (forw=false);
+    // dir 1 predicts backward to trace i+is+1 with the slopes of ip-1.
+    const int ip = dir == 0 ? i - is - 1 : i + is + 1;
+    if (ip < 0 || ip >= n2) break;
+    const int sl = dir == 0 ? ns - is - 1 : ns + is + 1;
+    const float* pq = pp + (long)(dir == 0 ? ip : ip - 1) * n1;
+    float* out = slot(U, ip, sl);
+    if (MODE == 1) {
+      float* outb = slot(U1, ip, sl);
+      predict_fwd<NW, false, true>(n1, b.eps, b.eps2, c, prev, pq, dir == 1, nullptr, nullptr,
+                                   false, out, my, prevb, outb, y2);
+      prevb = outb;
+    } else {
+      predict_fwd<NW, false>(n1, b.eps, b.eps2, c, prev, pq, dir == 1, nullptr, nullptr, false,
+                             out, my);
     }
+    prev = out;
   }
 }
 
@@ -71,161 +119,299 @@ __device__ __forceinline__ float tri_weight(int is, int ns) {
   return (float)(ns + 1 - (a >= 0 ? a : -a));
 }
 
-// pwsmooth_set :1102-1122: w1 = 1 / (weighted spray of ones), 0 where 0.
-__global__ void k_norm_weights(const float* __restrict__ u, float* __restrict__ w1, Spray2 s) {
-  long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long n = (long)s.n1 * s.n2 * s.n3;
-  if (t >= n) return;
-  const long tr = t / s.n1;
-  const int i1 = (int)(t % s.n1);
-  const float* panel = u + tr * s.np * (long)s.n1 + i1;
-  float acc = 0.f;
-  for (int is = 0; is < s.np; is++)
-    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(panel[(long)is * s.n1], tri_weight(is, s.ns)), 1.0f));
-  w1[t] = (acc != 0.f) ? __double2float_rn(1.0 / (double)acc) : 0.f;
+struct TileRange {
+  int sec;
+  long lo, hi;
+};
+__device__ __forceinline__ TileRange tile_range(const SprayB& b, int t) {
+  TileRange r;
+  r.sec = b.tile_sec[t];
+  const SecDesc& s = b.secs[r.sec];
+  r.lo = (long)(t - s.tile0) * kTile;
+  r.hi = min(s.n, r.lo + kTile);
+  return r;
 }
 
-// pwsmooth_lop forward :1088-1098: smooth = sum_is u*w[is]*w1.
-__global__ void k_weighted_mean(const float* __restrict__ u, const float* __restrict__ w1,
-                                float* __restrict__ out, Spray2 s) {
-  long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long n = (long)s.n1 * s.n2 * s.n3;
-  if (t >= n) return;
-  const long tr = t / s.n1;
-  const int i1 = (int)(t % s.n1);
-  const float* panel = u + tr * s.np * (long)s.n1 + i1;
-  const float ws = w1[t];
-  float acc = 0.f;
-  for (int is = 0; is < s.np; is++)
-    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(panel[(long)is * s.n1], tri_weight(is, s.ns)), ws));
-  out[t] = acc;
+// pwsmooth_set :1102-1122 and pwsmooth_lop forward :1088-1098: w1 = 1 /
+// (weighted spray of ones) (0 where 0), smooth = sum_is u*w[is]*w1.
+__global__ void k_weighted_mean(SprayBufs bf, float* __restrict__ out, SprayB b, int store_w1,
+                                int mean) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
+    const long trc = j / s.n1;
+    const int i1 = (int)(j % s.n1);
+    const long po = s.u0 + trc * b.np * (long)s.n1 + i1;
+    float acc = 0.f;
+    for (int is = 0; is < b.np; is++)
+      acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(bf.u1[po + (long)is * s.n1], tri_weight(is, b.ns)),
+                                     1.0f));
+    const float ws = (acc != 0.f) ? __double2float_rn(1.0 / (double)acc) : 0.f;
+    if (store_w1) bf.w1[s.off + j] = ws;
+    if (mean) {
+      float m = 0.f;
+      for (int is = 0; is < b.np; is++)
+        m = __fadd_rn(m, __fmul_rn(__fmul_rn(bf.u[po + (long)is * s.n1], tri_weight(is, b.ns)), ws));
+      out[s.pout + j] = m;
+    }
+  }
+}
+
+// mf centre row (sof_cfuns.c:1294-1332 via csomf2d :1623-1649).
+__global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ out, SprayB b,
+                               int nmf) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const int m = (nmf - 1) / 2, c = (b.np - 1) / 2;
+  float v[kMaxWin];
+  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
+    const long trc = j / s.n1;
+    const int i1 = (int)(j % s.n1);
+    const float* panel = u + s.u0 + trc * b.np * (long)s.n1 + i1;
+    for (int k = 0; k < nmf; k++) v[k] = panel[(long)clampi(c + k - m, 0, b.np - 1) * s.n1];
+    out[s.pout + j] = select_rank(v, nmf, m);
+  }
 }
 
 // Adjoint of the weighted mean (pwsmooth_lop adjoint :1072-1086 with
-// pwspray_lop adjoint :957-989).  Thread (i3, output trace i); traces in a
-// per-thread contiguous buffer tb[n1].
+// pwspray_lop adjoint :957-989).  Thread per output trace; chain traces in a
+// per-thread buffer.
 template <int NW>
 __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restrict__ dip,
-                               const float* __restrict__ w1, float* __restrict__ out,
-                               float* __restrict__ tbuf, Spray2 s, ApCoef c, PredictScratch sc) {
-  const long nthr = (long)s.n2 * s.n3;
-  long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= nthr) return;
-  const int i = (int)(t % s.n2);
-  const long i3 = t / s.n2;
-  const long n12 = (long)s.n1 * s.n2;
-  const float* pp = dip + i3 * n12;
-  const float* X = x + i3 * n12;
-  const float* W = w1 + i3 * n12;
-  float* tr = tbuf + t * s.n1;
-  PredictScratch my = sc;
-  my.o += t;
-  my.d += t;
-  my.y += t;
-  float* o = out + i3 * n12 + (long)i * s.n1;
+                               float* __restrict__ out, SprayBufs bf, SprayB b, ApCoef c) {
+  long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= b.ntr) return;
+  long q;
+  const SecDesc& s = trace_section(b, g, q);
+  const int n1 = s.n1, n2 = s.n2;
+  const int i = (int)(q % n2);
+  const long i3 = q / n2;
+  const long n12 = (long)n1 * n2;
+  const float* pp = dip + s.off + i3 * n12;
+  const float* X = x + s.off + i3 * n12;
+  const float* W = bf.w1 + s.off + i3 * n12;
+  float* tr = bf.tbuf + s.off + q * n1;
+  const long nthr_s = 2L * n2 * s.n3;
+  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, q, nthr_s, nullptr);
+  float* o = out + s.pout + i3 * n12 + (long)i * n1;
   auto add_slot = [&](int ip, int sl) {
-    const float wv = tri_weight(sl, s.ns);
-    for (int i1 = 0; i1 < s.n1; i1++) {
-      long e = (long)ip * s.n1 + i1;
+    const float wv = tri_weight(sl, b.ns);
+    for (int i1 = 0; i1 < n1; i1++) {
+      long e = (long)ip * n1 + i1;
       tr[i1] = __fadd_rn(tr[i1], __fmul_rn(__fmul_rn(X[e], wv), W[e]));
     }
   };
-  for (int i1 = 0; i1 < s.n1; i1++) tr[i1] = 0.f;
-  for (int is = s.ns - 1; is >= 0; is--) {
+  for (int i1 = 0; i1 < n1; i1++) tr[i1] = 0.f;
+  for (int is = b.ns - 1; is >= 0; is--) {
     int ip = i + is + 1;
-    if (ip >= s.n2) continue;
-    add_slot(ip, s.ns + is + 1);
-    predict_adj<NW>(s.n1, s.eps, s.eps2, c, tr, pp + (long)(ip - 1) * s.n1, true, my, my.y);
+    if (ip >= n2) continue;
+    add_slot(ip, b.ns + is + 1);
+    predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)(ip - 1) * n1, true, my, my.y);
   }
-  for (int i1 = 0; i1 < s.n1; i1++) {
+  for (int i1 = 0; i1 < n1; i1++) {
     o[i1] = __fadd_rn(0.f, tr[i1]);
     tr[i1] = 0.f;
   }
-  for (int is = s.ns - 1; is >= 0; is--) {
+  for (int is = b.ns - 1; is >= 0; is--) {
     int ip = i - is - 1;
     if (ip < 0) continue;
-    add_slot(ip, s.ns - is - 1);
-    predict_adj<NW>(s.n1, s.eps, s.eps2, c, tr, pp + (long)ip * s.n1, false, my, my.y);
+    add_slot(ip, b.ns - is - 1);
+    predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)ip * n1, false, my, my.y);
   }
-  const float wc = tri_weight(s.ns, s.ns);
-  for (int i1 = 0; i1 < s.n1; i1++) {
-    long e = (long)i * s.n1 + i1;
+  const float wc = tri_weight(b.ns, b.ns);
+  for (int i1 = 0; i1 < n1; i1++) {
+    long e = (long)i * n1 + i1;
     float v = __fadd_rn(o[i1], tr[i1]);
     o[i1] = __fadd_rn(v, __fmul_rn(__fmul_rn(X[e], wc), W[e]));
   }
 }
 
-struct SprayWork {
-  float *u, *w1, *ones, *v2, *avg, *tbuf;
-  PredictScratch sc;
-};
-
-SprayWork carve_spray2(void* ws, int n1, int n2, int n3, int ns, int order, bool need_w1,
-                       bool need_svmf, bool adj, size_t* total) {
-  const long n = (long)n1 * n2 * n3;
-  const int np = 2 * ns + 1, nb = 2 * order;
-  const long nthr = 2L * n2 * n3;
-  Carver cv(ws);
-  SprayWork w;
-  w.u = cv.take<float>(n * np);
-  w.w1 = need_w1 ? cv.take<float>(n) : nullptr;
-  w.ones = cv.take<float>(n1);
-  w.v2 = need_svmf ? cv.take<float>(n * np) : nullptr;
-  w.avg = need_svmf ? cv.take<float>((long)n2 * n3) : nullptr;
-  w.tbuf = adj ? cv.take<float>(n) : nullptr;
-  w.sc.o = cv.take<float>((long)nb * n1 * nthr);
-  w.sc.d = cv.take<float>((long)n1 * nthr);
-  w.sc.y = cv.take<float>((long)n1 * nthr);
-  w.sc.ss = nthr;
-  *total = cv.size();
-  return w;
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsec) return;
+  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
 }
+
+__global__ void k_put_single(SecDesc* dst, SecDesc v) { *dst = v; }
 
 __global__ void k_fill(float* x, float v, long n) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i < n) x[i] = v;
 }
 
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+enum Filter { kMean = 1, kMeanAdj = 2, kMedian = 3 };
+
+struct SprayLayout {
+  int ntiles;
+  long ntr, nu, nscr, n1max, nsamp;
+};
+
+SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order, bool two_rhs) {
+  SprayLayout L{};
+  const int np = 2 * ns + 1, nb = 2 * order;
+  long u = 0, sc = 0, tr = 0, samp = 0;
+  int tiles = 0;
+  for (auto& s : secs) {
+    s.n = (long)s.n1 * s.n2 * s.n3;
+    s.tile0 = tiles;
+    s.ntile = (int)((s.n + kTile - 1) / kTile);
+    tiles += s.ntile;
+    s.tr0 = tr;
+    tr += (long)s.n2 * s.n3;
+    s.u0 = u;
+    u += s.n * np;
+    s.sc0 = sc;
+    sc += (long)(nb + (two_rhs ? 3 : 2)) * s.n1 * (2L * s.n2 * s.n3);
+    samp = std::max(samp, s.off + s.n);
+    L.n1max = std::max(L.n1max, (long)s.n1);
+  }
+  L.ntiles = tiles;
+  L.ntr = tr;
+  L.nu = u;
+  L.nscr = sc;
+  L.nsamp = samp;
+  return L;
+}
+
+struct SprayWork {
+  SprayBufs bf;
+  float* ones;
+  float *v2, *avg;
+  SecDesc* secs;
+  int* tile_sec;
+};
+
+SprayWork carve2(void* ws, const SprayLayout& L, int nsec, int filter, int option,
+                 size_t* total) {
+  Carver cv(ws);
+  SprayWork w{};
+  const bool mean = filter == kMean || filter == kMeanAdj;
+  w.bf.u = filter == kMeanAdj ? nullptr : cv.take<float>(L.nu);
+  w.bf.u1 = mean ? cv.take<float>(L.nu) : nullptr;
+  w.bf.w1 = filter == kMeanAdj ? cv.take<float>(L.nsamp) : nullptr;
+  w.bf.scr = cv.take<float>(std::max(L.nscr, 1L));
+  w.bf.tbuf = filter == kMeanAdj ? cv.take<float>(L.nsamp) : nullptr;
+  w.ones = cv.take<float>(L.n1max);
+  const bool svmf = filter == kMedian && option != 1;
+  w.v2 = svmf ? cv.take<float>(L.nu) : nullptr;
+  w.avg = svmf ? cv.take<float>(L.ntr) : nullptr;
+  w.secs = cv.take<SecDesc>(nsec);
+  w.tile_sec = cv.take<int>(L.ntiles);
+  *total = cv.size();
+  return w;
+}
+
 template <int NW>
-int spray2_forward(const float* in, const float* dip, const SprayWork& w, const Spray2& s,
-                   cudaStream_t st) {
+int spray2_run(const float* data, const float* dip, float* out, int filter, int option, int nmf,
+               const std::vector<SecDesc>& secs, const SprayLayout& L, const SprayWork& w,
+               int ns, float eps, cudaStream_t st) {
+  const int nsec = (int)secs.size();
   const ApCoef c = make_apcoef(NW);
-  const long nthr = 2L * s.n2 * s.n3;
-  const int b = 64;
-  k_spray2_chains<NW><<<(unsigned)((nthr + b - 1) / b), b, 0, st>>>(in, w.ones, dip, w.u, s, c,
-                                                                    w.sc);
+  SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, ns, 2 * ns + 1, eps * eps, eps * eps};
+  const int bs = 64;
+  const unsigned gch = (unsigned)((2 * L.ntr + bs - 1) / bs);
+  PWD_KERNEL(PWD_FAM_OTHER, st,
+             k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
+  PWD_KERNEL(PWD_FAM_OTHER, st,
+             k_fill<<<(unsigned)((L.n1max + 255) / 256), 256, 0, st>>>(w.ones, 1.0f, L.n1max));
+  // slots whose source lies outside the section stay 0 (pwspray_lop :995)
+  if (w.bf.u && cudaMemsetAsync(w.bf.u, 0, sizeof(float) * L.nu, st) != cudaSuccess)
+    return PWD_ECUDA;
+  if (w.bf.u1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
+    return PWD_ECUDA;
+  if (filter == kMean) {
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_spray2_chains<NW, 1><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+    PWD_KERNEL(PWD_FAM_FILTER, st,
+               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
+  } else if (filter == kMeanAdj) {
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_spray2_chains<NW, 2><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+    PWD_KERNEL(PWD_FAM_FILTER, st,
+               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
+    const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
+  } else {
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_spray2_chains<NW, 0><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+    if (option == 1) {
+      PWD_KERNEL(PWD_FAM_FILTER, st,
+                 k_median_tiles<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
+    } else {
+      for (const SecDesc& s : secs) {  // svmf needs whole-panel means: per section
+        int rc = launch_panel_median(w.bf.u + s.u0, out + s.pout, w.v2 + s.u0, w.avg + s.tr0,
+                                     s.n1, b.np, (long)s.n2 * s.n3, nmf, option, st);
+        if (rc != PWD_OK) return rc;
+      }
+    }
+  }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
-int spray2_forward_dispatch(int order, const float* in, const float* dip, const SprayWork& w,
-                            const Spray2& s, cudaStream_t st) {
+int spray2_dispatch(int order, const float* data, const float* dip, float* out, int filter,
+                    int option, int nmf, const std::vector<SecDesc>& secs, const SprayLayout& L,
+                    const SprayWork& w, int ns, float eps, cudaStream_t st) {
   switch (order) {
-    case 1: return spray2_forward<1>(in, dip, w, s, st);
-    case 2: return spray2_forward<2>(in, dip, w, s, st);
-    case 3: return spray2_forward<3>(in, dip, w, s, st);
-    case 4: return spray2_forward<4>(in, dip, w, s, st);
+    case 1: return spray2_run<1>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+    case 2: return spray2_run<2>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+    case 3: return spray2_run<3>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+    case 4: return spray2_run<4>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
   }
   return PWD_ENOTSUP;
-}
-
-int somean2d_adj_dispatch(int order, const float* x, const float* dip, float* out,
-                          const SprayWork& w, const Spray2& s, cudaStream_t st) {
-  const long nthr = (long)s.n2 * s.n3;
-  const int b = 64;
-  const unsigned g = (unsigned)((nthr + b - 1) / b);
-  switch (order) {
-    case 1: k_somean2d_adj<1><<<g, b, 0, st>>>(x, dip, w.w1, out, w.tbuf, s, make_apcoef(1), w.sc); break;
-    case 2: k_somean2d_adj<2><<<g, b, 0, st>>>(x, dip, w.w1, out, w.tbuf, s, make_apcoef(2), w.sc); break;
-    case 3: k_somean2d_adj<3><<<g, b, 0, st>>>(x, dip, w.w1, out, w.tbuf, s, make_apcoef(3), w.sc); break;
-    case 4: k_somean2d_adj<4><<<g, b, 0, st>>>(x, dip, w.w1, out, w.tbuf, s, make_apcoef(4), w.sc); break;
-    default: return PWD_ENOTSUP;
-  }
-  return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
 int check2(int n1, int n2, int n3, int ns, int order) {
   if (n1 < 4 || n2 < 1 || n3 < 1 || ns < 0 || order < 1) return PWD_EINVAL;
   if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  return PWD_OK;
+}
+
+std::vector<SecDesc> single(int n1, int n2, int n3) {
+  std::vector<SecDesc> v(1, SecDesc{});
+  v[0].n1 = n1;
+  v[0].n2 = n2;
+  v[0].n3 = n3;
+  return v;
+}
+
+size_t need_single(int n1, int n2, int n3, int ns, int order, int filter, int option) {
+  std::vector<SecDesc> secs = single(n1, n2, n3);
+  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  size_t need = 0;
+  carve2(nullptr, L, 1, filter, option, &need);
+  return need;
+}
+
+int run_single(const float* data, const float* dip, float* out, int n1, int n2, int n3, int ns,
+               int order, float eps, int filter, int option, int nmf, void* ws, size_t wsb,
+               cudaStream_t st) {
+  std::vector<SecDesc> secs = single(n1, n2, n3);
+  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  size_t need = 0;
+  carve2(nullptr, L, 1, filter, option, &need);
+  if (!ws || wsb < need || ((uintptr_t)ws & 255)) return PWD_EWORKSPACE;
+  SprayWork w = carve2(ws, L, 1, filter, option, &need);
+  PWD_KERNEL(PWD_FAM_OTHER, st, k_put_single<<<1, 1, 0, st>>>(w.secs, secs[0]));
+  return spray2_dispatch(order, data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+}
+
+int batch_table2(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
+  if (!in || nsec < 1) return PWD_EINVAL;
+  secs.assign(nsec, SecDesc{});
+  for (int i = 0; i < nsec; i++) {
+    if (check2(in[i].n1, in[i].n2, in[i].n3, 0, 1) != PWD_OK || in[i].offset < 0 ||
+        in[i].out_offset < 0)
+      return PWD_EINVAL;
+    secs[i].off = in[i].offset;
+    secs[i].pout = in[i].out_offset;
+    secs[i].n1 = in[i].n1;
+    secs[i].n2 = in[i].n2;
+    secs[i].n3 = in[i].n3;
+  }
   return PWD_OK;
 }
 
@@ -236,9 +422,8 @@ using namespace pwd;
 
 extern "C" size_t pwd_somean2d_workspace_size(int n1, int n2, int n3, int ns, int order) {
   if (check2(n1, n2, n3, ns, order) != PWD_OK) return 0;
-  size_t t = 0;
-  carve_spray2(nullptr, n1, n2, n3, ns, order, true, false, true, &t);
-  return t;
+  return std::max(need_single(n1, n2, n3, ns, order, kMean, 1),
+                  need_single(n1, n2, n3, ns, order, kMeanAdj, 1));
 }
 
 extern "C" int pwd_somean2d(const float* data, const float* dip, float* out, int n1, int n2,
@@ -247,38 +432,14 @@ extern "C" int pwd_somean2d(const float* data, const float* dip, float* out, int
   int rc = check2(n1, n2, n3, ns, order);
   if (rc != PWD_OK) return rc;
   if (!data || !dip || !out) return PWD_EINVAL;
-  size_t need = 0;
-  carve_spray2(nullptr, n1, n2, n3, ns, order, true, false, true, &need);
-  if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  SprayWork w = carve_spray2(workspace, n1, n2, n3, ns, order, true, false, true, &need);
-  cudaStream_t st = (cudaStream_t)stream;
-  Spray2 s;
-  s.n1 = n1; s.n2 = n2; s.n3 = n3; s.ns = ns; s.np = 2 * ns + 1;
-  s.eps = eps * eps;  // pwspray_init :928 predict_init(eps*eps, ...)
-  s.eps2 = s.eps;
-  const long n = (long)n1 * n2 * n3;
-  const int b = 256;
-  const unsigned gn = (unsigned)((n + b - 1) / b);
-  k_fill<<<(unsigned)((n1 + b - 1) / b), b, 0, st>>>(w.ones, 1.0f, n1);
-  // pwsmooth_set: spray of ones and its weighted sum
-  if ((rc = spray2_forward_dispatch(order, nullptr, dip, w, s, st)) != PWD_OK) return rc;
-  k_norm_weights<<<gn, b, 0, st>>>(w.u, w.w1, s);
-  if (adj) {
-    rc = somean2d_adj_dispatch(order, data, dip, out, w, s, st);
-    if (rc != PWD_OK) return rc;
-  } else {
-    if ((rc = spray2_forward_dispatch(order, data, dip, w, s, st)) != PWD_OK) return rc;
-    k_weighted_mean<<<gn, b, 0, st>>>(w.u, w.w1, out, s);
-  }
-  return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
+  return run_single(data, dip, out, n1, n2, n3, ns, order, eps, adj ? kMeanAdj : kMean, 1, 0,
+                    workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 extern "C" size_t pwd_somf2d_workspace_size(int n1, int n2, int n3, int ns, int nmf, int option,
                                             int order) {
   if (check2(n1, n2, n3, ns, order) != PWD_OK || !median_args_ok(nmf, option)) return 0;
-  size_t t = 0;
-  carve_spray2(nullptr, n1, n2, n3, ns, order, false, option != 1, false, &t);
-  return t;
+  return need_single(n1, n2, n3, ns, order, kMedian, option);
 }
 
 extern "C" int pwd_somf2d(const float* data, const float* dip, float* out, int n1, int n2, int n3,
@@ -288,17 +449,43 @@ extern "C" int pwd_somf2d(const float* data, const float* dip, float* out, int n
   if (rc != PWD_OK) return rc;
   if (!data || !dip || !out) return PWD_EINVAL;
   if (!median_args_ok(nmf, option)) return nmf < 1 ? PWD_EINVAL : PWD_ENOTSUP;
+  return run_single(data, dip, out, n1, n2, n3, ns, order, eps, kMedian, option, nmf, workspace,
+                    workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t pwd_sofilter2d_batch_workspace_size(const pwd_section* sections, int nsec,
+                                                      int ns, int order, int filter, int nmf,
+                                                      int option) {
+  std::vector<SecDesc> secs;
+  if (ns < 0 || order < 1 || order > PWD_MAX_ORDER || filter < 1 || filter > 3) return 0;
+  if (filter == kMedian && !median_args_ok(nmf, option)) return 0;
+  if (batch_table2(sections, nsec, secs) != PWD_OK) return 0;
+  SprayLayout L = layout2(secs, ns, order, filter == kMean);
   size_t need = 0;
-  carve_spray2(nullptr, n1, n2, n3, ns, order, false, option != 1, false, &need);
+  carve2(nullptr, L, nsec, filter, option, &need);
+  return need;
+}
+
+extern "C" int pwd_sofilter2d_batch(const float* data, const float* dip, float* out,
+                                    const pwd_section* sections, int nsec, int ns, int order,
+                                    int filter, int nmf, int option, float eps, void* workspace,
+                                    size_t workspace_bytes, pwd_stream_t stream) {
+  if (!data || !dip || !out || ns < 0 || order < 1 || filter < 1 || filter > 3) return PWD_EINVAL;
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  if (filter == kMedian && !median_args_ok(nmf, option)) return nmf < 1 ? PWD_EINVAL : PWD_ENOTSUP;
+  std::vector<SecDesc> secs;
+  int rc = batch_table2(sections, nsec, secs);
+  if (rc != PWD_OK) return rc;
+  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  size_t need = 0;
+  carve2(nullptr, L, nsec, filter, option, &need);
   if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  SprayWork w = carve_spray2(workspace, n1, n2, n3, ns, order, false, option != 1, false, &need);
+  SprayWork w = carve2(workspace, L, nsec, filter, option, &need);
   cudaStream_t st = (cudaStream_t)stream;
-  Spray2 s;
-  s.n1 = n1; s.n2 = n2; s.n3 = n3; s.ns = ns; s.np = 2 * ns + 1;
-  s.eps = eps * eps;
-  s.eps2 = s.eps;
-  if ((rc = spray2_forward_dispatch(order, data, dip, w, s, st)) != PWD_OK) return rc;
-  return launch_panel_median(w.u, out, w.v2, w.avg, n1, s.np, (long)n2 * n3, nmf, option, st);
+  if (cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PWD_ECUDA;
+  return spray2_dispatch(order, data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
 }
 
 extern "C" size_t pwd_panel_median_workspace_size(int n1, int np, long ntr, int nmf, int option) {

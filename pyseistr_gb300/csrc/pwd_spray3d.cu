@@ -177,10 +177,10 @@ int spray3(const float* d, const float* p1, const float* p2, const Spray3Work& w
   const int b = 64;
   const unsigned g = (unsigned)((n23 + b - 1) / b);
   switch (order) {
-    case 1: k_spray3_tree<1><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(1), w.sc); break;
-    case 2: k_spray3_tree<2><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(2), w.sc); break;
-    case 3: k_spray3_tree<3><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(3), w.sc); break;
-    case 4: k_spray3_tree<4><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(4), w.sc); break;
+    case 1: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<1><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(1), w.sc)); break;
+    case 2: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<2><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(2), w.sc)); break;
+    case 3: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<3><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(3), w.sc)); break;
+    case 4: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<4><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(4), w.sc)); break;
     default: return PWD_ENOTSUP;
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
@@ -215,7 +215,7 @@ extern "C" int pwd_somean3d(const float* data, const float* dip_inline, const fl
     return rc;
   const long n = (long)n1 * n2 * n3;
   const int np = (2 * r1 + 1) * (2 * r2 + 1);
-  k_panel_mean<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w.u, out, n1, np, (long)n2 * n3);
+  PWD_KERNEL(PWD_FAM_FILTER, st, k_panel_mean<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w.u, out, n1, np, (long)n2 * n3));
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 

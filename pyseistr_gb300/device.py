@@ -145,3 +145,63 @@ def panel_median(panels, nmf, option=1, out=None, workspace=None):
     _lib.check(L.pwd_panel_median(_ptr(panels), _ptr(out), n1, npn, ntr, nmf, option, _ptr(ws),
                                   ws.numel(), _stream()), "panel_median")
     return out
+
+
+def section_table(shapes, offsets=None, out_offsets=None):
+    """ctypes array of pwd_section for sections of the given shapes packed
+    one after another (or at the given element offsets)."""
+    n = len(shapes)
+    tab = (_lib.Section * n)()
+    off = oof = 0
+    for k, sh in enumerate(shapes):
+        n1, n2 = int(sh[0]), int(sh[1])
+        n3 = int(sh[2]) if len(sh) > 2 else 1
+        tab[k].offset = off if offsets is None else int(offsets[k])
+        tab[k].out_offset = oof if out_offsets is None else int(out_offsets[k])
+        tab[k].n1, tab[k].n2, tab[k].n3 = n1, n2, n3
+        size = n1 * n2 * n3
+        off += size
+        oof += size if n3 == 1 else 2 * size
+    return tab, off, oof
+
+
+def dip_batch(data, shapes, niter=5, liter=20, order=2, rect=(10, 10, 1), mask=None, out=None,
+              workspace=None):
+    """Slopes of many sections packed one after another in `data` (flat,
+    each section column-major), all in one launch sequence.  Returns the
+    packed slopes (n per 2-D section, 2n per cube)."""
+    L = _lib.load()
+    tab, ntot, nout = section_table(shapes)
+    data = _as_flat(data, ntot, "data")
+    if mask is not None:
+        mask = _as_flat(mask, ntot, "mask")
+    rc = (ctypes.c_int * 3)(*[int(r) for r in rect])
+    nbytes = L.pwd_dip_batch_workspace_size(tab, len(shapes), order, rc, int(mask is not None))
+    ws = _workspace(nbytes, data.device, workspace)
+    if out is None:
+        out = torch.empty(nout, dtype=torch.float32, device=data.device)
+    _lib.check(L.pwd_dip_batch(_ptr(data), _ptr(mask), _ptr(out), tab, len(shapes), niter, liter,
+                               order, rc, _ptr(ws), ws.numel(), _stream()), "dip_batch")
+    return out
+
+
+FILTER_MEAN, FILTER_MEAN_ADJ, FILTER_MEDIAN = 1, 2, 3
+
+
+def sofilter2d_batch(data, dip_, shapes, ns, order=2, eps=0.01, filter=FILTER_MEAN, nmf=None,
+                     option=1, out=None, workspace=None):
+    """Structure-oriented mean (filter 1), adjoint mean (2) or median (3) of
+    many 2-D sections packed one after another in `data` / `dip_`."""
+    L = _lib.load()
+    tab, ntot, _ = section_table(shapes, out_offsets=None)
+    for k in range(len(shapes)):  # filter output uses the data layout
+        tab[k].out_offset = tab[k].offset
+    data, dip_ = _as_flat(data, ntot, "data"), _as_flat(dip_, ntot, "dip")
+    nmf = 2 * ns + 1 if nmf is None else nmf
+    nbytes = L.pwd_sofilter2d_batch_workspace_size(tab, len(shapes), ns, order, filter, nmf, option)
+    ws = _workspace(nbytes, data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_sofilter2d_batch(_ptr(data), _ptr(dip_), _ptr(out), tab, len(shapes), ns,
+                                      order, filter, nmf, option, float(eps), _ptr(ws), ws.numel(),
+                                      _stream()), "sofilter2d_batch")
+    return out

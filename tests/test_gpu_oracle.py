@@ -124,3 +124,49 @@ def test_full_size_properties(ps):
     zp = np.zeros_like(p)
     med = ps.somf2dc(c, zp, 10, 2, 0.01)
     assert np.abs(med - 0.75).max() < 1e-3
+
+
+def test_dip_batch_equals_per_section(ps):
+    """A batch of uneven sections (2-D and 3-D mixed) gives bit for bit the
+    slopes of one call per section."""
+    import torch
+    import workloads
+    from pyseistr_gb300 import device as D
+
+    secs = [s[: max(40, s.shape[0] // 4), : max(12, s.shape[1] // 6)].copy()
+            for s in workloads.batch2d(count=6)]
+    cube = workloads.plain3d()[:50, :9, :7].copy()
+    shapes = [s.shape for s in secs] + [cube.shape]
+    flat = np.concatenate([s.reshape(-1, order="F") for s in secs] + [cube.reshape(-1, order="F")])
+    out = D.dip_batch(torch.from_numpy(flat).cuda(), shapes, 3, 6, 2, (5, 4, 3)).cpu().numpy()
+    k = 0
+    for s in secs:
+        want = ps.dip2dc(s, 3, 6, 2, rect=[5, 4, 3])
+        assert np.array_equal(out[k:k + s.size].reshape(s.shape, order="F"), want)
+        k += s.size
+    wi, wx = ps.dip3dc(cube, 3, 6, 2, rect=[5, 4, 3])
+    assert np.array_equal(out[k:k + cube.size].reshape(cube.shape, order="F"), wi)
+    assert np.array_equal(out[k + cube.size:].reshape(cube.shape, order="F"), wx)
+
+
+@pytest.mark.parametrize("flt", [1, 2, 3])
+def test_sofilter2d_batch_equals_per_section(ps, O, flt):
+    import torch
+    import workloads
+    from pyseistr_gb300 import device as D
+
+    secs = [s[: max(30, s.shape[0] // 5), : max(10, s.shape[1] // 8)].copy()
+            for s in workloads.batch2d(count=5, seed=7)]
+    dips = [O.dip2d(s, 2, 4, 2, (4, 4, 1)) for s in secs]
+    shapes = [s.shape for s in secs]
+    fl = lambda xs: np.concatenate([x.reshape(-1, order="F") for x in xs])
+    out = D.sofilter2d_batch(torch.from_numpy(fl(secs)).cuda(), torch.from_numpy(fl(dips)).cuda(),
+                             shapes, 3, 2, 0.01, filter=flt).cpu().numpy()
+    k = 0
+    for s, p in zip(secs, dips):
+        if flt == 3:
+            want = O.somf2d(s, p, 3, 2, 0.01)
+        else:
+            want = O.somean2d(s, p, 3, 2, 0.01, adj=flt - 1)
+        assert np.array_equal(out[k:k + s.size].reshape(s.shape, order="F"), want)
+        k += s.size
