@@ -20,6 +20,7 @@
 // restatement against them.
 
 #include <algorithm>
+#include <cfenv>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -918,7 +919,11 @@ struct SprayMedian {
     n1 = n1_; np = np_; nmf = nmf_; option = option_;
     int nfilter = (option == 1) ? nmf : nmf + 2;
     m = (nfilter - 1) / 2;
-    ext.assign((long)n1 * (np + 2 * m), 0);
+    // One row more than boundary() fills: svmf's first pass reads one row
+    // past the padded panel for its last row (sof_cfuns.c:1366-1376, an
+    // out-of-bounds read in the reference); here that row is one more
+    // replica of the last trace, as the padding rows are.
+    ext.assign((long)n1 * (np + 2 * m + 1), 0);
     tmp.assign(nfilter + 8, 0);
     trace2.assign((long)n1 * np, 0);
   }
@@ -927,7 +932,7 @@ struct SprayMedian {
       for (int j = 0; j < n1; j++) ext[(long)n1 * i + j] = tt[j];
     for (int i = 0; i < np; i++)
       for (int j = 0; j < n1; j++) ext[(long)n1 * (i + m) + j] = tt[(long)n1 * i + j];
-    for (int i = 0; i < m; i++)
+    for (int i = 0; i < m + 1; i++)
       for (int j = 0; j < n1; j++) ext[(long)n1 * (i + np + m) + j] = tt[(long)n1 * (np - 1) + j];
   }
   // out[n1] = row `row` of the filtered panel
@@ -1321,21 +1326,39 @@ static int soint3d(const R* din, const R* mask, const R* pp, const R* qq, R* dou
 // ---------------------------------------------------------------------------
 // C ABI of the oracle (f32 = reference arithmetic, f64 = FP64 oracle).
 // ---------------------------------------------------------------------------
+namespace {
+// Every entry point runs in the default floating-point environment (IEEE
+// denormals, round to nearest), whatever libraries loaded into the process
+// have set: some set flush-to-zero at load time, which the reference does
+// not run with.
+struct DefaultFpEnv {
+  std::fenv_t saved;
+  DefaultFpEnv() {
+    std::fegetenv(&saved);
+    std::fesetenv(FE_DFL_ENV);
+  }
+  ~DefaultFpEnv() { std::fesetenv(&saved); }
+};
+}  // namespace
+
 extern "C" {
 
 int orc_dip_f32(const float* u, const float* mask, float* p, int n1, int n2, int n3, int niter,
                 int liter, int order, int r1, int r2, int r3, int flags, int* ls) {
+  DefaultFpEnv fpenv;
   int rect[3] = {r1, r2, r3};
   return orc::dipc<float>(u, mask, p, n1, n2, n3, niter, liter, order, rect, flags, ls);
 }
 int orc_dip_f64(const double* u, const double* mask, double* p, int n1, int n2, int n3,
                 int niter, int liter, int order, int r1, int r2, int r3, int flags, int* ls) {
+  DefaultFpEnv fpenv;
   int rect[3] = {r1, r2, r3};
   return orc::dipc<double>(u, mask, p, n1, n2, n3, niter, liter, order, rect, flags, ls);
 }
 
 int orc_pwspray2d_f32(const float* d, const float* p, float* u, int n1, int n2, int ns,
                       int order, float eps) {
+  DefaultFpEnv fpenv;
   if (n1 < 4 || n2 < 1 || ns < 0 || order < 1 || order > 8) return orc::ORC_EINVAL;
   orc::Predict<float> pr;
   pr.init(n1, eps * eps, order, false);
@@ -1345,23 +1368,28 @@ int orc_pwspray2d_f32(const float* d, const float* p, float* u, int n1, int n2, 
 
 int orc_somean2d_f32(const float* d, const float* p, float* out, int n1, int n2, int n3, int ns,
                      int order, float eps, int adj) {
+  DefaultFpEnv fpenv;
   return orc::somean2d<float>(d, p, out, n1, n2, n3, ns, order, eps, adj);
 }
 int orc_somean2d_f64(const double* d, const double* p, double* out, int n1, int n2, int n3,
                      int ns, int order, double eps, int adj) {
+  DefaultFpEnv fpenv;
   return orc::somean2d<double>(d, p, out, n1, n2, n3, ns, order, eps, adj);
 }
 int orc_somf2d_f32(const float* d, const float* p, float* out, int n1, int n2, int n3, int ns,
                    int nmf, int option, int order, float eps) {
+  DefaultFpEnv fpenv;
   return orc::somf2d<float>(d, p, out, n1, n2, n3, ns, nmf, option, order, eps);
 }
 int orc_somf2d_f64(const double* d, const double* p, double* out, int n1, int n2, int n3, int ns,
                    int nmf, int option, int order, double eps) {
+  DefaultFpEnv fpenv;
   return orc::somf2d<double>(d, p, out, n1, n2, n3, ns, nmf, option, order, eps);
 }
 
 int orc_pwspray3d_f32(const float* d, const float* p1, const float* p2, float* u, int n1, int n2,
                       int n3, int r1, int r2, int order) {
+  DefaultFpEnv fpenv;
   if (n1 < 4 || n2 < 1 || n3 < 1 || r1 < 0 || r2 < 0 || order < 1 || order > 8)
     return orc::ORC_EINVAL;
   orc::pwspray3<float>(n1, n2, n3, r1, r2, order, d, p1, p2, u);
@@ -1369,18 +1397,22 @@ int orc_pwspray3d_f32(const float* d, const float* p1, const float* p2, float* u
 }
 int orc_somean3d_f32(const float* d, const float* p1, const float* p2, float* out, int n1,
                      int n2, int n3, int r1, int r2, int order) {
+  DefaultFpEnv fpenv;
   return orc::somean3d<float>(d, p1, p2, out, n1, n2, n3, r1, r2, order);
 }
 int orc_somean3d_f64(const double* d, const double* p1, const double* p2, double* out, int n1,
                      int n2, int n3, int r1, int r2, int order) {
+  DefaultFpEnv fpenv;
   return orc::somean3d<double>(d, p1, p2, out, n1, n2, n3, r1, r2, order);
 }
 int orc_somf3d_f32(const float* d, const float* p1, const float* p2, float* out, int n1, int n2,
                    int n3, int r1, int r2, int nmf, int option, int order) {
+  DefaultFpEnv fpenv;
   return orc::somf3d<float>(d, p1, p2, out, n1, n2, n3, r1, r2, nmf, option, order);
 }
 int orc_somf3d_f64(const double* d, const double* p1, const double* p2, double* out, int n1,
                    int n2, int n3, int r1, int r2, int nmf, int option, int order) {
+  DefaultFpEnv fpenv;
   return orc::somf3d<double>(d, p1, p2, out, n1, n2, n3, r1, r2, nmf, option, order);
 }
 
@@ -1388,6 +1420,7 @@ int orc_somf3d_f64(const double* d, const double* p1, const double* p2, double* 
 // (the selection step alone, for the bit-exact median check).
 int orc_spray_median_f32(const float* u, float* out, int n1, int np, long ntr, int nmf,
                          int option) {
+  DefaultFpEnv fpenv;
   if (n1 < 1 || np < 1 || nmf < 1 || (option != 1 && nmf < 5)) return orc::ORC_EINVAL;
   orc::SprayMedian<float> med;
   med.init(n1, np, nmf, option);
@@ -1398,12 +1431,14 @@ int orc_spray_median_f32(const float* u, float* out, int n1, int np, long ntr, i
 int orc_soint3d_f32(const float* din, const float* mask, const float* pp, const float* qq,
                     float* out, int n1, int n2, int n3, int nw, int nj1, int nj2, int niter,
                     int drift, int seed, int hasmask, float var) {
+  DefaultFpEnv fpenv;
   return orc::soint3d<float>(din, mask, pp, qq, out, n1, n2, n3, nw, nj1, nj2, niter, drift, seed,
                              hasmask, var);
 }
 int orc_soint3d_f64(const double* din, const double* mask, const double* pp, const double* qq,
                     double* out, int n1, int n2, int n3, int nw, int nj1, int nj2, int niter,
                     int drift, int seed, int hasmask, double var) {
+  DefaultFpEnv fpenv;
   return orc::soint3d<double>(din, mask, pp, qq, out, n1, n2, n3, nw, nj1, nj2, niter, drift,
                               seed, hasmask, var);
 }
