@@ -143,6 +143,84 @@ __device__ __forceinline__ float ader_tap(const ApCoef& c, int k, float p) {
   return __double2float_rn(__dmul_rn(ak, c.b[k]));
 }
 
+// Per-thread accumulator of a dot product of floats in float-float: each
+// product is split exactly (FMA), sums are error-free (TwoSum) up to the
+// low word, about 2^-45 relative over a thread's few terms; converted to
+// double for the block and tile sums.  This keeps the double accuracy of
+// the reference's dsdot (dip_cfuns.c:122) without per-sample FP64 work.
+struct ffacc {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    float p = __fmul_rn(a, b);
+    float pe = __fmaf_rn(a, b, -p);
+    ff s = ff_two_sum(h, p);
+    h = s.h;
+    l = __fadd_rn(l, __fadd_rn(s.l, pe));
+  }
+  __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
+// (float) (x * s) for a double scale s, as the reference's float*double
+// products (dip_cfuns.c:807, :822): float-float product, FP64 near ties.
+__device__ __forceinline__ float mul_by_double(float x, float sh, float sl, double s) {
+  if (x == 0.f) return __fmul_rn(x, sh);
+  float ph = __fmul_rn(x, sh);
+  float pl = __fmaf_rn(x, sh, -ph);
+  pl = __fmaf_rn(x, sl, pl);
+  float h = __fadd_rn(ph, pl);
+  float l = __fsub_rn(pl, __fsub_rn(h, ph));
+  if (!ff_near_tie(h, l, fabsf(h) * 0x1p-40f)) return h;
+  return __double2float_rn(__dmul_rn((double)x, s));
+}
+
+// num = r / hypot(d, 1), den = d / hypot(d, 1), each rounded as the
+// reference's double computation 1.0/hypot(d,1.0) then float*double
+// (dip_cfuns.c:804-808): float-float sqrt and reciprocal, FP64 near ties.
+__device__ __forceinline__ void invhypot_scale(float r, float d, float& num, float& den) {
+  if (d == 0.f) {  // 1/hypot(0,1) = 1 exactly
+    num = __fmul_rn(r, 1.f);
+    den = __fmul_rn(d, 1.f);
+    return;
+  }
+  float dh = __fmul_rn(d, d), dl = __fmaf_rn(d, d, -dh);
+  ff q = ff_two_sum(1.0f, dh);
+  q = ff_two_sum(q.h, __fadd_rn(q.l, dl));
+  bool exact = isfinite(q.h);
+  float sh = __fsqrt_rn(q.h);
+  float t = __fadd_rn(__fmaf_rn(-sh, sh, q.h), q.l);
+  float sl = __fdiv_rn(t, __fmul_rn(2.f, sh));
+  float ih = __fdiv_rn(1.f, sh);
+  float ph = __fmul_rn(sh, ih), pl = __fmaf_rn(sh, ih, -ph);
+  float e = __fsub_rn(__fsub_rn(1.f, ph), pl);
+  e = __fsub_rn(e, __fmul_rn(sl, ih));
+  float il = __fmul_rn(ih, e);
+  float out[2];
+  const float in[2] = {r, d};
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    float x = in[k];
+    if (x == 0.f) {
+      out[k] = __fmul_rn(x, ih);
+      continue;
+    }
+    float nh = __fmul_rn(x, ih);
+    float nl = __fmaf_rn(x, ih, -nh);
+    nl = __fmaf_rn(x, il, nl);
+    float h = __fadd_rn(nh, nl);
+    float l = __fsub_rn(nl, __fsub_rn(h, nh));
+    out[k] = h;
+    if (ff_near_tie(h, l, fabsf(h) * 0x1p-38f)) exact = false;
+  }
+  if (exact) {
+    num = out[0];
+    den = out[1];
+    return;
+  }
+  double nrm = 1.0 / hypot((double)d, 1.0);
+  num = __double2float_rn(__dmul_rn((double)r, nrm));
+  den = __double2float_rn(__dmul_rn((double)d, nrm));
+}
+
 template <int NW>
 __device__ __forceinline__ void passfilter(const ApCoef& c, float p, float* a) {
 #pragma unroll

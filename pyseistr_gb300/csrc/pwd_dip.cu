@@ -157,24 +157,24 @@ __global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
   float *u2 = a.u2 + s.off, *u1 = a.u1 + s.off, *p0 = a.p0 + s.off;
   const uint8_t* mask = a.mask ? a.mask + s.off : nullptr;
   const long ip = nb_offset(s, dip);
-  dvec<2> acc = {{0.0, 0.0}};
+  ffacc a0, a1;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float pi = p[i];
     float d = pwd_valid(s, i, NW, dip) ? pwd_at<NW, true>(u, i, ip, c, pi) : 0.f;
     float r = u2[i];
-    acc.v[0] += (double)r * (double)r;
+    a0.add_prod(r, r);
     p0[i] = pi;
     if (mask && mask[i]) {
       d = 0.f;
       r = 0.f;
     }
-    double nrm = 1.0 / hypot((double)d, 1.0);
-    float num = __double2float_rn(__dmul_rn((double)r, nrm));
-    float den = __double2float_rn(__dmul_rn((double)d, nrm));
+    float num, den;
+    invhypot_scale(r, d, num, den);
     u2[i] = num;
     u1[i] = den;
-    acc.v[1] += (double)den * (double)den;
+    a1.add_prod(den, den);
   }
+  dvec<2> acc = {{a0.value(), a1.value()}};
   DipScalars* S = b.S + tr.sec;
   dvec<2> tot;
   if (sec_sum_last<2>(acc, b, t, s, &S->cnt[0], tot) && threadIdx.x == 0) {
@@ -199,19 +199,22 @@ __global__ void k_scale(DipArrays a, DipBatch b, int dip) {
   const double nrm = S->norm2;
   float *num = a.u2 + s.off, *den = a.u1 + s.off, *r = a.r + s.off, *pcg = a.pcg + s.off,
         *x = a.dp + s.off;
-  dvec<1> acc = {{0.0}};
+  const float nh = __double2float_rn(nrm);
+  const float nl = __double2float_rn(nrm - (double)nh);
+  ffacc a0;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     x[i] = 0.f;
     if (zero) continue;
-    float va = __double2float_rn(__dmul_rn((double)num[i], nrm));
-    float vb = __double2float_rn(__dmul_rn((double)den[i], nrm));
+    float va = mul_by_double(num[i], nh, nl, nrm);
+    float vb = mul_by_double(den[i], nh, nl, nrm);
     num[i] = va;
     den[i] = vb;
     float ri = -va;
     r[i] = ri;
     pcg[i] = 0.f;
-    acc.v[0] += (double)ri * (double)ri;
+    a0.add_prod(ri, ri);
   }
+  dvec<1> acc = {{a0.value()}};
   dvec<1> tot;
   if (sec_sum_last<1>(acc, b, t, s, &S->cnt[1], tot) && threadIdx.x == 0) {
     S->r0 = tot.v[0];
@@ -268,13 +271,14 @@ __global__ void k_cg_gp(DipArrays a, DipBatch b, int iter) {
   if (S->cg_done) return;
   const float* pcg = a.pcg + s.off;
   float *tmp = a.tmp + s.off, *gp = a.gp + s.off;
-  dvec<1> acc = {{0.0}};
+  ffacc a0;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float v = __fadd_rn(pcg[i], tmp[i]);
     gp[i] = v;
     tmp[i] = v;
-    acc.v[0] += (double)v * (double)v;
+    a0.add_prod(v, v);
   }
+  dvec<1> acc = {{a0.value()}};
   dvec<1> tot;
   if (sec_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0) {
     double gn = tot.v[0];
@@ -301,7 +305,7 @@ __global__ void k_cg_update(DipArrays a, DipBatch b, int iter) {
   const float al = __double2float_rn(S->alpha);
   const float *gp = a.gp + s.off, *tmp = a.tmp + s.off, *w = a.u1 + s.off;
   float *sp = a.sp + s.off, *sx = a.sx + s.off, *sr = a.sr + s.off;
-  dvec<3> acc = {{0.0, 0.0, 0.0}};
+  ffacc a0, a1, a2;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float gx = tmp[i];
     float gr = __fadd_rn(0.f, __fmul_rn(gx, w[i]));
@@ -314,10 +318,11 @@ __global__ void k_cg_update(DipArrays a, DipBatch b, int iter) {
     sp[i] = vp;
     sx[i] = vx;
     sr[i] = vr;
-    acc.v[0] += (double)vr * (double)vr;
-    acc.v[1] += (double)vp * (double)vp;
-    acc.v[2] += (double)vx * (double)vx;
+    a0.add_prod(vr, vr);
+    a1.add_prod(vp, vp);
+    a2.add_prod(vx, vx);
   }
+  dvec<3> acc = {{a0.value(), a1.value(), a2.value()}};
   dvec<3> tot;
   if (sec_sum_last<3>(acc, b, t, s, &S->cnt[3], tot) && threadIdx.x == 0) {
     double beta = tot.v[0] + 1.0 * (tot.v[1] - tot.v[2]);
@@ -353,43 +358,97 @@ __device__ __forceinline__ int sec_of_line(const SecDesc* secs, int nsec, int ax
 
 constexpr int kMaxRect = 64;
 
+constexpr int kTriThreads = 128;
+constexpr int kTriChunk = 8;
+
+// Line geometry of global line g of one axis.
+struct LineGeo {
+  int si, L;
+  long o, d, nl, line;
+};
+__device__ __forceinline__ LineGeo line_geo(const DipBatch& b, const TriParams& tp, long g) {
+  LineGeo q;
+  q.si = sec_of_line(b.secs, b.nsec, tp.axis, g);
+  const SecDesc& s = b.secs[q.si];
+  q.line = g - s.line0[tp.axis];
+  q.L = tp.axis == 0 ? s.n1 : (tp.axis == 1 ? s.n2 : s.n3);
+  q.nl = s.n / q.L;
+  if (tp.axis == 0) {
+    q.o = q.line * s.n1;
+    q.d = 1;
+  } else if (tp.axis == 1) {
+    q.o = (q.line % s.n1) + (q.line / s.n1) * (long)s.n1 * s.n2;
+    q.d = s.n1;
+  } else {
+    q.o = q.line;
+    q.d = (long)s.n1 * s.n2;
+  }
+  return q;
+}
+
+// Forward pass of doubint2 over the spread of triple2: S[m] = sum_{k<=m}
+// v(k), v(m) = ((0 + -wt x[m]) + 2wt x[m-nb]) + -wt x[m-2nb] (terms present
+// where the index is inside the line).  The delayed inputs come from a
+// per-thread ring in shared memory (ring[r*T + tid], conflict free); loads
+// are double-buffered in chunks so that kTriChunk loads are in flight.
+__device__ __forceinline__ void tri_forward(const float* __restrict__ x, long d, int L, int nb,
+                                            float mw, float w2, float* __restrict__ sc, long ss,
+                                            float* ring, int R) {
+  const int T = blockDim.x, tid = threadIdx.x;
+  const int np = L + 2 * nb;
+  float cur[kTriChunk], nxt[kTriChunk];
+#pragma unroll
+  for (int k = 0; k < kTriChunk; k++) cur[k] = k < L ? x[k * d] : 0.f;
+  float acc = 0.f;
+  int r = 0;  // ring slot of x[m]
+  for (int m0 = 0; m0 < np; m0 += kTriChunk) {
+#pragma unroll
+    for (int k = 0; k < kTriChunk; k++) {
+      const int m = m0 + kTriChunk + k;
+      nxt[k] = m < L ? x[m * d] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kTriChunk; k++) {
+      const int m = m0 + k;
+      if (m < np) {
+        const float xm = cur[k];
+        float v = 0.f;
+        if (m < L) v = __fadd_rn(v, __fmul_rn(mw, xm));
+        const int q1 = m - nb, q2 = m - 2 * nb;
+        if (q1 >= 0 && q1 < L) {
+          int rr = r - nb;
+          if (rr < 0) rr += R;
+          v = __fadd_rn(v, __fmul_rn(w2, ring[rr * T + tid]));
+        }
+        if (q2 >= 0 && q2 < L) {
+          int rr = r - 2 * nb;
+          if (rr < 0) rr += R;
+          v = __fadd_rn(v, __fmul_rn(mw, ring[rr * T + tid]));
+        }
+        ring[r * T + tid] = xm;
+        r = (r + 1 == R) ? 0 : r + 1;
+        acc = __fadd_rn(acc, v);
+        sc[m * ss] = acc;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kTriChunk; k++) cur[k] = nxt[k];
+  }
+}
+
 __global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
+  extern __shared__ float ring[];
   long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= tp.nlines) return;
-  const int si = sec_of_line(b.secs, b.nsec, tp.axis, g);
-  if (b.S[si].cg_done) return;
-  const SecDesc& s = b.secs[si];
-  const long line = g - s.line0[tp.axis];
-  const int L = tp.axis == 0 ? s.n1 : (tp.axis == 1 ? s.n2 : s.n3);
-  const long nl = s.n / L;
-  long o, d;
-  if (tp.axis == 0) {
-    o = line * s.n1;
-    d = 1;
-  } else if (tp.axis == 1) {
-    o = (line % s.n1) + (line / s.n1) * (long)s.n1 * s.n2;
-    d = s.n1;
-  } else {
-    o = line;
-    d = (long)s.n1 * s.n2;
-  }
-  float* x = a.tmp + s.off + o;
-  float* sc = a.tri + s.scr0[tp.axis] + line;
-  const long ss = nl;
-  const int nb = tp.nb, np = L + 2 * nb;
-  const float mw = -tp.wt, w2 = tp.w2;
+  const LineGeo q = line_geo(b, tp, g);
+  if (b.S[q.si].cg_done) return;
+  const SecDesc& s = b.secs[q.si];
+  float* x = a.tmp + s.off + q.o;
+  float* sc = a.tri + s.scr0[tp.axis] + q.line;
+  const long ss = q.nl, d = q.d;
+  const int L = q.L, nb = tp.nb, np = L + 2 * nb;
+  tri_forward(x, d, L, nb, -tp.wt, tp.w2, sc, ss, ring, 2 * nb + 1);
   float acc = 0.f;
-  for (int m = 0; m < np; m++) {
-    float v = 0.f;
-    if (m < L) v = __fadd_rn(v, __fmul_rn(mw, x[m * d]));
-    int q = m - nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(w2, x[q * d]));
-    q = m - 2 * nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(mw, x[q * d]));
-    acc = __fadd_rn(acc, v);
-    sc[m * ss] = acc;
-  }
-  acc = 0.f;
   if (nb <= L) {
     // fold2 with one reflection per side: x[i] = B[i+nb], then
     // + B[2L+nb-1-i] for i >= L-nb, then + B[nb-1-i] for i < nb.  The right
@@ -397,22 +456,39 @@ __global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
     // i < nb wait for their left reflection.
     float right[kMaxRect];
     float left_main[kMaxRect];
-    for (int m = np - 1; m >= 0; m--) {
-      acc = __fadd_rn(acc, sc[m * ss]);
-      if (m >= L + nb) {
-        right[m - (L + nb)] = acc;
-      } else if (m >= nb) {
-        const int i = m - nb;
-        float v = acc;
-        if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
-        if (i < nb)
-          left_main[i] = v;
-        else
-          x[i * d] = v;
-      } else {
-        const int i = nb - 1 - m;
-        x[i * d] = __fadd_rn(left_main[i], acc);
+    float cur[kTriChunk], nxt[kTriChunk];
+    const int top = np - 1;
+#pragma unroll
+    for (int k = 0; k < kTriChunk; k++) cur[k] = (top - k >= 0) ? sc[(top - k) * ss] : 0.f;
+    for (int m0 = top; m0 >= 0; m0 -= kTriChunk) {
+#pragma unroll
+      for (int k = 0; k < kTriChunk; k++) {
+        const int m = m0 - kTriChunk - k;
+        nxt[k] = m >= 0 ? sc[m * ss] : 0.f;
       }
+#pragma unroll
+      for (int k = 0; k < kTriChunk; k++) {
+        const int m = m0 - k;
+        if (m >= 0) {
+          acc = __fadd_rn(acc, cur[k]);
+          if (m >= L + nb) {
+            right[m - (L + nb)] = acc;
+          } else if (m >= nb) {
+            const int i = m - nb;
+            float v = acc;
+            if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
+            if (i < nb)
+              left_main[i] = v;
+            else
+              x[i * d] = v;
+          } else {
+            const int i = nb - 1 - m;
+            x[i * d] = __fadd_rn(left_main[i], acc);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kTriChunk; k++) cur[k] = nxt[k];
     }
   } else {
     for (int m = np - 1; m >= 0; m--) {
@@ -450,7 +526,7 @@ __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
   const float *u = a.u + s.off, *p0 = a.p0 + s.off, *dp = a.dp + s.off;
   float *p = a.p + pout_of(s, dip), *u2 = a.u2 + s.off;
   const long ip = nb_offset(s, dip);
-  dvec<1> acc = {{0.0}};
+  ffacc a0;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float pi = __fadd_rn(p0[i], __fmul_rn(lam, dp[i]));
     if (pi < pmin) pi = pmin;
@@ -458,8 +534,9 @@ __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
     p[i] = pi;
     float r = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false>(u, i, ip, c, pi) : 0.f;
     u2[i] = r;
-    acc.v[0] += (double)r * (double)r;
+    a0.add_prod(r, r);
   }
+  dvec<1> acc = {{a0.value()}};
   dvec<1> tot;
   if (sec_sum_last<1>(acc, b, t, s, &S->cnt[4], tot) && threadIdx.x == 0) {
     S->usum2 = tot.v[0];
@@ -615,11 +692,22 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
     tp[nax++] = t;
   }
   const unsigned gt = (unsigned)L.ntiles;
+  {
+    // the delayed-input ring needs up to (2*64+1)*128 floats of shared memory
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_tri_line, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(float) * (2 * kMaxRect + 1) * kTriThreads));
+      attr_set = true;
+    }
+  }
   auto sweeps = [&]() {
     for (int k = 0; k < nax; k++) {
-      const int bs = 128;
+      const int bs = kTriThreads;
+      const size_t smem = sizeof(float) * (2 * tp[k].nb + 1) * bs;
       PWD_KERNEL(PWD_FAM_TRIANGLE, st,
-                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, 0, st>>>(a, b, tp[k]));
+                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, smem, st>>>(a, b,
+                                                                                      tp[k]));
     }
   };
   PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
