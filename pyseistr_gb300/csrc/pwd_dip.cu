@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "pwd_batch.cuh"
@@ -97,12 +98,14 @@ __device__ __forceinline__ bool sec_sum_last(dvec<K> x, const DipBatch& b, int t
   return true;
 }
 
+// Sections hold fewer than 2^31 samples, so 32-bit index arithmetic is used.
 __device__ __forceinline__ bool pwd_valid(const SecDesc& s, long i, int nw, int dip) {
-  int i1 = (int)(i % s.n1);
-  long r = i / s.n1;
+  const unsigned ii = (unsigned)i, n1 = (unsigned)s.n1, n2 = (unsigned)s.n2;
+  const int i1 = (int)(ii % n1);
+  const unsigned r = ii / n1;
   if (i1 < nw || i1 >= s.n1 - nw) return false;
-  if (dip == 1) return (int)(r % s.n2) < s.n2 - 1;
-  return (int)(r / s.n2) < s.n3 - 1;
+  if (dip == 1) return (int)(r % n2) < s.n2 - 1;
+  return (int)(r / n2) < s.n3 - 1;
 }
 
 // allpass1/allpass2 at one sample (dip_cfuns.c:1135-1200, :1399-1465).
@@ -359,7 +362,6 @@ __device__ __forceinline__ int sec_of_line(const SecDesc* secs, int nsec, int ax
 constexpr int kMaxRect = 64;
 
 constexpr int kTriThreads = 128;
-constexpr int kTriChunk = 8;
 
 // Line geometry of global line g of one axis.
 struct LineGeo {
@@ -386,58 +388,78 @@ __device__ __forceinline__ LineGeo line_geo(const DipBatch& b, const TriParams& 
   return q;
 }
 
-// Forward pass of doubint2 over the spread of triple2: S[m] = sum_{k<=m}
-// v(k), v(m) = ((0 + -wt x[m]) + 2wt x[m-nb]) + -wt x[m-2nb] (terms present
-// where the index is inside the line).  The delayed inputs come from a
-// per-thread ring in shared memory (ring[r*T + tid], conflict free); loads
-// are double-buffered in chunks so that kTriChunk loads are in flight.
+// Forward pass of doubint2 over the spread of triple2 for m in [lo, hi):
+// v(m) = (x[m]*-wt + x[m-nb]*2wt) + x[m-2nb]*-wt with the terms T1/T2/T3
+// present (the reference adds each to a zeroed tmp, 0 + a = a for every
+// value the running sum can see); S[m] = S[m-1] + v(m).  The phases of a
+// line are branch-free; the delayed inputs are reloaded (L1 hits).
+template <bool T1, bool T2, bool T3>
+__device__ __forceinline__ float tri_fwd_phase(const float* __restrict__ x, long d, int nb,
+                                               float mw, float w2, float* __restrict__ sc,
+                                               long ss, int lo, int hi, float acc) {
+#pragma unroll 4
+  for (int m = lo; m < hi; m++) {
+    float v;
+    if (T1) v = __fmul_rn(mw, x[m * d]);
+    if (T2) {
+      const float t = __fmul_rn(w2, x[(m - nb) * d]);
+      v = T1 ? __fadd_rn(v, t) : t;
+    }
+    if (T3) {
+      const float t = __fmul_rn(mw, x[(m - 2 * nb) * d]);
+      v = (T1 || T2) ? __fadd_rn(v, t) : t;
+    }
+    acc = __fadd_rn(acc, v);
+    sc[m * ss] = acc;
+  }
+  return acc;
+}
+
+// Whole forward pass of one line (nb <= L).
 __device__ __forceinline__ void tri_forward(const float* __restrict__ x, long d, int L, int nb,
-                                            float mw, float w2, float* __restrict__ sc, long ss,
-                                            float* ring, int R) {
-  const int T = blockDim.x, tid = threadIdx.x;
-  const int np = L + 2 * nb;
-  float cur[kTriChunk], nxt[kTriChunk];
-#pragma unroll
-  for (int k = 0; k < kTriChunk; k++) cur[k] = k < L ? x[k * d] : 0.f;
+                                            float mw, float w2, float* __restrict__ sc,
+                                            long ss) {
   float acc = 0.f;
-  int r = 0;  // ring slot of x[m]
-  for (int m0 = 0; m0 < np; m0 += kTriChunk) {
-#pragma unroll
-    for (int k = 0; k < kTriChunk; k++) {
-      const int m = m0 + kTriChunk + k;
-      nxt[k] = m < L ? x[m * d] : 0.f;
-    }
-#pragma unroll
-    for (int k = 0; k < kTriChunk; k++) {
-      const int m = m0 + k;
-      if (m < np) {
-        const float xm = cur[k];
-        float v = 0.f;
-        if (m < L) v = __fadd_rn(v, __fmul_rn(mw, xm));
-        const int q1 = m - nb, q2 = m - 2 * nb;
-        if (q1 >= 0 && q1 < L) {
-          int rr = r - nb;
-          if (rr < 0) rr += R;
-          v = __fadd_rn(v, __fmul_rn(w2, ring[rr * T + tid]));
-        }
-        if (q2 >= 0 && q2 < L) {
-          int rr = r - 2 * nb;
-          if (rr < 0) rr += R;
-          v = __fadd_rn(v, __fmul_rn(mw, ring[rr * T + tid]));
-        }
-        ring[r * T + tid] = xm;
-        r = (r + 1 == R) ? 0 : r + 1;
-        acc = __fadd_rn(acc, v);
-        sc[m * ss] = acc;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kTriChunk; k++) cur[k] = nxt[k];
+  // term windows: T1 for m < L, T2 for nb <= m < L+nb, T3 for 2nb <= m < L+2nb
+  int cuts[6] = {0, nb, 2 * nb, L, L + nb, L + 2 * nb};
+  // sort the five inner cut points (only nb..L+nb ordering varies with 2nb vs L)
+  if (2 * nb > L) {
+    cuts[2] = L;
+    cuts[3] = 2 * nb;
+  }
+  for (int ph = 0; ph < 5; ph++) {
+    const int lo = cuts[ph], hi = cuts[ph + 1];
+    if (lo >= hi) continue;
+    const bool t1 = lo < L, t2 = lo >= nb && lo < L + nb, t3 = lo >= 2 * nb;
+    if (t1 && !t2 && !t3) acc = tri_fwd_phase<true, false, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (t1 && t2 && !t3) acc = tri_fwd_phase<true, true, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (t1 && t2 && t3) acc = tri_fwd_phase<true, true, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (!t1 && t2 && t3) acc = tri_fwd_phase<false, true, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (!t1 && t2 && !t3) acc = tri_fwd_phase<false, true, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (!t1 && !t2 && t3) acc = tri_fwd_phase<false, false, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+    else if (t1 && !t2 && t3) acc = tri_fwd_phase<true, false, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
+  }
+}
+
+// General forward pass (any nb), per element conditions.
+__device__ __forceinline__ void tri_forward_any(const float* __restrict__ x, long d, int L, int nb,
+                                                float mw, float w2, float* __restrict__ sc,
+                                                long ss) {
+  const int np = L + 2 * nb;
+  float acc = 0.f;
+  for (int m = 0; m < np; m++) {
+    float v = 0.f;
+    if (m < L) v = __fadd_rn(v, __fmul_rn(mw, x[m * d]));
+    int q = m - nb;
+    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(w2, x[q * d]));
+    q = m - 2 * nb;
+    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(mw, x[q * d]));
+    acc = __fadd_rn(acc, v);
+    sc[m * ss] = acc;
   }
 }
 
 __global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
-  extern __shared__ float ring[];
   long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= tp.nlines) return;
   const LineGeo q = line_geo(b, tp, g);
@@ -447,50 +469,45 @@ __global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
   float* sc = a.tri + s.scr0[tp.axis] + q.line;
   const long ss = q.nl, d = q.d;
   const int L = q.L, nb = tp.nb, np = L + 2 * nb;
-  tri_forward(x, d, L, nb, -tp.wt, tp.w2, sc, ss, ring, 2 * nb + 1);
   float acc = 0.f;
   if (nb <= L) {
+    tri_forward(x, d, L, nb, -tp.wt, tp.w2, sc, ss);
     // fold2 with one reflection per side: x[i] = B[i+nb], then
     // + B[2L+nb-1-i] for i >= L-nb, then + B[nb-1-i] for i < nb.  The right
-    // reflections are met first in the descending pass and kept; outputs
+    // reflections come first in the descending pass and are kept; outputs
     // i < nb wait for their left reflection.
     float right[kMaxRect];
     float left_main[kMaxRect];
-    float cur[kTriChunk], nxt[kTriChunk];
-    const int top = np - 1;
-#pragma unroll
-    for (int k = 0; k < kTriChunk; k++) cur[k] = (top - k >= 0) ? sc[(top - k) * ss] : 0.f;
-    for (int m0 = top; m0 >= 0; m0 -= kTriChunk) {
-#pragma unroll
-      for (int k = 0; k < kTriChunk; k++) {
-        const int m = m0 - kTriChunk - k;
-        nxt[k] = m >= 0 ? sc[m * ss] : 0.f;
-      }
-#pragma unroll
-      for (int k = 0; k < kTriChunk; k++) {
-        const int m = m0 - k;
-        if (m >= 0) {
-          acc = __fadd_rn(acc, cur[k]);
-          if (m >= L + nb) {
-            right[m - (L + nb)] = acc;
-          } else if (m >= nb) {
-            const int i = m - nb;
-            float v = acc;
-            if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
-            if (i < nb)
-              left_main[i] = v;
-            else
-              x[i * d] = v;
-          } else {
-            const int i = nb - 1 - m;
-            x[i * d] = __fadd_rn(left_main[i], acc);
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < kTriChunk; k++) cur[k] = nxt[k];
+    int m = np - 1;
+    for (; m >= L + nb; m--) {
+      acc = __fadd_rn(acc, sc[m * ss]);
+      right[m - (L + nb)] = acc;
+    }
+    const int mid_lo = max(2 * nb, L);  // m >= mid_lo: output i = m-nb >= max(nb, L-nb)
+#pragma unroll 4
+    for (; m >= mid_lo; m--) {  // i >= nb and i >= L-nb: main + right reflection
+      acc = __fadd_rn(acc, sc[m * ss]);
+      const int i = m - nb;
+      x[i * d] = __fadd_rn(acc, right[L - 1 - i]);
+    }
+#pragma unroll 4
+    for (; m >= nb; m--) {
+      acc = __fadd_rn(acc, sc[m * ss]);
+      const int i = m - nb;
+      float v = acc;
+      if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
+      if (i < nb)
+        left_main[i] = v;
+      else
+        x[i * d] = v;
+    }
+    for (; m >= 0; m--) {
+      acc = __fadd_rn(acc, sc[m * ss]);
+      const int i = nb - 1 - m;
+      x[i * d] = __fadd_rn(left_main[i], acc);
     }
   } else {
+    tri_forward_any(x, d, L, nb, -tp.wt, tp.w2, sc, ss);
     for (int m = np - 1; m >= 0; m--) {
       acc = __fadd_rn(acc, sc[m * ss]);
       sc[m * ss] = acc;
@@ -554,9 +571,9 @@ __global__ void k_mask32(const float* __restrict__ mdata, uint8_t* __restrict__ 
   const float* yy = mdata + s.off;
   const int n1 = s.n1, n2 = s.n2, n3 = s.n3;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
-    int ix = (int)(i % n1);
-    long r = i / n1;
-    int iy = (int)(r % n2), iz = (int)(r / n2);
+    const unsigned ii = (unsigned)i, r = ii / (unsigned)n1;
+    int ix = (int)(ii % (unsigned)n1);
+    int iy = (int)(r % (unsigned)n2), iz = (int)(r / (unsigned)n2);
     bool ma = false, mb = false;
     if (ix >= nw && ix < n1 - nw) {
       if (iy < n2 - 1)
@@ -692,22 +709,12 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
     tp[nax++] = t;
   }
   const unsigned gt = (unsigned)L.ntiles;
-  {
-    // the delayed-input ring needs up to (2*64+1)*128 floats of shared memory
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(k_tri_line, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(sizeof(float) * (2 * kMaxRect + 1) * kTriThreads));
-      attr_set = true;
-    }
-  }
   auto sweeps = [&]() {
     for (int k = 0; k < nax; k++) {
-      const int bs = kTriThreads;
-      const size_t smem = sizeof(float) * (2 * tp[k].nb + 1) * bs;
+      // few lines (one section with a short axis) spread over more SMs
+      const int bs = tp[k].nlines < 152L * 4 * kTriThreads ? 32 : kTriThreads;
       PWD_KERNEL(PWD_FAM_TRIANGLE, st,
-                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, smem, st>>>(a, b,
-                                                                                      tp[k]));
+                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, 0, st>>>(a, b, tp[k]));
     }
   };
   PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
@@ -799,6 +806,7 @@ extern "C" int pwd_dip(const float* data, const float* mask, float* dip_out, int
   int rc = check_dip_args(niter, liter, order, rect);
   if (rc != PWD_OK) return rc;
   if (!data || !dip_out || n1 < 1 || n2 < 1 || n3 < 1 || 2 * order >= n1) return PWD_EINVAL;
+  if ((long)n1 * n2 * n3 >= (1L << 31)) return PWD_EINVAL;
   std::vector<SecDesc> secs(1, SecDesc{});
   secs[0].n1 = n1;
   secs[0].n2 = n2;
@@ -823,7 +831,8 @@ int batch_table(const pwd_section* in, int nsec, int order, std::vector<SecDesc>
   secs.assign(nsec, SecDesc{});
   for (int i = 0; i < nsec; i++) {
     if (in[i].n1 < 1 || in[i].n2 < 1 || in[i].n3 < 1 || 2 * order >= in[i].n1 ||
-        in[i].offset < 0 || in[i].out_offset < 0)
+        in[i].offset < 0 || in[i].out_offset < 0 ||
+        (long)in[i].n1 * in[i].n2 * in[i].n3 >= (1L << 31))
       return PWD_EINVAL;
     secs[i].off = in[i].offset;
     secs[i].pout = in[i].out_offset;

@@ -76,16 +76,32 @@ __device__ __forceinline__ void band_add(const FilterWin<NW>& w, int i, int n1, 
   }
 }
 
+// regularization() (sof_cfuns.c:603-620) constants, computed once per
+// prediction: the reference evaluates 6.*eps, eps2+5.*eps, -4.*eps and
+// -2.*eps in double and stores them as float.
+struct RegConst {
+  float d_mid, d_end, d_next, o_mid, o_end, o1;
+};
+__device__ __forceinline__ RegConst reg_const(float eps, float eps2) {
+  RegConst r;
+  r.d_mid = __double2float_rn(6. * (double)eps);
+  r.d_end = __fadd_rn(eps2, eps);
+  r.d_next = __double2float_rn((double)eps2 + 5. * (double)eps);
+  r.o_mid = __double2float_rn(-4. * (double)eps);
+  r.o_end = __double2float_rn(-2. * (double)eps);
+  r.o1 = eps;
+  return r;
+}
+
 // regularization() values of row i.
 template <int NB>
-__device__ __forceinline__ void reg_row(int i, int n1, float eps, float eps2, float& diag,
+__device__ __forceinline__ void reg_row(int i, int n1, const RegConst& rc, float& diag,
                                         float* offd) {
-  diag = __double2float_rn(6. * (double)eps);
-  if (i == 0 || i == n1 - 1) diag = __fadd_rn(eps2, eps);
-  if (i == 1 || i == n1 - 2) diag = __double2float_rn((double)eps2 + 5. * (double)eps);
-  offd[0] = __double2float_rn(-4. * (double)eps);
-  if (i == 0 || i == n1 - 2) offd[0] = __double2float_rn(-2. * (double)eps);
-  offd[1] = eps;
+  diag = rc.d_mid;
+  if (i == 0 || i == n1 - 1) diag = rc.d_end;
+  if (i == 1 || i == n1 - 2) diag = rc.d_next;
+  offd[0] = (i == 0 || i == n1 - 2) ? rc.o_end : rc.o_mid;
+  offd[1] = rc.o1;
 #pragma unroll
   for (int b = 2; b < NB; b++) offd[b] = 0.f;
 }
@@ -129,6 +145,7 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
                             float* __restrict__ outb = nullptr, float* __restrict__ yb = nullptr) {
   static_assert(!(TWO && RHS2), "two predictions with two right-hand sides is not used");
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  const RegConst rc = reg_const(eps, eps2);
   FilterWin<NW> w1, w2;
   float x1[NA], x2[NA], xb[NA];  // input windows in[i .. i+2NW]
   float t1[NA], t2[NA], tb[NA];  // pwd_set intermediates tmp[i-NW .. i+NW]
@@ -239,7 +256,7 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
 
     // band row i: regularization + pwd_define of each filter
     float diag, offd[NB];
-    reg_row<NB>(i, n1, eps, eps2, diag, offd);
+    reg_row<NB>(i, n1, rc, diag, offd);
     band_add<NW>(w1, i, n1, diag, offd);
     if (TWO) band_add<NW>(w2, i, n1, diag, offd);
 
@@ -338,6 +355,7 @@ __device__ void predict_adj(int n1, float eps, float eps2, const ApCoef& c, floa
                             const float* __restrict__ pp, bool forw, const PredictScratch& sc,
                             float* __restrict__ xs) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  const RegConst rc = reg_const(eps, eps2);
   FilterWin<NW> w1;
   float O[NB][NB], D[NB], Y[NB];
 #pragma unroll
@@ -364,7 +382,7 @@ __device__ void predict_adj(int n1, float eps, float eps2, const ApCoef& c, floa
 #pragma unroll
       for (int j = 0; j < NA; j++) w1.a[2 * NW][j] = 0.f;
     float diag, offd[NB];
-    reg_row<NB>(i, n1, eps, eps2, diag, offd);
+    reg_row<NB>(i, n1, rc, diag, offd);
     band_add<NW>(w1, i, n1, diag, offd);
     float dk, ok[NB];
     ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);

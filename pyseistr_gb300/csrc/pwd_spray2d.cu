@@ -139,14 +139,16 @@ __global__ void k_weighted_mean(SprayBufs bf, float* __restrict__ out, SprayB b,
   const TileRange tr = tile_range(b, blockIdx.x);
   const SecDesc& s = b.secs[tr.sec];
   for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
-    const long trc = j / s.n1;
-    const int i1 = (int)(j % s.n1);
+    const unsigned jj = (unsigned)j;  // sections hold fewer than 2^31 samples
+    const long trc = jj / (unsigned)s.n1;
+    const int i1 = (int)(jj % (unsigned)s.n1);
     const long po = s.u0 + trc * b.np * (long)s.n1 + i1;
     float acc = 0.f;
     for (int is = 0; is < b.np; is++)
       acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(bf.u1[po + (long)is * s.n1], tri_weight(is, b.ns)),
                                      1.0f));
-    const float ws = (acc != 0.f) ? __double2float_rn(1.0 / (double)acc) : 0.f;
+    // 1.0/t in double rounded to float equals the float quotient
+    const float ws = (acc != 0.f) ? __fdiv_rn(1.0f, acc) : 0.f;
     if (store_w1) bf.w1[s.off + j] = ws;
     if (mean) {
       float m = 0.f;
@@ -165,8 +167,9 @@ __global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ 
   const int m = (nmf - 1) / 2, c = (b.np - 1) / 2;
   float v[kMaxWin];
   for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
-    const long trc = j / s.n1;
-    const int i1 = (int)(j % s.n1);
+    const unsigned jj = (unsigned)j;
+    const long trc = jj / (unsigned)s.n1;
+    const int i1 = (int)(jj % (unsigned)s.n1);
     const float* panel = u + s.u0 + trc * b.np * (long)s.n1 + i1;
     for (int k = 0; k < nmf; k++) v[k] = panel[(long)clampi(c + k - m, 0, b.np - 1) * s.n1];
     out[s.pout + j] = select_rank(v, nmf, m);
@@ -366,6 +369,7 @@ int spray2_dispatch(int order, const float* data, const float* dip, float* out, 
 
 int check2(int n1, int n2, int n3, int ns, int order) {
   if (n1 < 4 || n2 < 1 || n3 < 1 || ns < 0 || order < 1) return PWD_EINVAL;
+  if ((long)n1 * n2 * n3 >= (1L << 31)) return PWD_EINVAL;
   if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
   return PWD_OK;
 }
