@@ -69,6 +69,28 @@ int pwd_dip(const float *data, const float *mask, float *dip_out, int n1, int n2
             size_t workspace_bytes, pwd_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Slope estimation that allocates nothing.  No counterpart in the reference
+ * (which has no GPU code): it serves callers that cannot allocate device
+ * memory when they estimate slopes -- a plugin inside a host application
+ * that owns the CUDA context and its memory budget, or a real-time loop
+ * that must not call cudaMalloc (which can synchronise the device) after
+ * start-up.  Same arguments and results as pwd_dip, without the workspace:
+ * the scratch is a file-scope device array of pwd_dip_static_capacity()
+ * bytes (64 MiB), resident on every GPU that loads the library until the
+ * process exits.  Sections whose pwd_dip_workspace_size() exceeds it are
+ * rejected with PWD_EWORKSPACE before any work is enqueued.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress, with that device current) and caches it; make
+ *     that first call before any stream capture on the device.
+ *   - Every call uses the same array; each call initialises the parts it
+ *     reads, but calls that overlap on the GPU (different streams, or
+ *     threads without ordering) race on it and give wrong results.
+ */
+size_t pwd_dip_static_capacity(void);
+int pwd_dip_static(const float *data, const float *mask, float *dip_out, int n1, int n2, int n3,
+                   int niter, int liter, int order, const int rect[3], pwd_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Batched slope estimation over many independent sections of uneven size
  * (the patch / DAS-window workflows), in one fixed launch sequence: every
  * kernel covers all sections.  Same results as one pwd_dip call per

@@ -21,6 +21,8 @@ SIGNATURES = {
     "pwd_status_string": ([_I], ctypes.c_char_p),
     "pwd_dip_workspace_size": ([_I, _I, _I, _I, _P, _I], _S),
     "pwd_dip": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _S, _P], _I),
+    "pwd_dip_static_capacity": ([], _S),
+    "pwd_dip_static": ([_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P], _I),
     "pwd_dip_batch_workspace_size": ([_P, _I, _I, _P, _I], _S),
     "pwd_dip_batch": ([_P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _S, _P], _I),
     "pwd_sofilter2d_batch_workspace_size": ([_P, _I, _I, _I, _I, _I, _I], _S),

@@ -875,3 +875,57 @@ extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_ou
     return PWD_ECUDA;
   return dip_enqueue(data, mask, dip_out, L, w, nsec, niter, liter, order, rect, st);
 }
+
+// ---------------------------------------------------------------------------
+// Slope estimation with no allocation at all.
+//
+// Some callers cannot allocate device memory when they estimate slopes: a
+// plugin that runs inside a host application owning the CUDA context and
+// its memory budget, or a real-time DAS acquisition loop that must not call
+// cudaMalloc (it may synchronise the device) after start-up.  For them this
+// entry point keeps its scratch in a file-scope device array of fixed size,
+// resident on every GPU that loads the library until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kDipStaticScratchBytes = size_t(64) << 20;  // 64 MiB per device
+static __device__ __align__(256) unsigned char g_dip_static_scratch[kDipStaticScratchBytes];
+
+constexpr int kMaxDevices = 128;
+std::mutex g_static_mu;
+void* g_static_addr[kMaxDevices];  // device address of the array, per device
+
+// Device address of the array on the current device.  The host-side name of
+// a __device__ array is not a device address, so it is looked up once per
+// device (with that device current) and cached.
+int static_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PWD_ECUDA;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_dip_static_scratch) != cudaSuccess || !p) return PWD_ECUDA;
+    g_static_addr[dev] = p;
+  }
+  *out = g_static_addr[dev];
+  return PWD_OK;
+}
+
+}  // namespace
+
+extern "C" size_t pwd_dip_static_capacity(void) { return kDipStaticScratchBytes; }
+
+extern "C" int pwd_dip_static(const float* data, const float* mask, float* dip_out, int n1,
+                              int n2, int n3, int niter, int liter, int order, const int rect[3],
+                              pwd_stream_t stream) {
+  int rc = check_dip_args(niter, liter, order, rect);
+  if (rc != PWD_OK) return rc;
+  if (!data || !dip_out || n1 < 1 || n2 < 1 || n3 < 1 || 2 * order >= n1) return PWD_EINVAL;
+  if ((long)n1 * n2 * n3 >= (1L << 31)) return PWD_EINVAL;
+  const size_t need = pwd_dip_workspace_size(n1, n2, n3, order, rect, mask != nullptr);
+  if (need == 0 || need > kDipStaticScratchBytes) return PWD_EWORKSPACE;  // section too large
+  void* ws = nullptr;
+  if ((rc = static_scratch(&ws)) != PWD_OK) return rc;
+  return pwd_dip(data, mask, dip_out, n1, n2, n3, niter, liter, order, rect, ws,
+                 kDipStaticScratchBytes, stream);
+}
