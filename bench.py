@@ -67,7 +67,8 @@ class Batch2D(Workload):
         return int(sum(s.size for s in self.sections))
 
     def config(self):
-        return {"workload": "batch2d: 512 independent 2-D sections, n1~logU[256,2048] x "
+        return {"workload": f"batch2d: {len(self.sections)} independent 2-D sections, "
+                            "n1~logU[256,2048] x "
                             "n2~logU[64,1024]; dip2d(niter=5,liter=10,order=2,rect=10,10,1) + "
                             "somean2d(ns=6,order=2,eps=0.01)",
                 "sections": len(self.sections), "samples_per_step": self.samples()}
@@ -107,6 +108,12 @@ class Plain2D(Workload):
 
 
 WORKLOADS = {"batch2d": Batch2D, "das2d": Das2D, "plain2d": Plain2D}
+
+
+def make_workload(args, rank=0):
+    if args.workload == "batch2d":
+        return Batch2D(seed=args.seed + rank, count=args.sections)
+    return WORKLOADS[args.workload](seed=args.seed + rank)
 
 
 # --------------------------------------------------------------------------
@@ -190,10 +197,9 @@ def family_bytes(wl, launches):
             bps = 20.0
         else:
             bps = per_outer.get(fam) or 8.0
-        # launches of a family process whole sections: bytes per launch is
-        # the per-sample figure times the samples of an average section
-        sec = n / max(1, len(wl.sections))
-        out[fam] = bps * sec
+        # every launch covers every section of the batch: bytes per launch
+        # is the per-sample figure times all samples of the step
+        out[fam] = bps * n
     return out
 
 
@@ -361,7 +367,7 @@ def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
         return 0
-    wl = WORKLOADS[args.workload](seed=args.seed)
+    wl = make_workload(args)
     kind = _ref_modules() or "port"
     workers = os.cpu_count() or 1
     sample, desc = cpu_sample(wl, budget_s=6.0 * workers)
@@ -397,6 +403,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch2d")
     ap.add_argument("--seed", type=int, default=2023)
+    ap.add_argument("--sections", type=int, default=512,
+                    help="sections of the batch2d workload (smaller counts for profiler captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of single-core CPU work for the cpu_baseline sample")
@@ -416,7 +424,7 @@ def main():
     from pyseistr_gb300 import _lib
 
     _lib.load()
-    wl = WORKLOADS[args.workload](seed=args.seed + rank)
+    wl = make_workload(args, rank)
     dev = torch.device("cuda", local)
     dst = DeviceState(wl, dev)
     torch.cuda.synchronize()
@@ -479,7 +487,7 @@ def main():
                 tj = json.load(fh)
             ent = tj.get(wl.name, {}).get(dom)
             if ent:
-                traffic = ent["bytes_per_sample"] * wl.samples() / max(1, len(wl.sections))
+                traffic = ent["bytes_per_sample"] * wl.samples()
         except (OSError, ValueError, KeyError):
             traffic = None
 

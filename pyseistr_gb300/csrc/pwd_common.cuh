@@ -226,10 +226,45 @@ __device__ __forceinline__ void passfilter(const ApCoef& c, float p, float* a) {
 #pragma unroll
   for (int k = 0; k <= 2 * NW; k++) a[k] = pass_tap(c, k, p);
 }
+// aderfilter, all taps at once: the factors (nf-j-p) and ((p+j)+1) are made
+// once, each term prod_{j != i} f_j comes from prefix and suffix products
+// (float-float, about 2^-46 relative; the order of the products does not
+// matter at that accuracy), and a tap falls back to the exact FP64 replica
+// (ader_tap) only near a rounding tie.
 template <int NW>
 __device__ __forceinline__ void aderfilter(const ApCoef& c, float p, float* a) {
+  constexpr int NF = 2 * NW;
+  float fa[NF], fb[NF];
 #pragma unroll
-  for (int k = 0; k <= 2 * NW; k++) a[k] = ader_tap(c, k, p);
+  for (int j = 0; j < NF; j++) {
+    fa[j] = __fsub_rn((float)(NF - j), p);
+    fb[j] = __fadd_rn(__fadd_rn(p, (float)j), 1.0f);
+  }
+#pragma unroll
+  for (int k = 0; k <= NF; k++) {
+    float f[NF];
+#pragma unroll
+    for (int j = 0; j < NF; j++) f[j] = j < NF - k ? fa[j] : fb[j];
+    ff pre[NF], suf[NF];
+    pre[0] = {1.f, 0.f};
+#pragma unroll
+    for (int i = 1; i < NF; i++) pre[i] = ff_mul_f(pre[i - 1], f[i - 1]);
+    suf[NF - 1] = {1.f, 0.f};
+#pragma unroll
+    for (int i = NF - 2; i >= 0; i--) suf[i] = ff_mul_f(suf[i + 1], f[i + 1]);
+    ff sum = {0.f, 0.f};
+    float sabs = 0.f;
+#pragma unroll
+    for (int i = 0; i < NF; i++) {
+      ff t = ff_mul(pre[i], suf[i]);
+      // ai = -1 * prod_{j != i} f_j, and * -1 once more when i < nf-k
+      if (!(i < NF - k)) t = {-t.h, -t.l};
+      sum = ff_add(sum, t);
+      sabs = __fadd_rn(sabs, fabsf(t.h));
+    }
+    ff r = ff_mul(sum, ff{c.bh[k], c.bl[k]});
+    a[k] = ff_near_tie(r.h, r.l, sabs * fabsf(c.bh[k]) * 0x1p-38f) ? ader_tap(c, k, p) : r.h;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -23,7 +23,7 @@
 namespace pwd {
 namespace {
 
-constexpr int kTile = 2048;  // samples per elementwise tile
+constexpr int kTile = 8192;  // samples per elementwise tile
 constexpr int kTileThreads = 256;
 
 struct DipScalars {
@@ -337,13 +337,22 @@ __global__ void k_cg_update(DipArrays a, DipBatch b, int iter) {
 
 // Triangle smoothing of every line along one axis of every section, in
 // place (ps_smooth2 :616-625 = triple2 :564 + doubint2 :508 + fold2 :458).
-// One thread per line, serial running sums as the reference; the forward
-// sums go to a line-interleaved scratch and the backward pass folds the
-// reflections straight into the output when the triangle is not longer than
-// the line (the general fold2 loops otherwise).
+//
+// One warp smooths 32 lines of one section, lane = line (each section's
+// lines of every axis are numbered from a multiple of 32).  The forward pass
+// forms the spread v(m) = ((0 + -wt x[m]) + 2wt x[m-nb]) + -wt x[m-2nb]
+// (terms present where the index is inside the line) ahead of the serial
+// loop, which only runs the running sum S[m] = S[m-1] + v(m) into a
+// line-interleaved scratch (lanes hold consecutive columns: coalesced).  The
+// backward pass runs the suffix sum B[m] = B[m+1] + S[m] in the reference's
+// order and folds the reflections straight into the output when the triangle
+// is not longer than the line (the general fold2 loops otherwise).  Absent
+// terms of v are added as +0 rather than skipped: that changes at most the
+// sign of a zero v, and a running sum that starts at +0 never becomes -0, so
+// S and B keep the reference's bits.
 struct TriParams {
   int axis, nb;
-  long nlines;  // lines of this axis over the batch
+  long nlines;  // lines of this axis over the batch (padded per section to 32)
   float wt, w2;
 };
 
@@ -360,172 +369,219 @@ __device__ __forceinline__ int sec_of_line(const SecDesc* secs, int nsec, int ax
 }
 
 constexpr int kMaxRect = 64;
+constexpr int kSweepWarps = 4;
+constexpr int kFwdChunk = 16;  // strided axes: positions per prefetched chunk
 
-constexpr int kTriThreads = 128;
-
-// Line geometry of global line g of one axis.
-struct LineGeo {
-  int si, L;
-  long o, d, nl, line;
-};
-__device__ __forceinline__ LineGeo line_geo(const DipBatch& b, const TriParams& tp, long g) {
-  LineGeo q;
-  q.si = sec_of_line(b.secs, b.nsec, tp.axis, g);
-  const SecDesc& s = b.secs[q.si];
-  q.line = g - s.line0[tp.axis];
-  q.L = tp.axis == 0 ? s.n1 : (tp.axis == 1 ? s.n2 : s.n3);
-  q.nl = s.n / q.L;
-  if (tp.axis == 0) {
-    q.o = q.line * s.n1;
-    q.d = 1;
-  } else if (tp.axis == 1) {
-    q.o = (q.line % s.n1) + (q.line / s.n1) * (long)s.n1 * s.n2;
-    q.d = s.n1;
-  } else {
-    q.o = q.line;
-    q.d = (long)s.n1 * s.n2;
-  }
+// Offset of line q of one axis inside its section.
+__device__ __forceinline__ long line_base(const SecDesc& s, int axis, long q) {
+  if (axis == 0) return q * s.n1;
+  if (axis == 1) return (q % s.n1) + (q / s.n1) * (long)s.n1 * s.n2;
   return q;
 }
 
-// Forward pass of doubint2 over the spread of triple2 for m in [lo, hi):
-// v(m) = (x[m]*-wt + x[m-nb]*2wt) + x[m-2nb]*-wt with the terms T1/T2/T3
-// present (the reference adds each to a zeroed tmp, 0 + a = a for every
-// value the running sum can see); S[m] = S[m-1] + v(m).  The phases of a
-// line are branch-free; the delayed inputs are reloaded (L1 hits).
-template <bool T1, bool T2, bool T3>
-__device__ __forceinline__ float tri_fwd_phase(const float* __restrict__ x, long d, int nb,
-                                               float mw, float w2, float* __restrict__ sc,
-                                               long ss, int lo, int hi, float acc) {
-#pragma unroll 4
-  for (int m = lo; m < hi; m++) {
-    float v;
-    if (T1) v = __fmul_rn(mw, x[m * d]);
-    if (T2) {
-      const float t = __fmul_rn(w2, x[(m - nb) * d]);
-      v = T1 ? __fadd_rn(v, t) : t;
-    }
-    if (T3) {
-      const float t = __fmul_rn(mw, x[(m - 2 * nb) * d]);
-      v = (T1 || T2) ? __fadd_rn(v, t) : t;
-    }
-    acc = __fadd_rn(acc, v);
-    sc[m * ss] = acc;
-  }
-  return acc;
-}
-
-// Whole forward pass of one line (nb <= L).
-__device__ __forceinline__ void tri_forward(const float* __restrict__ x, long d, int L, int nb,
-                                            float mw, float w2, float* __restrict__ sc,
-                                            long ss) {
-  float acc = 0.f;
-  // term windows: T1 for m < L, T2 for nb <= m < L+nb, T3 for 2nb <= m < L+2nb
-  int cuts[6] = {0, nb, 2 * nb, L, L + nb, L + 2 * nb};
-  // sort the five inner cut points (only nb..L+nb ordering varies with 2nb vs L)
-  if (2 * nb > L) {
-    cuts[2] = L;
-    cuts[3] = 2 * nb;
-  }
-  for (int ph = 0; ph < 5; ph++) {
-    const int lo = cuts[ph], hi = cuts[ph + 1];
-    if (lo >= hi) continue;
-    const bool t1 = lo < L, t2 = lo >= nb && lo < L + nb, t3 = lo >= 2 * nb;
-    if (t1 && !t2 && !t3) acc = tri_fwd_phase<true, false, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (t1 && t2 && !t3) acc = tri_fwd_phase<true, true, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (t1 && t2 && t3) acc = tri_fwd_phase<true, true, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (!t1 && t2 && t3) acc = tri_fwd_phase<false, true, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (!t1 && t2 && !t3) acc = tri_fwd_phase<false, true, false>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (!t1 && !t2 && t3) acc = tri_fwd_phase<false, false, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-    else if (t1 && !t2 && t3) acc = tri_fwd_phase<true, false, true>(x, d, nb, mw, w2, sc, ss, lo, hi, acc);
-  }
-}
-
-// General forward pass (any nb), per element conditions.
-__device__ __forceinline__ void tri_forward_any(const float* __restrict__ x, long d, int L, int nb,
-                                                float mw, float w2, float* __restrict__ sc,
-                                                long ss) {
+// fold2 when the triangle is longer than the line: backward sums written
+// back to the scratch, reflections folded by the reference's loops.
+__device__ void tri_fold_general(float* __restrict__ x, long d, int L, int nb,
+                                 float* __restrict__ sc, long ss) {
   const int np = L + 2 * nb;
   float acc = 0.f;
-  for (int m = 0; m < np; m++) {
-    float v = 0.f;
-    if (m < L) v = __fadd_rn(v, __fmul_rn(mw, x[m * d]));
-    int q = m - nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(w2, x[q * d]));
-    q = m - 2 * nb;
-    if (q >= 0 && q < L) v = __fadd_rn(v, __fmul_rn(mw, x[q * d]));
-    acc = __fadd_rn(acc, v);
+  for (int m = np - 1; m >= 0; m--) {
+    acc = __fadd_rn(acc, sc[m * ss]);
     sc[m * ss] = acc;
+  }
+  int i, j;
+  for (i = 0; i < L; i++) x[i * d] = sc[(i + nb) * ss];
+  for (j = nb + L; j < np; j += L) {
+    for (i = 0; i < L && i < np - j; i++)
+      x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j + i) * ss]);
+    j += L;
+    for (i = 0; i < L && i < np - j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j + i) * ss]);
+  }
+  for (j = nb; j >= 0; j -= L) {
+    for (i = 0; i < L && i < j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j - 1 - i) * ss]);
+    j -= L;
+    for (i = 0; i < L && i < j; i++)
+      x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j - 1 - i) * ss]);
   }
 }
 
-__global__ void k_tri_line(DipArrays a, DipBatch b, TriParams tp) {
-  long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (g >= tp.nlines) return;
-  const LineGeo q = line_geo(b, tp, g);
-  if (b.S[q.si].cg_done) return;
-  const SecDesc& s = b.secs[q.si];
-  float* x = a.tmp + s.off + q.o;
-  float* sc = a.tri + s.scr0[tp.axis] + q.line;
-  const long ss = q.nl, d = q.d;
-  const int L = q.L, nb = tp.nb, np = L + 2 * nb;
+// Shared memory of one warp: the [32][33] transposition tile (axis 0 only)
+// and the right-reflection / left-output stashes [nb][32] each.
+__host__ __device__ constexpr int sweep_warp_floats(int axis, int nb) {
+  return (axis == 0 ? 32 * 33 : 0) + 2 * nb * 32;
+}
+
+template <int AXIS>
+__global__ void __launch_bounds__(32 * kSweepWarps) k_tri_sweep(DipArrays a, DipBatch b,
+                                                                TriParams tp) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long g0 = (blockIdx.x * (long)kSweepWarps + w) * 32;
+  if (g0 >= tp.nlines) return;
+  const int si = sec_of_line(b.secs, b.nsec, AXIS, g0);
+  if (b.S[si].cg_done) return;
+  const SecDesc& s = b.secs[si];
+  const int nb = tp.nb;
+  const int L = AXIS == 0 ? s.n1 : (AXIS == 1 ? s.n2 : s.n3);
+  const long nl = s.n / L;
+  const long lb = g0 - s.line0[AXIS];
+  if (lb >= nl) return;  // padding lines of the section
+  const int nvalid = (int)min(32L, nl - lb);
+  const bool mine = lane < nvalid;
+  const long q = lb + (mine ? lane : 0);
+  const int d = AXIS == 0 ? 1 : (AXIS == 1 ? s.n1 : s.n1 * s.n2);
+  float* __restrict__ xl = a.tmp + s.off + line_base(s, AXIS, q);
+  float* __restrict__ sc = a.tri + s.scr0[AXIS] + q;
+  const long ss = nl;
+  const int np = L + 2 * nb;
+  const float mw = -tp.wt, w2 = tp.w2;
+  float* tile = smem + w * sweep_warp_floats(AXIS, nb);
+  float* er = tile + (AXIS == 0 ? 32 * 33 : 0);  // er[j][lane] = B[L+nb+j]
+  float* el = er + nb * 32;                       // el[i][lane], outputs i < nb
+
+  // ---- forward pass ----
   float acc = 0.f;
-  if (nb <= L) {
-    tri_forward(x, d, L, nb, -tp.wt, tp.w2, sc, ss);
-    // fold2 with one reflection per side: x[i] = B[i+nb], then
-    // + B[2L+nb-1-i] for i >= L-nb, then + B[nb-1-i] for i < nb.  The right
-    // reflections come first in the descending pass and are kept; outputs
-    // i < nb wait for their left reflection.
-    float right[kMaxRect];
-    float left_main[kMaxRect];
-    int m = np - 1;
-    for (; m >= L + nb; m--) {
-      acc = __fadd_rn(acc, sc[m * ss]);
-      right[m - (L + nb)] = acc;
-    }
-    const int mid_lo = max(2 * nb, L);  // m >= mid_lo: output i = m-nb >= max(nb, L-nb)
-#pragma unroll 4
-    for (; m >= mid_lo; m--) {  // i >= nb and i >= L-nb: main + right reflection
-      acc = __fadd_rn(acc, sc[m * ss]);
-      const int i = m - nb;
-      x[i * d] = __fadd_rn(acc, right[L - 1 - i]);
-    }
-#pragma unroll 4
-    for (; m >= nb; m--) {
-      acc = __fadd_rn(acc, sc[m * ss]);
-      const int i = m - nb;
-      float v = acc;
-      if (i >= L - nb) v = __fadd_rn(v, right[L - 1 - i]);
-      if (i < nb)
-        left_main[i] = v;
-      else
-        x[i * d] = v;
-    }
-    for (; m >= 0; m--) {
-      acc = __fadd_rn(acc, sc[m * ss]);
-      const int i = nb - 1 - m;
-      x[i * d] = __fadd_rn(left_main[i], acc);
+  if (AXIS == 0) {
+    // lane j forms v at position m0+j of each of the warp's traces (coalesced
+    // loads), the tile is transposed, then lane t sums its trace serially
+    const float* xs = a.tmp + s.off + lb * L;
+    for (int m0 = 0; m0 < np; m0 += 32) {
+      const int p = m0 + lane;
+      const bool c1 = p < L, c2 = p >= nb && p < L + nb, c3 = p >= 2 * nb && p < np;
+      const float* xp = xs + p;
+#pragma unroll 8
+      for (int t = 0; t < 32; t++) {
+        if (t < nvalid) {
+          const float* xt = xp + t * L;
+          const float t1 = c1 ? __fmul_rn(mw, xt[0]) : 0.f;
+          const float t2 = c2 ? __fmul_rn(w2, xt[-nb]) : 0.f;
+          const float t3 = c3 ? __fmul_rn(mw, xt[-2 * nb]) : 0.f;
+          tile[t * 33 + lane] = __fadd_rn(__fadd_rn(t1, t2), t3);
+        }
+      }
+      __syncwarp();
+      const int kmax = min(32, np - m0);
+      float* sp = sc + m0 * ss;
+#pragma unroll 8
+      for (int k = 0; k < kmax; k++) {
+        acc = __fadd_rn(acc, tile[lane * 33 + k]);
+        if (mine) *sp = acc;
+        sp += ss;
+      }
+      __syncwarp();
     }
   } else {
-    tri_forward_any(x, d, L, nb, -tp.wt, tp.w2, sc, ss);
-    for (int m = np - 1; m >= 0; m--) {
-      acc = __fadd_rn(acc, sc[m * ss]);
-      sc[m * ss] = acc;
+    // lanes hold consecutive lines: the loads of x[p], x[p-nb], x[p-2nb] are
+    // coalesced; the next chunk's loads are in flight during this chunk's sums
+    constexpr int C = kFwdChunk;
+    float r1[C], r2[C], r3[C];
+#pragma unroll
+    for (int k = 0; k < C; k++) {
+      const int p = k;
+      r1[k] = p < L ? xl[p * d] : 0.f;
+      r2[k] = (p >= nb && p < L + nb) ? xl[(p - nb) * d] : 0.f;
+      r3[k] = (p >= 2 * nb && p < np) ? xl[(p - 2 * nb) * d] : 0.f;
     }
-    int i, j;
-    for (i = 0; i < L; i++) x[i * d] = sc[(i + nb) * ss];
-    for (j = nb + L; j < np; j += L) {
-      for (i = 0; i < L && i < np - j; i++)
-        x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j + i) * ss]);
-      j += L;
-      for (i = 0; i < L && i < np - j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j + i) * ss]);
+    for (int m0 = 0; m0 < np; m0 += C) {
+      float v[C];
+#pragma unroll
+      for (int k = 0; k < C; k++)
+        v[k] = __fadd_rn(__fadd_rn(__fmul_rn(mw, r1[k]), __fmul_rn(w2, r2[k])),
+                         __fmul_rn(mw, r3[k]));
+#pragma unroll
+      for (int k = 0; k < C; k++) {
+        const int p = m0 + C + k;
+        r1[k] = p < L ? xl[p * d] : 0.f;
+        r2[k] = (p >= nb && p < L + nb) ? xl[(p - nb) * d] : 0.f;
+        r3[k] = (p >= 2 * nb && p < np) ? xl[(p - 2 * nb) * d] : 0.f;
+      }
+      float* sp = sc + m0 * ss;
+#pragma unroll
+      for (int k = 0; k < C; k++) {
+        if (m0 + k < np) {
+          acc = __fadd_rn(acc, v[k]);
+          if (mine) *sp = acc;
+          sp += ss;
+        }
+      }
     }
-    for (j = nb; j >= 0; j -= L) {
-      for (i = 0; i < L && i < j; i++) x[i * d] = __fadd_rn(x[i * d], sc[(j - 1 - i) * ss]);
-      j -= L;
-      for (i = 0; i < L && i < j; i++)
-        x[(L - 1 - i) * d] = __fadd_rn(x[(L - 1 - i) * d], sc[(j - 1 - i) * ss]);
+  }
+
+  if (nb > L) {  // triangle longer than the line: the general fold, per lane
+    if (mine) tri_fold_general(xl, d, L, nb, sc, ss);
+    return;
+  }
+
+  // ---- backward pass: B[m] for m = np-1 .. 0, chunked by output index
+  // i = m - nb in aligned groups of 32 (i from -nb to L+nb-1) ----
+  float* xs0 = a.tmp + s.off + lb * L;  // axis 0: trace t at xs0 + t*L
+  auto put = [&](int i, float v) {            // output i < nb: written directly
+    if (mine) xl[i * d] = v;
+  };
+  auto flush = [&](int c) {                   // axis 0: tile chunk c to x
+    __syncwarp();
+    const int i = c * 32 + lane;
+    if (i >= nb && i < L) {
+#pragma unroll 8
+      for (int t = 0; t < 32; t++)
+        if (t < nvalid) xs0[t * L + i] = tile[t * 33 + lane];
     }
+    __syncwarp();
+  };
+  const int ctop = (L + nb - 1) >> 5;
+  const int cbot = -((nb + 31) >> 5);
+  float cur[32], nxt[32];
+  auto load = [&](int c, float* buf) {
+    const int mtop = c * 32 + 31 + nb;
+    const float* sp = sc + (long)mtop * ss;
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      const int m = mtop - k;
+      buf[k] = (m >= 0 && m < np) ? *sp : 0.f;
+      sp -= ss;
+    }
+  };
+  load(ctop, cur);
+  acc = 0.f;
+  for (int c = ctop; c >= cbot; c--) {
+    if (c > cbot) load(c - 1, nxt);
+    const int ibase = c * 32;
+    if (ibase >= nb && ibase + 31 < L - nb) {
+      // interior chunk: outputs are the backward sums themselves
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        acc = __fadd_rn(acc, cur[k]);
+        if (AXIS == 0)
+          tile[lane * 33 + 31 - k] = acc;
+        else if (mine)
+          xl[(ibase + 31 - k) * d] = acc;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        const int i = ibase + 31 - k, m = i + nb;
+        if (m < 0 || m >= np) continue;
+        acc = __fadd_rn(acc, cur[k]);
+        if (i >= L) {
+          er[(i - L) * 32 + lane] = acc;
+        } else if (i >= 0) {
+          float v = acc;
+          if (i >= L - nb) v = __fadd_rn(v, er[(L - 1 - i) * 32 + lane]);
+          if (i < nb)
+            el[i * 32 + lane] = v;
+          else if (AXIS == 0)
+            tile[lane * 33 + 31 - k] = v;
+          else if (mine)
+            xl[i * d] = v;
+        } else {
+          const int ii = -1 - i;
+          put(ii, __fadd_rn(el[ii * 32 + lane], acc));
+        }
+      }
+    }
+    if (AXIS == 0 && c >= 0) flush(c);
+#pragma unroll
+    for (int k = 0; k < 32; k++) cur[k] = nxt[k];
   }
 }
 
@@ -646,7 +702,8 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
       s.scr0[a] = scr[a];
       if (rect[a] > 1) {
         long nl = s.n / len[a];
-        lines[a] += nl;
+        // lines are swept 32 per warp: each section starts a new warp
+        lines[a] += (nl + 31) / 32 * 32;
         scr[a] += nl * (len[a] + 2L * rect[a]);
       }
     }
@@ -709,12 +766,21 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
     tp[nax++] = t;
   }
   const unsigned gt = (unsigned)L.ntiles;
+  // shared-memory limits of the sweep kernels (the axis-0 form with the
+  // largest triangle needs more than the default 48 KB)
+  for (int ax = 0; ax < 3; ax++) {
+    const int bytes = (int)(sizeof(float) * kSweepWarps * sweep_warp_floats(ax, kMaxRect));
+    cudaFuncSetAttribute(ax == 0 ? k_tri_sweep<0> : (ax == 1 ? k_tri_sweep<1> : k_tri_sweep<2>),
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
   auto sweeps = [&]() {
     for (int k = 0; k < nax; k++) {
-      // few lines (one section with a short axis) spread over more SMs
-      const int bs = tp[k].nlines < 152L * 4 * kTriThreads ? 32 : kTriThreads;
+      const int ax = tp[k].axis;
+      const size_t smem = sizeof(float) * kSweepWarps * sweep_warp_floats(ax, tp[k].nb);
+      const unsigned grid = (unsigned)((tp[k].nlines / 32 + kSweepWarps - 1) / kSweepWarps);
+      auto* kern = ax == 0 ? k_tri_sweep<0> : (ax == 1 ? k_tri_sweep<1> : k_tri_sweep<2>);
       PWD_KERNEL(PWD_FAM_TRIANGLE, st,
-                 k_tri_line<<<(unsigned)((tp[k].nlines + bs - 1) / bs), bs, 0, st>>>(a, b, tp[k]));
+                 kern<<<grid, 32 * kSweepWarps, smem, st>>>(a, b, tp[k]));
     }
   };
   PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
