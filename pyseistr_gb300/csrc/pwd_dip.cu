@@ -405,10 +405,16 @@ __device__ void tri_fold_general(float* __restrict__ x, long d, int L, int nb,
   }
 }
 
-// Shared memory of one warp: the [32][33] transposition tile (axis 0 only)
-// and the right-reflection / left-output stashes [nb][32] each.
+// Positions kept by the axis-0 window: a power of two >= 32 + 2 nb.
+__host__ __device__ constexpr int sweep_window(int nb) {
+  return 32 + 2 * nb <= 64 ? 64 : (32 + 2 * nb <= 128 ? 128 : 256);
+}
+
+// Shared memory of one warp: on axis 0 the window [32][P+1] (reused as the
+// [32][33] output transposition tile of the backward pass), then the
+// right-reflection / left-output stashes [nb][32] each.
 __host__ __device__ constexpr int sweep_warp_floats(int axis, int nb) {
-  return (axis == 0 ? 32 * 33 : 0) + 2 * nb * 32;
+  return (axis == 0 ? 32 * (sweep_window(nb) + 1) : 0) + 2 * nb * 32;
 }
 
 template <int AXIS>
@@ -436,40 +442,58 @@ __global__ void __launch_bounds__(32 * kSweepWarps) k_tri_sweep(DipArrays a, Dip
   const int np = L + 2 * nb;
   const float mw = -tp.wt, w2 = tp.w2;
   float* tile = smem + w * sweep_warp_floats(AXIS, nb);
-  float* er = tile + (AXIS == 0 ? 32 * 33 : 0);  // er[j][lane] = B[L+nb+j]
+  float* er = tile + (AXIS == 0 ? 32 * (sweep_window(nb) + 1) : 0);  // er[j][lane] = B[L+nb+j]
   float* el = er + nb * 32;                       // el[i][lane], outputs i < nb
 
   // ---- forward pass ----
   float acc = 0.f;
   if (AXIS == 0) {
-    // lane j forms v at position m0+j of each of the warp's traces (coalesced
-    // loads), the tile is transposed, then lane t sums its trace serially
+    // the warp's 32 traces pass through a shared-memory window of the last
+    // P positions, W[t][pos mod P]: lane j loads position m0+j of every
+    // trace (coalesced, unconditional: clamped addresses), and lane t then
+    // reads x[m], x[m-nb], x[m-2nb] of its own trace from the window.  The
+    // next chunk's loads are in flight during this chunk's sums.
+    const int P = sweep_window(nb), P1 = P + 1;
     const float* xs = a.tmp + s.off + lb * L;
+    const float* xp = xs + min(lane, L - 1);
+    const int tmax = nvalid - 1;
+    float xr[32];
+#pragma unroll
+    for (int t = 0; t < 32; t++) xr[t] = xp[min(t, tmax) * L];
+#pragma unroll
+    for (int t = 0; t < 32; t++) tile[t * P1 + lane] = xr[t];
+    const float* Wl = tile + lane * P1;
     for (int m0 = 0; m0 < np; m0 += 32) {
-      const int p = m0 + lane;
-      const bool c1 = p < L, c2 = p >= nb && p < L + nb, c3 = p >= 2 * nb && p < np;
-      const float* xp = xs + p;
-#pragma unroll 8
-      for (int t = 0; t < 32; t++) {
-        if (t < nvalid) {
-          const float* xt = xp + t * L;
-          const float t1 = c1 ? __fmul_rn(mw, xt[0]) : 0.f;
-          const float t2 = c2 ? __fmul_rn(w2, xt[-nb]) : 0.f;
-          const float t3 = c3 ? __fmul_rn(mw, xt[-2 * nb]) : 0.f;
-          tile[t * 33 + lane] = __fadd_rn(__fadd_rn(t1, t2), t3);
-        }
+      const bool more = m0 + 32 < L;
+      if (more) {
+        const float* xq = xs + min(m0 + 32 + lane, L - 1);
+#pragma unroll
+        for (int t = 0; t < 32; t++) xr[t] = xq[min(t, tmax) * L];
       }
       __syncwarp();
       const int kmax = min(32, np - m0);
       float* sp = sc + m0 * ss;
 #pragma unroll 8
       for (int k = 0; k < kmax; k++) {
-        acc = __fadd_rn(acc, tile[lane * 33 + k]);
+        const int m = m0 + k;
+        const float x1 = Wl[m & (P - 1)];
+        const float x2 = Wl[(m - nb) & (P - 1)];
+        const float x3 = Wl[(m - 2 * nb) & (P - 1)];
+        const float t1 = m < L ? __fmul_rn(mw, x1) : 0.f;
+        const float t2 = (m >= nb && m < L + nb) ? __fmul_rn(w2, x2) : 0.f;
+        const float t3 = m >= 2 * nb ? __fmul_rn(mw, x3) : 0.f;
+        acc = __fadd_rn(acc, __fadd_rn(__fadd_rn(t1, t2), t3));
         if (mine) *sp = acc;
         sp += ss;
       }
       __syncwarp();
+      if (more) {
+        const int col = (m0 + 32 + lane) & (P - 1);
+#pragma unroll
+        for (int t = 0; t < 32; t++) tile[t * P1 + col] = xr[t];
+      }
     }
+    __syncwarp();
   } else {
     // lanes hold consecutive lines: the loads of x[p], x[p-nb], x[p-2nb] are
     // coalesced; the next chunk's loads are in flight during this chunk's sums
