@@ -135,11 +135,12 @@ class DeviceState:
         self.D = D
 
 
-def gpu_step(wl, st):
+def gpu_step(wl, st, mixed=False):
     D = st.D
     d = wl.dip
     f = wl.filt
-    D.dip_batch(st.d, st.shapes, d["niter"], d["liter"], d["order"], d["rect"], out=st.p)
+    D.dip_batch(st.d, st.shapes, d["niter"], d["liter"], d["order"], d["rect"], out=st.p,
+                mixed=mixed)
     if wl.name == "das2d":
         D.sofilter2d_batch(st.d, st.p, st.shapes, f["ns"], f["order"], f["eps"],
                            filter=D.FILTER_MEDIAN, out=st.f)
@@ -151,7 +152,7 @@ def gpu_step(wl, st):
                                filter=D.FILTER_MEDIAN, out=st.g)
 
 
-def api_step(wl):
+def api_step(wl, mixed=False):
     """The public batched API on host arrays: upload, slopes, filter,
     download.  Returns (h2d_bytes, d2h_bytes)."""
     import pyseistr_gb300 as ps
@@ -161,7 +162,7 @@ def api_step(wl):
     nbytes = sum(s.nbytes for s in wl.sections)
     p, out = ps.dip_somean2d_batch(wl.sections, niter=d["niter"], liter=d["liter"],
                                    order=d["order"], rect=list(d["rect"]), ns=f["ns"],
-                                   eps=f["eps"], median=(wl.name == "das2d"))
+                                   eps=f["eps"], median=(wl.name == "das2d"), mixed=mixed)
     h2d, d2h = nbytes, 2 * nbytes
     if wl.name == "plain2d":
         ps.somf2dc_batch(wl.sections, p, f["ns"], f["order"], f["eps"])
@@ -170,35 +171,42 @@ def api_step(wl):
     return h2d, d2h
 
 
-# Algorithmic bytes per sample of the kernels of each family (what one
-# launch must read and write at minimum, per sample of the section it
-# processes): see the design doc.
-def family_bytes(wl, launches):
+# Algorithmic bytes per sample of each kernel family, averaged over the
+# family's launches of one step (what the launches must read and write at
+# minimum; every launch covers every section of the batch).
+def family_bytes(wl, launches, mixed=False):
     """Average algorithmic bytes per launch of each family for one step."""
     n = wl.samples()
     d = wl.dip
-    naxes = sum(1 for r in d["rect"] if r > 1)
-    per_outer = {
-        # residual (12 B) once, prep (24 B) per iteration, trials (20 B)
-        "pwd": None,
-        # scale 28 + per CG iteration grad 16 + gp 16 + update 36 + step 36
-        "cg": (28 + d["liter"] * (16 + 16 + 36 + 36)) / (1 + 4 * d["liter"]),
-        # each line sweep reads and writes its axis once: 8 B
-        "triangle": 8.0,
-        # spray: read the data trace and slopes, write the panels it fills
-        "spray": 8.0,
-        "filter": 8.0,
-    }
+    liter, niter = d["liter"], d["niter"]
     out = {}
     for fam, cnt in launches.items():
         if cnt == 0:
             continue
         if fam == "pwd":
-            bps = 20.0
+            # residual: read u, p, write r (12 B); derivative + normalisation:
+            # read u, p, r, write num, den, p0 (24 B); line-search trials:
+            # read u, p0, dp, write p (16 B)
+            trials = max(0, cnt - 1 - niter)
+            bps = (12.0 + 24.0 * niter + 16.0 * trials) / max(1, 1 + niter + trials)
+        elif fam == "cg" and mixed:
+            # per Gauss-Newton iteration: scale 28; fused pass 1 (step,
+            # gradient, smoothing, gp) 28 then 44; fused pass 2 (smoothing,
+            # conjugate update) 20 then 32; final step 36
+            per_outer = 28 + 28 + 44 * (liter - 1) + 20 + 32 * (liter - 1) + 36
+            bps = per_outer / (2.0 + 2.0 * liter)
+        elif fam == "cg":
+            # per Gauss-Newton iteration: scale 28, first gradient 16, later
+            # step+gradient 44, gp 16, first update 24, later updates 36,
+            # final step 36 (bytes per sample)
+            per_outer = 28 + 16 + 44 * (liter - 1) + 16 * liter + 24 + 36 * (liter - 1) + 36
+            bps = per_outer / (2.0 + 3.0 * liter)
+        elif fam == "triangle":
+            bps = 8.0  # each line sweep reads and writes its axis once
+        elif fam == "spray":
+            bps = 8.0  # read the data and the slopes
         else:
-            bps = per_outer.get(fam) or 8.0
-        # every launch covers every section of the batch: bytes per launch
-        # is the per-sample figure times all samples of the step
+            bps = 12.0
         out[fam] = bps * n
     return out
 
@@ -405,6 +413,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
                     help="sections of the batch2d workload (smaller counts for profiler captures)")
+    ap.add_argument("--precision", choices=["plain", "mixed"], default="plain",
+                    help="slope estimation arithmetic: plain (bit-faithful FP32) or mixed "
+                         "(FP32 taps, fused convolution smoothing, FP64 reductions)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of single-core CPU work for the cpu_baseline sample")
@@ -433,8 +444,9 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    mixed = args.precision == "mixed"
     for _ in range(max(3, args.warmup)):
-        gpu_step(wl, dst)
+        gpu_step(wl, dst, mixed)
     torch.cuda.synchronize()
 
     # ---- timed region (device) ----
@@ -447,7 +459,7 @@ def main():
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
-            gpu_step(wl, dst)
+            gpu_step(wl, dst, mixed)
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.launch_count() - l0
@@ -465,12 +477,12 @@ def main():
     torch.cuda.synchronize()
     with _lib.profile() as prof:
         for _ in range(args.steps):
-            gpu_step(wl, dst)
+            gpu_step(wl, dst, mixed)
         torch.cuda.synchronize()
     fam_ms = {f: v / args.steps for f, v in prof.ms.items()}
     fam_n = {f: v // args.steps for f, v in prof.launches.items()}
     dom = max(fam_ms, key=lambda f: fam_ms[f])
-    bpl = family_bytes(wl, fam_n)
+    bpl = family_bytes(wl, fam_n, mixed)
     peak, peak_src = HBM_FALLBACK_GBS, "fallback"
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -497,7 +509,7 @@ def main():
     t0 = time.perf_counter()
     h2d = d2h = 0
     for _ in range(args.steps):
-        h2d, d2h = api_step(wl)
+        h2d, d2h = api_step(wl, mixed)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     if world > 1:
@@ -506,12 +518,37 @@ def main():
         e2e_s = float(t.item())
     e2e = world * wl.samples() / e2e_s
 
+    plain = None
+    if mixed:
+        # the plain FP32 path on the same inputs: the mixed/plain ratio and
+        # the distance between the two slope fields
+        p_mixed = dst.p.clone()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            gpu_step(wl, dst, False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = ev0.elapsed_time(ev1) / args.steps
+        errs, k = [], 0
+        for shp in dst.shapes:
+            n = int(np.prod(shp))
+            a, b = p_mixed[k:k + n].double(), dst.p[k:k + n].double()
+            errs.append(float(torch.linalg.norm(a - b) / max(float(torch.linalg.norm(b)), 1e-30)))
+            k += n
+        plain = {"value": world * wl.samples() / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                 "speedup_mixed_vs_plain": plain_ms / ms_step,
+                 "slopes_rel_l2_mixed_vs_plain_max_section": max(errs)}
+
     line = {
         "metric": "output samples/sec (dip+SO filter)", "value": value, "unit": "samples/s",
         "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
-        "config": dict(wl.config(), precision="plain FP32 (bit-faithful to the reference)",
+        "config": dict(wl.config(),
+                       precision=("mixed: FP32 taps, convolution smoothing fused with the CG, "
+                                  "FP64 reductions; filters plain FP32") if mixed
+                       else "plain FP32 (bit-faithful to the reference)",
                        l2="inputs larger than L2 (129 MB)" if 4 * wl.samples() > 129e6
                        else "inputs fit in L2; no flush between steps",
                        parallelism=f"replicas x{world}"),
@@ -524,6 +561,8 @@ def main():
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "family_ms_per_step": fam_ms, "family_launches_per_step": fam_n},
     }
+    if plain is not None:
+        line["plain_fp32"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         kind = _ref_modules() or "port"
         sample, desc = cpu_sample(wl, args.cpu_budget)

@@ -111,6 +111,22 @@ int pwd_dip_batch(const float *data, const float *mask, float *dip_out,
                   const int rect[3], void *workspace, size_t workspace_bytes,
                   pwd_stream_t stream);
 
+/* Mixed mode of pwd_dip_batch (same arguments).  Not bit-faithful: the
+ * filter taps are evaluated in FP32, the triangle smoothing of the shaping
+ * CG is applied as the equivalent direct convolution (triangle weights
+ * (nb-|k|)/nb^2 on the half-sample-mirrored line) fused with the CG vector
+ * updates, and the dot products stay in FP64 as in the plain path.  The
+ * slopes agree with an FP64 evaluation of the reference algorithm to about
+ * the accuracy of the plain FP32 path.  No reference counterpart: it is an
+ * alternative arithmetic for the same dipc computation.
+ */
+size_t pwd_dip_batch_mixed_workspace_size(const pwd_section *sections, int nsec, int order,
+                                          const int rect[3], int has_mask);
+int pwd_dip_batch_mixed(const float *data, const float *mask, float *dip_out,
+                        const pwd_section *sections, int nsec, int niter, int liter, int order,
+                        const int rect[3], void *workspace, size_t workspace_bytes,
+                        pwd_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * 2-D structure-oriented mean, slice by slice over n3.
  * Replaces csomean2d, pyseistr/src/sof_cfuns.c:1433-1531 (somean2dc,

@@ -218,11 +218,12 @@ def _unpack(t, shapes):
     return out
 
 
-def dip2dc_batch(sections, niter=5, liter=20, order=2, rect=[10, 10, 1]):
+def dip2dc_batch(sections, niter=5, liter=20, order=2, rect=[10, 10, 1], mixed=False):
     """dip2dc over a list of 2-D sections, all in one launch sequence;
-    returns the list of slopes (each equal to dip2dc of its section)."""
+    returns the list of slopes (each equal to dip2dc of its section, or its
+    mixed-mode approximation with mixed=True)."""
     shapes = [tuple(s.shape) for s in sections]
-    out = D.dip_batch(_pack(sections), shapes, niter, liter, order, rect)
+    out = D.dip_batch(_pack(sections), shapes, niter, liter, order, rect, mixed=mixed)
     return _unpack(out, shapes)
 
 
@@ -243,13 +244,14 @@ def somf2dc_batch(sections, dips, ns, order, eps, option=1):
 
 
 def dip_somean2d_batch(sections, niter=5, liter=10, order=2, rect=[10, 10, 1], ns=6, eps=0.01,
-                       median=False):
+                       median=False, mixed=False):
     """Slope estimation followed by the structure-oriented mean (or median)
     of many sections: one upload, both stages on the device, one download.
-    Returns (slopes, filtered) lists."""
+    Returns (slopes, filtered) lists.  mixed=True estimates the slopes in
+    the mixed mode."""
     shapes = [tuple(s.shape) for s in sections]
     d = _pack(sections)
-    p = D.dip_batch(d, shapes, niter, liter, order, rect)
+    p = D.dip_batch(d, shapes, niter, liter, order, rect, mixed=mixed)
     if median:
         f = D.sofilter2d_batch(d, p, shapes, ns, order, eps, filter=D.FILTER_MEDIAN)
     else:

@@ -12,7 +12,9 @@ struct SecDesc {
   int n1, n2, n3;
   int tile0;      // first elementwise tile of the section
   int ntile;      // tiles of the section
-  int pad;
+  int ftile0;     // first 2-D smoothing tile (mixed-mode slope estimation)
+  int nftile;     // 2-D smoothing tiles of the section
+  int pad[2];
   long line0[3];  // first global triangle line of each smoothed axis
   long scr0[3];   // triangle scratch offset of each smoothed axis
   long tr0;       // spray: first global trace (n2*n3 traces per section)

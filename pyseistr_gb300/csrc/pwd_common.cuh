@@ -268,6 +268,56 @@ __device__ __forceinline__ void aderfilter(const ApCoef& c, float p, float* a) {
 }
 
 // ---------------------------------------------------------------------------
+// Mixed-mode filter taps: the same products evaluated directly in FP32
+// (relative error a few units of 2^-24 instead of the reference's rounding
+// of a double product).  b[k] enters as its float-float pair.
+// ---------------------------------------------------------------------------
+template <int NW>
+__device__ __forceinline__ void passfilter_f32(const ApCoef& c, float p, float* a) {
+  constexpr int NF = 2 * NW;
+#pragma unroll
+  for (int k = 0; k <= NF; k++) {
+    float t = 1.f;
+#pragma unroll
+    for (int j = 0; j < NF; j++)
+      t = __fmul_rn(t, j < NF - k ? __fsub_rn((float)(NF - j), p) : __fadd_rn(p, (float)(j + 1)));
+    a[k] = __fmaf_rn(c.bl[k], t, __fmul_rn(c.bh[k], t));
+  }
+}
+
+template <int NW>
+__device__ __forceinline__ void aderfilter_f32(const ApCoef& c, float p, float* a) {
+  constexpr int NF = 2 * NW;
+  float fa[NF], fb[NF];
+#pragma unroll
+  for (int j = 0; j < NF; j++) {
+    fa[j] = __fsub_rn((float)(NF - j), p);
+    fb[j] = __fadd_rn(p, (float)(j + 1));
+  }
+#pragma unroll
+  for (int k = 0; k <= NF; k++) {
+    float f[NF], pre[NF], suf[NF];
+#pragma unroll
+    for (int j = 0; j < NF; j++) f[j] = j < NF - k ? fa[j] : fb[j];
+    pre[0] = 1.f;
+#pragma unroll
+    for (int i = 1; i < NF; i++) pre[i] = __fmul_rn(pre[i - 1], f[i - 1]);
+    suf[NF - 1] = 1.f;
+#pragma unroll
+    for (int i = NF - 2; i >= 0; i--) suf[i] = __fmul_rn(suf[i + 1], f[i + 1]);
+    // sum_i s_i prod_{j != i} f_j with s_i = +1 where the factor falls with
+    // p (i < nf-k) and -1 where it rises, as the reference's sign rule
+    float sum = 0.f;
+#pragma unroll
+    for (int i = 0; i < NF; i++) {
+      const float t = __fmul_rn(pre[i], suf[i]);
+      sum = i < NF - k ? __fadd_rn(sum, t) : __fsub_rn(sum, t);
+    }
+    a[k] = __fmaf_rn(c.bl[k], sum, __fmul_rn(c.bh[k], sum));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Deterministic reductions: per-block partials, summed in a fixed order by
 // the last block to finish (no floating-point atomics).
 // ---------------------------------------------------------------------------

@@ -46,6 +46,7 @@ struct DipArrays {
   float* p;        // slopes (output)
   const uint8_t* mask;
   float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
+  float *x2, *r2;  // mixed mode: second buffers of x (dp) and r
 };
 
 struct TileRange {
@@ -109,14 +110,20 @@ __device__ __forceinline__ bool pwd_valid(const SecDesc& s, long i, int nw, int 
 }
 
 // allpass1/allpass2 at one sample (dip_cfuns.c:1135-1200, :1399-1465).
-template <int NW, bool DER>
+template <int NW, bool DER, bool FAST = false>
 __device__ __forceinline__ float pwd_at(const float* __restrict__ u, long i, long ip,
                                         const ApCoef& c, float p) {
   float f[2 * NW + 1];
-  if (DER)
+  if (FAST) {
+    if (DER)
+      aderfilter_f32<NW>(c, p, f);
+    else
+      passfilter_f32<NW>(c, p, f);
+  } else if (DER) {
     aderfilter<NW>(c, p, f);
-  else
+  } else {
     passfilter<NW>(c, p, f);
+  }
   float y = 0.f;
 #pragma unroll
   for (int iw = 0; iw <= 2 * NW; iw++) {
@@ -133,7 +140,7 @@ __device__ __forceinline__ long nb_offset(const SecDesc& s, int dip) {
 // 2-D sections of a batch that also holds cubes have no crossline slope.
 __device__ __forceinline__ bool no_pass(const SecDesc& s, int dip) { return dip == 2 && s.n3 == 1; }
 
-template <int NW>
+template <int NW, bool FAST>
 __global__ void k_residual(DipArrays a, DipBatch b, ApCoef c, int dip) {
   const TileRange tr = tile_range(b, blockIdx.x);
   const SecDesc& s = b.secs[tr.sec];
@@ -143,13 +150,13 @@ __global__ void k_residual(DipArrays a, DipBatch b, ApCoef c, int dip) {
   float* u2 = a.u2 + s.off;
   const long ip = nb_offset(s, dip);
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
-    u2[i] = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false>(u, i, ip, c, p[i]) : 0.f;
+    u2[i] = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false, FAST>(u, i, ip, c, p[i]) : 0.f;
 }
 
 // One Gauss-Newton linearisation (dip3 :1645-1665 up to ps_divne's first
 // normalisation, ps_divne :796-815): derivative filter, residual energy,
 // mask, 1/hypot(den,1) scaling and the sum of den^2.
-template <int NW>
+template <int NW, bool FAST>
 __global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
   const int t = blockIdx.x;
   const TileRange tr = tile_range(b, t);
@@ -163,7 +170,7 @@ __global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
   ffacc a0, a1;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
     float pi = p[i];
-    float d = pwd_valid(s, i, NW, dip) ? pwd_at<NW, true>(u, i, ip, c, pi) : 0.f;
+    float d = pwd_valid(s, i, NW, dip) ? pwd_at<NW, true, FAST>(u, i, ip, c, pi) : 0.f;
     float r = u2[i];
     a0.add_prod(r, r);
     p0[i] = pi;
@@ -172,7 +179,13 @@ __global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
       r = 0.f;
     }
     float num, den;
-    invhypot_scale(r, d, num, den);
+    if (FAST) {
+      const float nrm = __frsqrt_rn(__fmaf_rn(d, d, 1.f));
+      num = __fmul_rn(r, nrm);
+      den = __fmul_rn(d, nrm);
+    } else {
+      invhypot_scale(r, d, num, den);
+    }
     u2[i] = num;
     u1[i] = den;
     a1.add_prod(den, den);
@@ -611,7 +624,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) k_tri_sweep(DipArrays a, Dip
 
 // One backtracking trial of dip3 :1666-1687: p = clip(p0 + lam*dp), new
 // residual and its energy; accepted when it decreases.
-template <int NW>
+template <int NW, bool FAST>
 __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
   const int t = blockIdx.x;
   const TileRange tr = tile_range(b, t);
@@ -629,7 +642,7 @@ __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
     if (pi < pmin) pi = pmin;
     if (pi > pmax) pi = pmax;
     p[i] = pi;
-    float r = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false>(u, i, ip, c, pi) : 0.f;
+    float r = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false, FAST>(u, i, ip, c, pi) : 0.f;
     u2[i] = r;
     a0.add_prod(r, r);
   }
@@ -698,14 +711,453 @@ __global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
 }
 
 // ---------------------------------------------------------------------------
+// Mixed mode of the shaping CG.
+//
+// ps_smooth2 along a line of length L with radius nb equals, in exact
+// arithmetic, the convolution with the triangle w(k) = (nb-|k|)/nb^2,
+// |k| < nb, of the line extended by half-sample mirroring (x[-1-i] = x[i],
+// x[2L-1-i] = x[i], repeated when nb > L): triple2's spread, the two running
+// sums and fold2's reflections are that operator.  The mixed mode applies it
+// as a direct convolution: axes 0 and 1 in one pass over a 2-D tile with a
+// halo staged in shared memory (axis 2 of cubes in a second, elementwise
+// pass), and folds the CG vector updates into the same passes, so that one
+// CG iteration reads and writes each vector about once: two launches for
+// 2-D sections instead of three elementwise kernels and four line sweeps.
+// The x and r vectors are double-buffered across iterations because the
+// halo of a tile reads neighbours that another tile steps.
+// ---------------------------------------------------------------------------
+// k_smooth12 strips: kSmB1 columns (one thread each) by up to kSmB2 rows.
+constexpr int kSmB1 = 64, kSmB2 = 128, kSmThreads = kSmB1;
+
+// Shared-memory floats of one k_smooth12 block for radii nb0, nb1.
+__host__ __device__ constexpr int sm_floats(int nb0, int nb1) {
+  return 2 * (kSmB1 + 2 * (nb0 - 1)) + (2 * nb1 - 1) * kSmB1;
+}
+enum { SM_IN_ARR = 0, SM_IN_CG1 = 1 };
+enum { SM_OUT_ARR = 0, SM_OUT_CG1 = 1, SM_OUT_CG2 = 2 };
+
+struct SmParams {
+  int sel;  // sections processed: 0 all, 1 slices of 2-D sections only, 2 cubes only
+  int nb0, nb1, nb2;
+  float wt0, wt1, wt2;
+  int iter;
+  const float* in;   // SM_IN_ARR input
+  float* out;        // SM_OUT_ARR output
+  const float* gpc;  // gp, read at the output sample by SM_OUT_CG2 of axis 2
+  const float *xo, *ro;
+  float *xn, *rn;
+};
+
+__device__ __forceinline__ bool sm_selected(int sel, const SecDesc& s) {
+  return sel == 0 || (sel == 1) == (s.n3 == 1);
+}
+
+__device__ __forceinline__ int mirror_idx(int i, int n) {
+  if (i >= 0 && i < n) return i;
+  if (i < 0 && i >= -n) return -1 - i;
+  if (i >= n && i < 2 * n) return 2 * n - 1 - i;
+  const int p = 2 * n;  // several reflections: the extension has period 2n
+  int r = i % p;
+  if (r < 0) r += p;
+  return r < n ? r : p - 1 - r;
+}
+
+// Triangle tap k of radius nb (|k| < nb).
+__device__ __forceinline__ float tri_tap(int k, int nb, float wt) {
+  return __fmul_rn((float)(nb - (k < 0 ? -k : k)), wt);
+}
+
+// Sum of K doubles over the tiles [tile0, tile0+ntile) of one section; true
+// in the block of the section's last tile to finish.
+template <int K>
+__device__ __forceinline__ bool tiles_sum_last(dvec<K> x, double* partials, int t, int tile0,
+                                               int ntile, unsigned* counter, dvec<K>& tot) {
+  __shared__ bool s_last;
+  dvec<K> blk = block_sum<K>(x);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) partials[(size_t)t * 3 + k] = blk.v[k];
+    __threadfence();
+    unsigned tk = atomicAdd(counter, 1u);
+    s_last = (tk == (unsigned)(ntile - 1));
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  dvec<K> y;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < ntile; i += blockDim.x)
+      v += __ldcg(partials + (size_t)(tile0 + i) * 3 + k);
+    y.v[k] = v;
+  }
+  tot = block_sum<K>(y);
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// gn = gp.gp, convergence test and alpha (ps_conjgrad :328-345), in the
+// last tile of a section.
+__device__ __forceinline__ void cg1_finish(DipScalars* S, double gn, int iter) {
+  S->gn = gn;
+  if (iter == 0) {
+    S->g0 = gn;
+  } else {
+    const double alpha = gn / S->gnp;
+    const double dg = gn / S->g0;
+    S->alpha = alpha;
+    const double tol = (double)1.e-6f;
+    if (alpha < tol || dg < tol) S->cg_done = 1;
+  }
+}
+
+// beta and the step (:346-359), in the last tile of a section.
+__device__ __forceinline__ void cg2_finish(DipScalars* S, const dvec<3>& tot, int iter) {
+  const double beta = tot.v[0] + 1.0 * (tot.v[1] - tot.v[2]);
+  S->step = -S->gn / beta;
+  S->gnp = S->gn;
+  S->cg_iters = iter + 1;
+}
+
+// Output operation at one sample given the smoothed value v.
+struct CgOut {
+  ffacc a0, a1, a2;
+  __device__ __forceinline__ void cg1(const DipArrays& a, long i, float v, float st, int iter) {
+    float p = a.pcg[i];
+    if (iter > 0) {
+      p = __fmaf_rn(st, a.sp[i], p);
+      a.pcg[i] = p;
+    }
+    const float g = __fadd_rn(p, v);  // gp = eps p + S' gx, eps = 1
+    a.gp[i] = g;
+    a0.add_prod(g, g);
+  }
+  // the same with the operands already loaded: pc = pcg, sv = sp
+  __device__ __forceinline__ void cg1v(const DipArrays& a, long i, float v, float st, int iter,
+                                       float pc, float sv) {
+    float p = pc;
+    if (iter > 0) {
+      p = __fmaf_rn(st, sv, p);
+      a.pcg[i] = p;
+    }
+    const float g = __fadd_rn(p, v);
+    a.gp[i] = g;
+    a0.add_prod(g, g);
+  }
+  __device__ __forceinline__ void cg2v(const DipArrays& a, long i, float gx, float gpv, float al,
+                                       int iter, float wv, float spv, float sxv, float srv) {
+    const float gr = __fmul_rn(gx, wv);
+    float vp = gpv, vx = gx, vr = gr;
+    if (iter > 0) {
+      vp = __fmaf_rn(al, spv, vp);
+      vx = __fmaf_rn(al, sxv, vx);
+      vr = __fmaf_rn(al, srv, vr);
+    }
+    a.sp[i] = vp;
+    a.sx[i] = vx;
+    a.sr[i] = vr;
+    a0.add_prod(vr, vr);
+    a1.add_prod(vp, vp);
+    a2.add_prod(vx, vx);
+  }
+  __device__ __forceinline__ void cg2(const DipArrays& a, long i, float gx, float gpv, float al,
+                                      int iter) {
+    const float gr = __fmul_rn(gx, a.u1[i]);
+    float vp = gpv, vx = gx, vr = gr;
+    if (iter > 0) {
+      vp = __fmaf_rn(al, a.sp[i], vp);
+      vx = __fmaf_rn(al, a.sx[i], vx);
+      vr = __fmaf_rn(al, a.sr[i], vr);
+    }
+    a.sp[i] = vp;
+    a.sx[i] = vx;
+    a.sr[i] = vr;
+    a0.add_prod(vr, vr);
+    a1.add_prod(vp, vp);
+    a2.add_prod(vx, vx);
+  }
+};
+
+// Smoothing along axes 0 and 1 of a strip of kSmB1 columns (samples along
+// axis 0) by up to kSmB2 rows (traces) of one slice, with the input and
+// output operations of the CG folded in.  One thread per output column
+// streams down the rows: the input row (with the axis-0 halo) goes through
+// a double-buffered shared row, the axis-0 result of each row enters the
+// thread's ring of the last 2 nb1 - 1 rows, and the axis-1 result of the
+// row nb1 - 1 behind is formed from the ring.  The next row's loads are in
+// flight while the current row is smoothed.  NB0, NB1 > 0 fix the radii at
+// compile time (constant taps, the ring in registers); 0 takes them from q
+// (the ring in shared memory, the thread's own column).
+template <int IN, int OUT, int NB0, int NB1>
+__global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b, SmParams q) {
+  extern __shared__ float sm[];
+  const int t = blockIdx.x;
+  const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
+  const SecDesc& s = b.secs[si];
+  if (!sm_selected(q.sel, s)) return;
+  DipScalars* S = b.S + si;
+  const int n1 = s.n1, n2 = s.n2;
+  const int nt1 = (n1 + kSmB1 - 1) / kSmB1, nt2 = (n2 + kSmB2 - 1) / kSmB2;
+  const int lt = t - s.ftile0;
+  const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
+  const int o1 = t1 * kSmB1, o2 = t2 * kSmB2;
+  const int rows = min(kSmB2, n2 - o2);
+  const long so = s.off + (long)i3 * n1 * n2;  // slice start
+  const int j = threadIdx.x;
+  const int g1 = o1 + j;                       // this thread's output column
+  const bool colok = g1 < n1;
+  if (S->cg_done) {
+    // a stopped section keeps its x and r: carry them to the new buffers
+    if (IN == SM_IN_CG1 && colok)
+      for (int r = 0; r < rows; r++) {
+        const long i = so + (long)(o2 + r) * n1 + g1;
+        q.xn[i] = q.xo[i];
+        q.rn[i] = q.ro[i];
+      }
+    return;
+  }
+  const int nb0 = NB0 > 0 ? NB0 : q.nb0, nb1 = NB1 > 0 ? NB1 : q.nb1;
+  const int h0 = nb0 - 1, h1 = nb1 - 1;
+  const int W0 = kSmB1 + 2 * h0;
+  float* rowbuf = sm;          // [2][W0]
+  float* sring = sm + 2 * W0;  // runtime radii: [2 h1 + 1][kSmB1]
+  const float st = (q.iter > 0 && (IN == SM_IN_CG1 || OUT == SM_OUT_CG1))
+                       ? __double2float_rn(S->step) : 0.f;
+  const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
+  const float wt0 = NB0 > 0 ? (float)(1.0 / (NB0 * NB0)) : q.wt0;
+  const float wt1 = NB1 > 0 ? (float)(1.0 / (NB1 * NB1)) : q.wt1;
+  // input columns of this thread: c = j + m kSmB1 (< W0)
+  constexpr int kCols = NB0 > 0 ? (kSmB1 + 2 * (NB0 - 1) + kSmB1 - 1) / kSmB1 : 3;
+  int gcol[kCols];
+  bool own[kCols];
+#pragma unroll
+  for (int m = 0; m < kCols; m++) {
+    const int c = j + m * kSmB1;
+    gcol[m] = c < W0 ? mirror_idx(o1 - h0 + c, n1) : -1;
+    own[m] = c >= h0 && c < h0 + kSmB1 && o1 - h0 + c < n1;
+  }
+  float rx[kCols], rsx[kCols], rr[kCols], rsr[kCols], rw[kCols];
+  float ov[5], ovn[5];  // operands of the output operation: this step, fetched step
+  auto fetch = [&](int step) {
+    const int g2 = mirror_idx(o2 - h1 + step, n2);
+    const long rowo = so + (long)g2 * n1;
+    const int orow = step - 2 * h1;
+    if (OUT != SM_OUT_ARR && orow >= 0 && colok) {
+      const long i = so + (long)(o2 + orow) * n1 + g1;
+      if (OUT == SM_OUT_CG1) {
+        ovn[0] = a.pcg[i];
+        if (q.iter > 0) ovn[1] = a.sp[i];
+      } else {
+        ovn[0] = q.in[i];
+        ovn[1] = a.u1[i];
+        if (q.iter > 0) {
+          ovn[2] = a.sp[i];
+          ovn[3] = a.sx[i];
+          ovn[4] = a.sr[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < kCols; m++) {
+      if (gcol[m] < 0) continue;
+      const long i = rowo + gcol[m];
+      if (IN == SM_IN_ARR) {
+        rx[m] = q.in[i];
+      } else {
+        rx[m] = q.xo[i];
+        rr[m] = q.ro[i];
+        rw[m] = a.u1[i];
+        if (q.iter > 0) {
+          rsx[m] = a.sx[i];
+          rsr[m] = a.sr[i];
+        }
+      }
+    }
+  };
+  // 1. input operation of one row into the shared row buffer, then the
+  //    next row's loads
+  const int nsteps = rows + 2 * h1;
+  auto in_row = [&](int step) {
+    const int r = o2 - h1 + step;  // input row (unmirrored)
+    const bool ownrow = r >= o2 && r < o2 + rows;
+    const long rowo = so + (long)r * n1;
+    float* rb = rowbuf + (step & 1) * W0;
+#pragma unroll
+    for (int m = 0; m < kCols; m++) {
+      if (gcol[m] < 0) continue;
+      float v;
+      if (IN == SM_IN_ARR) {
+        v = rx[m];
+      } else {
+        float xi = rx[m], ri = rr[m];
+        if (q.iter > 0) {
+          xi = __fmaf_rn(st, rsx[m], xi);
+          ri = __fmaf_rn(st, rsr[m], ri);
+        }
+        v = __fmaf_rn(ri, rw[m], -xi);  // gx = -eps x + W' r
+        if (ownrow && own[m]) {
+          q.xn[rowo + gcol[m]] = xi;
+          q.rn[rowo + gcol[m]] = ri;
+        }
+      }
+      rb[j + m * kSmB1] = v;
+    }
+    if (step + 1 < nsteps) fetch(step + 1);
+  };
+  // 2. axis 0 at this thread's column
+  auto axis0 = [&](int step) -> float {
+    const float* row = rowbuf + (step & 1) * W0 + j + h0;
+    float acc = __fmul_rn(tri_tap(0, nb0, wt0), row[0]);
+    if (NB0 > 0) {
+#pragma unroll
+      for (int k = 1; k < NB0; k++)
+        acc = __fmaf_rn(tri_tap(k, NB0, wt0), __fadd_rn(row[-k], row[k]), acc);
+    } else {
+      for (int k = 1; k <= h0; k++)
+        acc = __fmaf_rn(tri_tap(k, nb0, wt0), __fadd_rn(row[-k], row[k]), acc);
+    }
+    return acc;
+  };
+  // 3. output operation of output row orow
+  CgOut co;
+  auto out_op = [&](int orow, float acc) {
+    if (!colok) return;
+    const long i = so + (long)(o2 + orow) * n1 + g1;
+    if (OUT == SM_OUT_ARR)
+      q.out[i] = acc;
+    else if (OUT == SM_OUT_CG1)
+      co.cg1v(a, i, acc, st, q.iter, ov[0], ov[1]);
+    else
+      co.cg2v(a, i, acc, ov[0], al, q.iter, ov[1], ov[2], ov[3], ov[4]);
+  };
+  auto next_ops = [&]() {
+#pragma unroll
+    for (int k = 0; k < 5; k++) ov[k] = ovn[k];
+  };
+  fetch(0);
+  next_ops();
+  if (NB1 > 0) {
+    constexpr int H1 = NB1 > 0 ? NB1 - 1 : 0, RING = 2 * H1 + 1;
+    float w1r[H1 + 1];
+#pragma unroll
+    for (int k = 0; k <= H1; k++) w1r[k] = tri_tap(k, NB1, wt1);
+    float rg[RING];
+    for (int step0 = 0; step0 < nsteps; step0 += RING) {
+#pragma unroll
+      for (int u = 0; u < RING; u++) {
+        const int step = step0 + u;
+        if (step < nsteps) {
+          in_row(step);
+          __syncthreads();
+          rg[u] = axis0(step);
+          if (step >= 2 * H1) {
+            // centre: ring slot of step - H1
+            float acc = __fmul_rn(w1r[0], rg[(u - H1 + RING) % RING]);
+#pragma unroll
+            for (int k = 1; k <= H1; k++)
+              acc = __fmaf_rn(w1r[k],
+                              __fadd_rn(rg[(u - H1 - k + 2 * RING) % RING],
+                                        rg[(u - H1 + k + RING) % RING]),
+                              acc);
+            out_op(step - 2 * H1, acc);
+          }
+          next_ops();
+        }
+      }
+    }
+  } else {
+    const int RING = 2 * h1 + 1;
+    int slot = 0;  // ring slot of the current input row
+    for (int step = 0; step < nsteps; step++) {
+      in_row(step);
+      __syncthreads();
+      sring[slot * kSmB1 + j] = axis0(step);
+      if (step >= 2 * h1) {
+        int c = slot - h1;
+        if (c < 0) c += RING;
+        float acc = __fmul_rn(tri_tap(0, nb1, wt1), sring[c * kSmB1 + j]);
+        int lo = c, hi = c;
+        for (int k = 1; k <= h1; k++) {
+          lo = lo == 0 ? RING - 1 : lo - 1;
+          hi = hi == RING - 1 ? 0 : hi + 1;
+          acc = __fmaf_rn(tri_tap(k, nb1, wt1),
+                          __fadd_rn(sring[lo * kSmB1 + j], sring[hi * kSmB1 + j]), acc);
+        }
+        out_op(step - 2 * h1, acc);
+      }
+      next_ops();
+      slot = slot == RING - 1 ? 0 : slot + 1;
+    }
+  }
+  if (OUT == SM_OUT_CG1) {
+    dvec<1> acc = {{co.a0.value()}};
+    dvec<1> tot;
+    if (tiles_sum_last<1>(acc, b.partials, t, s.ftile0, s.nftile, &S->cnt[2], tot) &&
+        threadIdx.x == 0)
+      cg1_finish(S, tot.v[0], q.iter);
+  } else if (OUT == SM_OUT_CG2) {
+    dvec<3> acc = {{co.a0.value(), co.a1.value(), co.a2.value()}};
+    dvec<3> tot;
+    if (tiles_sum_last<3>(acc, b.partials, t, s.ftile0, s.nftile, &S->cnt[3], tot) &&
+        threadIdx.x == 0)
+      cg2_finish(S, tot, q.iter);
+  }
+}
+
+// Smoothing along axis 2 (cubes), elementwise tiles, with the CG output
+// operation.
+template <int OUT>
+__global__ void k_smooth3(DipArrays a, DipBatch b, SmParams q) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  DipScalars* S = b.S + tr.sec;
+  if (!sm_selected(q.sel, s) || S->cg_done) return;
+  const int n3 = s.n3, h2 = q.nb2 - 1;
+  const long n12 = (long)s.n1 * s.n2;
+  const float st = (OUT == SM_OUT_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
+  const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
+  const float* src = q.in + s.off;
+  CgOut co;
+  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
+    const int i3 = (int)(j / n12);
+    const long rem = j - (long)i3 * n12;
+    float acc = __fmul_rn(tri_tap(0, q.nb2, q.wt2), src[j]);
+    for (int k = 1; k <= h2; k++) {
+      const float lo = src[rem + n12 * mirror_idx(i3 - k, n3)];
+      const float hi = src[rem + n12 * mirror_idx(i3 + k, n3)];
+      acc = __fmaf_rn(tri_tap(k, q.nb2, q.wt2), __fadd_rn(lo, hi), acc);
+    }
+    const long i = s.off + j;
+    if (OUT == SM_OUT_CG1)
+      co.cg1(a, i, acc, st, q.iter);
+    else
+      co.cg2(a, i, acc, q.gpc[i], al, q.iter);
+  }
+  if (OUT == SM_OUT_CG1) {
+    dvec<1> acc = {{co.a0.value()}};
+    dvec<1> tot;
+    if (sec_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0)
+      cg1_finish(S, tot.v[0], q.iter);
+  } else {
+    dvec<3> acc = {{co.a0.value(), co.a1.value(), co.a2.value()}};
+    dvec<3> tot;
+    if (sec_sum_last<3>(acc, b, t, s, &S->cnt[3], tot) && threadIdx.x == 0)
+      cg2_finish(S, tot, q.iter);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 struct DipLayout {
   long ntot;  // elements spanned by the input arrays
   int ntiles;
+  int nftiles;  // 2-D smoothing tiles (mixed mode)
   long scr_total;
   long nlines[3];
-  bool any3d;
+  bool any3d, any2d;
 };
 
 // Completes the section table (tiles, triangle line numbering and scratch).
@@ -717,9 +1169,13 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
     s.n = (long)s.n1 * s.n2 * s.n3;
     L.ntot = std::max(L.ntot, s.off + s.n);
     L.any3d |= s.n3 > 1;
+    L.any2d |= s.n3 == 1;
     s.tile0 = tiles;
     s.ntile = (int)((s.n + kTile - 1) / kTile);
     tiles += s.ntile;
+    s.ftile0 = L.nftiles;
+    s.nftile = ((s.n1 + kSmB1 - 1) / kSmB1) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
+    L.nftiles += s.nftile;
     const int len[3] = {s.n1, s.n2, s.n3};
     for (int a = 0; a < 3; a++) {
       s.line0[a] = lines[a];
@@ -747,7 +1203,8 @@ struct DipWork {
   double* partials;
 };
 
-DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t* total) {
+DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t* total,
+                  bool mixed = false) {
   Carver cv(ws);
   DipWork w{};
   const long n = L.ntot;
@@ -762,13 +1219,15 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.sp = cv.take<float>(n);
   w.a.sx = cv.take<float>(n);
   w.a.sr = cv.take<float>(n);
-  w.a.tri = cv.take<float>(L.scr_total);
+  w.a.tri = mixed ? nullptr : cv.take<float>(L.scr_total);
+  w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
+  w.a.r2 = mixed ? cv.take<float>(n) : nullptr;
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.m1 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.secs = cv.take<SecDesc>(nsec);
   w.tile_sec = cv.take<int>(L.ntiles);
   w.S = cv.take<DipScalars>(nsec);
-  w.partials = cv.take<double>((size_t)L.ntiles * 3);
+  w.partials = cv.take<double>((size_t)std::max(L.ntiles, mixed ? L.nftiles : 0) * 3);
   *total = cv.size();
   return w;
 }
@@ -807,9 +1266,9 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
                  kern<<<grid, 32 * kSweepWarps, smem, st>>>(a, b, tp[k]));
     }
   };
-  PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
+  PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW, false><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
   for (int iter = 0; iter < niter; iter++) {
-    PWD_KERNEL(PWD_FAM_PWD, st, k_prep<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
+    PWD_KERNEL(PWD_FAM_PWD, st, k_prep<NW, false><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
     PWD_KERNEL(PWD_FAM_CG, st, k_scale<<<gt, kTileThreads, 0, st>>>(a, b, dip));
     for (int it = 0; it < liter; it++) {
       PWD_KERNEL(PWD_FAM_CG, st, k_cg_stepgrad<<<gt, kTileThreads, 0, st>>>(a, b, it));
@@ -820,13 +1279,108 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
     }
     if (liter > 0) PWD_KERNEL(PWD_FAM_CG, st, k_cg_step<<<gt, kTileThreads, 0, st>>>(a, b));
     for (int k = 0; k < 8; k++)
-      PWD_KERNEL(PWD_FAM_PWD, st, k_ls_trial<NW><<<gt, kTileThreads, 0, st>>>(a, b, c, dip, k));
+      PWD_KERNEL(PWD_FAM_PWD, st,
+                 k_ls_trial<NW, false><<<gt, kTileThreads, 0, st>>>(a, b, c, dip, k));
+  }
+  return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
+}
+
+typedef void (*SmKernel)(DipArrays, DipBatch, SmParams);
+
+// The k_smooth12 instance for radii nb0, nb1: compiled radii for the common
+// 10 x 10 (2-D sections) and 5 x 5 (cubes), runtime radii otherwise.
+template <int IN, int OUT>
+SmKernel sm_kernel(int nb0, int nb1) {
+  if (nb0 == 10 && nb1 == 10) return k_smooth12<IN, OUT, 10, 10>;
+  if (nb0 == 5 && nb1 == 5) return k_smooth12<IN, OUT, 5, 5>;
+  return k_smooth12<IN, OUT, 0, 0>;
+}
+
+// Mixed mode of dip3: FP32 filter taps, the fused smoothing passes of the
+// shaping CG, FP64 reductions as in the plain path.
+template <int NW>
+int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3],
+                   const DipLayout& L, const DipBatch& b, cudaStream_t st) {
+  const ApCoef c = make_apcoef(NW);
+  SmParams q{};
+  q.nb0 = std::max(rect[0], 1);
+  q.nb1 = std::max(rect[1], 1);
+  q.nb2 = std::max(rect[2], 1);
+  q.wt0 = (float)(1.0 / ((double)q.nb0 * q.nb0));
+  q.wt1 = (float)(1.0 / ((double)q.nb1 * q.nb1));
+  q.wt2 = (float)(1.0 / ((double)q.nb2 * q.nb2));
+  const bool ax2 = q.nb2 > 1 && L.any3d;
+  const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
+  const size_t smem = sizeof(float) * (size_t)sm_floats(q.nb0, q.nb1);
+  const SmKernel k_cg1 = sm_kernel<SM_IN_CG1, SM_OUT_CG1>(q.nb0, q.nb1);
+  const SmKernel k_cg2 = sm_kernel<SM_IN_ARR, SM_OUT_CG2>(q.nb0, q.nb1);
+  const SmKernel k_in1 = sm_kernel<SM_IN_CG1, SM_OUT_ARR>(q.nb0, q.nb1);
+  const SmKernel k_arr = sm_kernel<SM_IN_ARR, SM_OUT_ARR>(q.nb0, q.nb1);
+  for (SmKernel k : {k_cg1, k_cg2, k_in1, k_arr})
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  float* X[2] = {a.dp, a.x2};
+  float* Rv[2] = {a.r, a.r2};
+  PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW, true><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
+  for (int iter = 0; iter < niter; iter++) {
+    PWD_KERNEL(PWD_FAM_PWD, st, k_prep<NW, true><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
+    PWD_KERNEL(PWD_FAM_CG, st, k_scale<<<gt, kTileThreads, 0, st>>>(a, b, dip));
+    for (int it = 0; it < liter; it++) {
+      q.iter = it;
+      q.xo = X[it & 1];
+      q.ro = Rv[it & 1];
+      q.xn = X[(it + 1) & 1];
+      q.rn = Rv[(it + 1) & 1];
+      // 2-D sections (every section when no cube is smoothed along axis 2):
+      // both passes fused; the axis-2 smoothing of a length-1 line is the
+      // identity
+      if (!ax2 || L.any2d) {
+        q.sel = ax2 ? 1 : 0;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   (k_cg1<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        q.in = a.gp;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   (k_cg2<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+      }
+      if (ax2) {  // cubes: axes 0-1 pass, then the axis-2 pass with the CG operation
+        q.sel = 2;
+        q.out = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   (k_in1<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        q.in = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   k_smooth3<SM_OUT_CG1><<<gt, kTileThreads, 0, st>>>(a, b, q));
+        q.in = a.gp;
+        q.out = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   (k_arr<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        q.in = a.tmp;
+        q.gpc = a.gp;
+        PWD_KERNEL(PWD_FAM_CG, st,
+                   k_smooth3<SM_OUT_CG2><<<gt, kTileThreads, 0, st>>>(a, b, q));
+      }
+    }
+    DipArrays af = a;  // x and r after the last iteration
+    af.dp = X[liter & 1];
+    af.r = Rv[liter & 1];
+    if (liter > 0) PWD_KERNEL(PWD_FAM_CG, st, k_cg_step<<<gt, kTileThreads, 0, st>>>(af, b));
+    for (int k = 0; k < 8; k++)
+      PWD_KERNEL(PWD_FAM_PWD, st,
+                 k_ls_trial<NW, true><<<gt, kTileThreads, 0, st>>>(af, b, c, dip, k));
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
 int dip_dispatch(int order, DipArrays a, int dip, int niter, int liter, const int rect[3],
-                 const DipLayout& L, const DipBatch& b, cudaStream_t st) {
+                 const DipLayout& L, const DipBatch& b, cudaStream_t st, bool mixed) {
+  if (mixed) {
+    switch (order) {
+      case 1: return dip3_run_mixed<1>(a, dip, niter, liter, rect, L, b, st);
+      case 2: return dip3_run_mixed<2>(a, dip, niter, liter, rect, L, b, st);
+      case 3: return dip3_run_mixed<3>(a, dip, niter, liter, rect, L, b, st);
+      case 4: return dip3_run_mixed<4>(a, dip, niter, liter, rect, L, b, st);
+    }
+    return PWD_ENOTSUP;
+  }
   switch (order) {
     case 1: return dip3_run<1>(a, dip, niter, liter, rect, L, b, st);
     case 2: return dip3_run<2>(a, dip, niter, liter, rect, L, b, st);
@@ -839,7 +1393,7 @@ int dip_dispatch(int order, DipArrays a, int dip, int niter, int liter, const in
 // Enqueues the estimation of a batch whose section table is in w.secs.
 int dip_enqueue(const float* data, const float* mask, float* out, const DipLayout& L,
                 const DipWork& w, int nsec, int niter, int liter, int order, const int rect[3],
-                cudaStream_t st) {
+                cudaStream_t st, bool mixed = false) {
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
   if (cudaMemsetAsync(w.S, 0, sizeof(DipScalars) * nsec, st) != cudaSuccess) return PWD_ECUDA;
@@ -852,13 +1406,13 @@ int dip_enqueue(const float* data, const float* mask, float* out, const DipLayou
     PWD_KERNEL(PWD_FAM_OTHER, st,
                k_mask32<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(mask, w.m0, w.m1, b, order));
   a.mask = mask ? w.m0 : nullptr;
-  int rc = dip_dispatch(order, a, 1, niter, liter, rect, L, b, st);
+  int rc = dip_dispatch(order, a, 1, niter, liter, rect, L, b, st, mixed);
   if (rc != PWD_OK || !L.any3d) return rc;
   // crossline slopes (dipc :1926); 2-D sections of a mixed batch skip them
   // because their crossline residual region is empty (n3 = 1).
   a.mask = mask ? w.m1 : nullptr;
   PWD_KERNEL(PWD_FAM_OTHER, st, k_skip_2d<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.S));
-  return dip_dispatch(order, a, 2, niter, liter, rect, L, b, st);
+  return dip_dispatch(order, a, 2, niter, liter, rect, L, b, st, mixed);
 }
 
 int check_dip_args(int niter, int liter, int order, const int rect[3]) {
@@ -945,10 +1499,12 @@ extern "C" size_t pwd_dip_batch_workspace_size(const pwd_section* sections, int 
   return need;
 }
 
-extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_out,
-                             const pwd_section* sections, int nsec, int niter, int liter,
-                             int order, const int rect[3], void* workspace,
-                             size_t workspace_bytes, pwd_stream_t stream) {
+namespace {
+
+int dip_batch_common(const float* data, const float* mask, float* dip_out,
+                     const pwd_section* sections, int nsec, int niter, int liter, int order,
+                     const int rect[3], void* workspace, size_t workspace_bytes,
+                     pwd_stream_t stream, bool mixed) {
   int rc = check_dip_args(niter, liter, order, rect);
   if (rc != PWD_OK) return rc;
   if (!data || !dip_out) return PWD_EINVAL;
@@ -956,14 +1512,43 @@ extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_ou
   if ((rc = batch_table(sections, nsec, order, secs)) != PWD_OK) return rc;
   DipLayout L = layout(secs, rect);
   size_t need = 0;
-  carve_dip(nullptr, L, nsec, mask != nullptr, &need);
+  carve_dip(nullptr, L, nsec, mask != nullptr, &need, mixed);
   if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  DipWork w = carve_dip(workspace, L, nsec, mask != nullptr, &need);
+  DipWork w = carve_dip(workspace, L, nsec, mask != nullptr, &need, mixed);
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
       cudaSuccess)
     return PWD_ECUDA;
-  return dip_enqueue(data, mask, dip_out, L, w, nsec, niter, liter, order, rect, st);
+  return dip_enqueue(data, mask, dip_out, L, w, nsec, niter, liter, order, rect, st, mixed);
+}
+
+}  // namespace
+
+extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_out,
+                             const pwd_section* sections, int nsec, int niter, int liter,
+                             int order, const int rect[3], void* workspace,
+                             size_t workspace_bytes, pwd_stream_t stream) {
+  return dip_batch_common(data, mask, dip_out, sections, nsec, niter, liter, order, rect,
+                          workspace, workspace_bytes, stream, false);
+}
+
+extern "C" size_t pwd_dip_batch_mixed_workspace_size(const pwd_section* sections, int nsec,
+                                                     int order, const int rect[3],
+                                                     int has_mask) {
+  std::vector<SecDesc> secs;
+  if (!rect || batch_table(sections, nsec, std::max(order, 1), secs) != PWD_OK) return 0;
+  DipLayout L = layout(secs, rect);
+  size_t need = 0;
+  carve_dip(nullptr, L, nsec, has_mask != 0, &need, true);
+  return need;
+}
+
+extern "C" int pwd_dip_batch_mixed(const float* data, const float* mask, float* dip_out,
+                                   const pwd_section* sections, int nsec, int niter, int liter,
+                                   int order, const int rect[3], void* workspace,
+                                   size_t workspace_bytes, pwd_stream_t stream) {
+  return dip_batch_common(data, mask, dip_out, sections, nsec, niter, liter, order, rect,
+                          workspace, workspace_bytes, stream, true);
 }
 
 // ---------------------------------------------------------------------------

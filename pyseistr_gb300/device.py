@@ -166,22 +166,26 @@ def section_table(shapes, offsets=None, out_offsets=None):
 
 
 def dip_batch(data, shapes, niter=5, liter=20, order=2, rect=(10, 10, 1), mask=None, out=None,
-              workspace=None):
+              workspace=None, mixed=False):
     """Slopes of many sections packed one after another in `data` (flat,
     each section column-major), all in one launch sequence.  Returns the
-    packed slopes (n per 2-D section, 2n per cube)."""
+    packed slopes (n per 2-D section, 2n per cube).  mixed=True selects the
+    mixed mode (FP32 taps, fused convolution smoothing, FP64 reductions)
+    instead of the bit-faithful plain path."""
     L = _lib.load()
     tab, ntot, nout = section_table(shapes)
     data = _as_flat(data, ntot, "data")
     if mask is not None:
         mask = _as_flat(mask, ntot, "mask")
     rc = (ctypes.c_int * 3)(*[int(r) for r in rect])
-    nbytes = L.pwd_dip_batch_workspace_size(tab, len(shapes), order, rc, int(mask is not None))
+    size_fn = L.pwd_dip_batch_mixed_workspace_size if mixed else L.pwd_dip_batch_workspace_size
+    run_fn = L.pwd_dip_batch_mixed if mixed else L.pwd_dip_batch
+    nbytes = size_fn(tab, len(shapes), order, rc, int(mask is not None))
     ws = _workspace(nbytes, data.device, workspace)
     if out is None:
         out = torch.empty(nout, dtype=torch.float32, device=data.device)
-    _lib.check(L.pwd_dip_batch(_ptr(data), _ptr(mask), _ptr(out), tab, len(shapes), niter, liter,
-                               order, rc, _ptr(ws), ws.numel(), _stream()), "dip_batch")
+    _lib.check(run_fn(_ptr(data), _ptr(mask), _ptr(out), tab, len(shapes), niter, liter,
+                      order, rc, _ptr(ws), ws.numel(), _stream()), "dip_batch")
     return out
 
 

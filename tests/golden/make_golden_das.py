@@ -1,0 +1,64 @@
+"""Full-size golden fixture of the DAS slope workload (2000 x 5000 record,
+dip2d niter=5, liter=20, order=2, rect=10,10,1).
+
+Runs the reference's own FP32 dipc (oracle/_ref/dipcfun, compiled from the
+reference sources by ``make -C oracle ref``) and the FP64 evaluation of the
+same algorithm (the oracle's double instantiation) on the seeded record of
+``workloads.das2d(seed=2023)``, and stores both slope fields at 32768 seeded
+random samples, plus each field's relative L2 distance to the FP64 field
+over the whole record.
+
+    make -C oracle ref && python tests/golden/make_golden_das.py
+
+Takes a few minutes on one core.  The fixture is what the full-size GPU
+tests read.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+sys.path.insert(0, ROOT)
+
+import dipcfun  # noqa: E402
+
+import workloads as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+NSAMPLE = 32768
+
+
+def main():
+    d = W.das2d(seed=2023)
+    n1, n2 = d.shape
+    fd = os.dup(1)
+    nul = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(nul, 1)
+    try:
+        # dipc positional tuple (dip_cfuns.c:1708) as dip2dc passes it
+        ref = np.asarray(dipcfun.dipc(np.float32(d.flatten(order="F")), n1, n2, 1, 5, 20, 2,
+                                      0.01, 1.0, 1e-6, 10, 10, 1, 0, 0), np.float32)
+    finally:
+        os.dup2(fd, 1)
+        os.close(fd)
+        os.close(nul)
+    ref = ref.reshape(n1, n2, order="F")
+    f64 = O.dip2d(d, 5, 20, 2, (10, 10, 1), precision="f64")
+    rng = np.random.default_rng(7)
+    idx = np.sort(rng.choice(d.size, NSAMPLE, replace=False)).astype(np.int64)
+    flat = lambda a: np.asarray(a).reshape(-1, order="F")  # noqa: E731
+    rel = float(np.linalg.norm(np.float64(flat(ref)) - flat(f64)) / np.linalg.norm(flat(f64)))
+    np.savez_compressed(os.path.join(HERE, "golden_das_full.npz"), idx=idx,
+                        ref32=flat(ref)[idx].astype(np.float32),
+                        f64=flat(f64)[idx].astype(np.float64),
+                        ref32_rel_l2_vs_f64=np.float64(rel), shape=np.array([n1, n2]))
+    print("reference FP32 vs FP64 relative L2 over the record:", rel)
+
+
+if __name__ == "__main__":
+    main()
