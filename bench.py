@@ -413,7 +413,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
                     help="sections of the batch2d workload (smaller counts for profiler captures)")
-    ap.add_argument("--precision", choices=["plain", "mixed"], default="plain",
+    ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed",
                     help="slope estimation arithmetic: plain (bit-faithful FP32) or mixed "
                          "(FP32 taps, fused convolution smoothing, FP64 reductions)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -497,7 +497,7 @@ def main():
         try:
             with open(tpath) as fh:
                 tj = json.load(fh)
-            ent = tj.get(wl.name, {}).get(dom)
+            ent = tj.get(wl.name, {}).get(args.precision, {}).get(dom)
             if ent:
                 traffic = ent["bytes_per_sample"] * wl.samples()
         except (OSError, ValueError, KeyError):

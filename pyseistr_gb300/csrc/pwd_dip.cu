@@ -726,12 +726,28 @@ __global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
 // The x and r vectors are double-buffered across iterations because the
 // halo of a tile reads neighbours that another tile steps.
 // ---------------------------------------------------------------------------
-// k_smooth12 strips: kSmB1 columns (one thread each) by up to kSmB2 rows.
-constexpr int kSmB1 = 64, kSmB2 = 128, kSmThreads = kSmB1;
+// k_smooth12 strips: kSmB1 columns (one thread each) by up to kSmB2 rows,
+// input rows staged kSmStages - 1 steps ahead.
+constexpr int kSmB1 = 64, kSmB2 = 128, kSmThreads = kSmB1, kSmStages = 4;
 
-// Shared-memory floats of one k_smooth12 block for radii nb0, nb1.
-__host__ __device__ constexpr int sm_floats(int nb0, int nb1) {
-  return 2 * (kSmB1 + 2 * (nb0 - 1)) + (2 * nb1 - 1) * kSmB1;
+// Shared-memory floats of one k_smooth12 block for radii nb0, nb1: row
+// buffers, ring (runtime radii), staging.
+__host__ __device__ constexpr int sm_floats(int nb0, int nb1, bool ring) {
+  return 2 * (kSmB1 + 2 * (nb0 - 1)) + (ring ? (2 * nb1 - 1) * kSmB1 : 0) +
+         kSmStages * (5 * (kSmB1 + 2 * (nb0 - 1)) + 5 * kSmB1);
+}
+
+// 4-byte asynchronous global-to-shared copies (cp.async, sm_80 and later).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 enum { SM_IN_ARR = 0, SM_IN_CG1 = 1 };
 enum { SM_OUT_ARR = 0, SM_OUT_CG1 = 1, SM_OUT_CG2 = 2 };
@@ -765,6 +781,11 @@ __device__ __forceinline__ int mirror_idx(int i, int n) {
 // Triangle tap k of radius nb (|k| < nb).
 __device__ __forceinline__ float tri_tap(int k, int nb, float wt) {
   return __fmul_rn((float)(nb - (k < 0 ? -k : k)), wt);
+}
+// The same for a radius known at compile time: a constant operand.
+template <int NB>
+__host__ __device__ constexpr float tri_tap_c(int k) {
+  return (float)((double)(NB - (k < 0 ? -k : k)) / ((double)NB * NB));
 }
 
 // Sum of K doubles over the tiles [tile0, tile0+ntile) of one section; true
@@ -890,7 +911,7 @@ struct CgOut {
 // compile time (constant taps, the ring in registers); 0 takes them from q
 // (the ring in shared memory, the thread's own column).
 template <int IN, int OUT, int NB0, int NB1>
-__global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b, SmParams q) {
+__global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBatch b, SmParams q) {
   extern __shared__ float sm[];
   const int t = blockIdx.x;
   const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
@@ -937,48 +958,62 @@ __global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b
     gcol[m] = c < W0 ? mirror_idx(o1 - h0 + c, n1) : -1;
     own[m] = c >= h0 && c < h0 + kSmB1 && o1 - h0 + c < n1;
   }
-  float rx[kCols], rsx[kCols], rr[kCols], rsr[kCols], rw[kCols];
-  float ov[5], ovn[5];  // operands of the output operation: this step, fetched step
-  auto fetch = [&](int step) {
-    const int g2 = mirror_idx(o2 - h1 + step, n2);
-    const long rowo = so + (long)g2 * n1;
-    const int orow = step - 2 * h1;
-    if (OUT != SM_OUT_ARR && orow >= 0 && colok) {
-      const long i = so + (long)(o2 + orow) * n1 + g1;
-      if (OUT == SM_OUT_CG1) {
-        ovn[0] = a.pcg[i];
-        if (q.iter > 0) ovn[1] = a.sp[i];
-      } else {
-        ovn[0] = q.in[i];
-        ovn[1] = a.u1[i];
-        if (q.iter > 0) {
-          ovn[2] = a.sp[i];
-          ovn[3] = a.sx[i];
-          ovn[4] = a.sr[i];
-        }
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < kCols; m++) {
-      if (gcol[m] < 0) continue;
-      const long i = rowo + gcol[m];
-      if (IN == SM_IN_ARR) {
-        rx[m] = q.in[i];
-      } else {
-        rx[m] = q.xo[i];
-        rr[m] = q.ro[i];
-        rw[m] = a.u1[i];
-        if (q.iter > 0) {
-          rsx[m] = a.sx[i];
-          rsr[m] = a.sr[i];
-        }
-      }
-    }
-  };
-  // 1. input operation of one row into the shared row buffer, then the
-  //    next row's loads
+  // Rows are staged in shared memory kSmStages - 1 steps ahead by cp.async
+  // (4-byte copies, each thread its own columns and its own output operands,
+  // so a thread only waits for its own copies): stage [NARR][W0] of the
+  // input row, then [5][kSmB1] of the output operands.
+  constexpr int NARR = IN == SM_IN_ARR ? 1 : 5;
+  const int stage_f = NARR * W0 + 5 * kSmB1;
+  float* stg = sring + (NB1 > 0 ? 0 : (2 * h1 + 1) * kSmB1);
   const int nsteps = rows + 2 * h1;
+  auto issue = [&](int step) {
+    if (step < nsteps) {
+      float* sg = stg + (step % kSmStages) * stage_f;
+      const int g2 = mirror_idx(o2 - h1 + step, n2);
+      const long rowo = so + (long)g2 * n1;
+#pragma unroll
+      for (int m = 0; m < kCols; m++) {
+        if (gcol[m] < 0) continue;
+        const long i = rowo + gcol[m];
+        const int c = j + m * kSmB1;
+        if (IN == SM_IN_ARR) {
+          cp_async4(sg + c, q.in + i);
+        } else {
+          cp_async4(sg + c, q.xo + i);
+          cp_async4(sg + W0 + c, q.ro + i);
+          cp_async4(sg + 2 * W0 + c, a.u1 + i);
+          if (q.iter > 0) {
+            cp_async4(sg + 3 * W0 + c, a.sx + i);
+            cp_async4(sg + 4 * W0 + c, a.sr + i);
+          }
+        }
+      }
+      const int orow = step - 2 * h1;
+      if (OUT != SM_OUT_ARR && orow >= 0 && colok) {
+        const long i = so + (long)(o2 + orow) * n1 + g1;
+        float* so_ = sg + NARR * W0 + j;
+        if (OUT == SM_OUT_CG1) {
+          cp_async4(so_, a.pcg + i);
+          if (q.iter > 0) cp_async4(so_ + kSmB1, a.sp + i);
+        } else {
+          cp_async4(so_, q.in + i);
+          cp_async4(so_ + kSmB1, a.u1 + i);
+          if (q.iter > 0) {
+            cp_async4(so_ + 2 * kSmB1, a.sp + i);
+            cp_async4(so_ + 3 * kSmB1, a.sx + i);
+            cp_async4(so_ + 4 * kSmB1, a.sr + i);
+          }
+        }
+      }
+    }
+    cp_async_commit();  // one group per step, empty past the end
+  };
+  float ov[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // operands of this step's output operation
+  // 1. input operation of one row (staged) into the shared row buffer
   auto in_row = [&](int step) {
+    issue(step + kSmStages - 1);
+    cp_async_wait<kSmStages - 1>();  // this step's row has landed
+    const float* sg = stg + (step % kSmStages) * stage_f;
     const int r = o2 - h1 + step;  // input row (unmirrored)
     const bool ownrow = r >= o2 && r < o2 + rows;
     const long rowo = so + (long)r * n1;
@@ -986,34 +1021,41 @@ __global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b
 #pragma unroll
     for (int m = 0; m < kCols; m++) {
       if (gcol[m] < 0) continue;
+      const int c = j + m * kSmB1;
       float v;
       if (IN == SM_IN_ARR) {
-        v = rx[m];
+        v = sg[c];
       } else {
-        float xi = rx[m], ri = rr[m];
+        float xi = sg[c], ri = sg[W0 + c];
         if (q.iter > 0) {
-          xi = __fmaf_rn(st, rsx[m], xi);
-          ri = __fmaf_rn(st, rsr[m], ri);
+          xi = __fmaf_rn(st, sg[3 * W0 + c], xi);
+          ri = __fmaf_rn(st, sg[4 * W0 + c], ri);
         }
-        v = __fmaf_rn(ri, rw[m], -xi);  // gx = -eps x + W' r
+        v = __fmaf_rn(ri, sg[2 * W0 + c], -xi);  // gx = -eps x + W' r
         if (ownrow && own[m]) {
           q.xn[rowo + gcol[m]] = xi;
           q.rn[rowo + gcol[m]] = ri;
         }
       }
-      rb[j + m * kSmB1] = v;
+      rb[c] = v;
     }
-    if (step + 1 < nsteps) fetch(step + 1);
+    if (OUT != SM_OUT_ARR) {
+#pragma unroll
+      for (int k = 0; k < 5; k++) ov[k] = sg[NARR * W0 + k * kSmB1 + j];
+    }
   };
   // 2. axis 0 at this thread's column
   auto axis0 = [&](int step) -> float {
     const float* row = rowbuf + (step & 1) * W0 + j + h0;
-    float acc = __fmul_rn(tri_tap(0, nb0, wt0), row[0]);
+    float acc;
     if (NB0 > 0) {
+      constexpr int NB0c = NB0 > 0 ? NB0 : 1;
+      acc = __fmul_rn(tri_tap_c<NB0c>(0), row[0]);
 #pragma unroll
       for (int k = 1; k < NB0; k++)
-        acc = __fmaf_rn(tri_tap(k, NB0, wt0), __fadd_rn(row[-k], row[k]), acc);
+        acc = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc);
     } else {
+      acc = __fmul_rn(tri_tap(0, nb0, wt0), row[0]);
       for (int k = 1; k <= h0; k++)
         acc = __fmaf_rn(tri_tap(k, nb0, wt0), __fadd_rn(row[-k], row[k]), acc);
     }
@@ -1031,17 +1073,10 @@ __global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b
     else
       co.cg2v(a, i, acc, ov[0], al, q.iter, ov[1], ov[2], ov[3], ov[4]);
   };
-  auto next_ops = [&]() {
-#pragma unroll
-    for (int k = 0; k < 5; k++) ov[k] = ovn[k];
-  };
-  fetch(0);
-  next_ops();
+  for (int k = 0; k < kSmStages - 1; k++) issue(k);
   if (NB1 > 0) {
     constexpr int H1 = NB1 > 0 ? NB1 - 1 : 0, RING = 2 * H1 + 1;
-    float w1r[H1 + 1];
-#pragma unroll
-    for (int k = 0; k <= H1; k++) w1r[k] = tri_tap(k, NB1, wt1);
+    constexpr int NB1c = NB1 > 0 ? NB1 : 1;
     float rg[RING];
     for (int step0 = 0; step0 < nsteps; step0 += RING) {
 #pragma unroll
@@ -1053,16 +1088,15 @@ __global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b
           rg[u] = axis0(step);
           if (step >= 2 * H1) {
             // centre: ring slot of step - H1
-            float acc = __fmul_rn(w1r[0], rg[(u - H1 + RING) % RING]);
+            float acc = __fmul_rn(tri_tap_c<NB1c>(0), rg[(u - H1 + RING) % RING]);
 #pragma unroll
             for (int k = 1; k <= H1; k++)
-              acc = __fmaf_rn(w1r[k],
+              acc = __fmaf_rn(tri_tap_c<NB1c>(k),
                               __fadd_rn(rg[(u - H1 - k + 2 * RING) % RING],
                                         rg[(u - H1 + k + RING) % RING]),
                               acc);
             out_op(step - 2 * H1, acc);
           }
-          next_ops();
         }
       }
     }
@@ -1086,7 +1120,6 @@ __global__ void __launch_bounds__(kSmThreads) k_smooth12(DipArrays a, DipBatch b
         }
         out_op(step - 2 * h1, acc);
       }
-      next_ops();
       slot = slot == RING - 1 ? 0 : slot + 1;
     }
   }
@@ -1311,7 +1344,8 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   q.wt2 = (float)(1.0 / ((double)q.nb2 * q.nb2));
   const bool ax2 = q.nb2 > 1 && L.any3d;
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
-  const size_t smem = sizeof(float) * (size_t)sm_floats(q.nb0, q.nb1);
+  const bool compiled = (q.nb0 == 10 && q.nb1 == 10) || (q.nb0 == 5 && q.nb1 == 5);
+  const size_t smem = sizeof(float) * (size_t)sm_floats(q.nb0, q.nb1, !compiled);
   const SmKernel k_cg1 = sm_kernel<SM_IN_CG1, SM_OUT_CG1>(q.nb0, q.nb1);
   const SmKernel k_cg2 = sm_kernel<SM_IN_ARR, SM_OUT_CG2>(q.nb0, q.nb1);
   const SmKernel k_in1 = sm_kernel<SM_IN_CG1, SM_OUT_ARR>(q.nb0, q.nb1);

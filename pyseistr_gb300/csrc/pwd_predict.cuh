@@ -347,6 +347,253 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Factor once, apply many times.  The band matrix of a prediction into a
+// trace (regularization + pwd_define of one filter) depends only on the
+// slopes used and the filter orientation, not on the trace predicted, so
+// every chain step of the spray that uses the slopes of trace k with
+// orientation forw shares one LDL' factor.  PredictFactor holds, for one
+// slope trace, its passfilter taps and the factors of both orientations,
+// element (m, i) at (m*n1 + i)*ss (ss = traces sharing the store).
+// ---------------------------------------------------------------------------
+struct PredictFactor {
+  float* taps;  // [NA][n1]  passfilter taps of each sample, unreversed
+  float* f0;    // [NB+1][n1] forw = false: o[0..NB) then d
+  float* f1;    // [NB+1][n1] forw = true
+  long ss;
+};
+
+// Taps and both factors of one slope trace pp (the band and LDL' steps of
+// predict_fwd with one filter, for the two orientations side by side).
+template <int NW>
+__device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
+                               const float* __restrict__ pp, const PredictFactor& F) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  const RegConst rc = reg_const(eps, eps2);
+  FilterWin<NW> wa, wb;  // unreversed / reversed columns
+  float Oa[NB][NB], Da[NB], Ob[NB][NB], Db[NB];
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++)
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      wa.a[cc][j] = 0.f;
+      wb.a[cc][j] = 0.f;
+    }
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    Da[m] = 0.f;
+    Db[m] = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; q++) {
+      Oa[m][q] = 0.f;
+      Ob[m][q] = 0.f;
+    }
+  }
+  auto column = [&](int cn, float* ca, float* cb) {
+    float t[NA];
+    passfilter<NW>(c, pp[cn], t);
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      F.taps[((long)j * n1 + cn) * F.ss] = t[j];
+      ca[j] = t[j];
+      cb[j] = t[NA - 1 - j];
+    }
+  };
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++)
+    if (cc < n1) column(cc, wa.a[NW + 1 + cc], wb.a[NW + 1 + cc]);
+  for (int i = 0; i < n1; i++) {
+    const int cn = i + NW;
+    shift_win<NW>(wa);
+    shift_win<NW>(wb);
+    if (cn < n1) {
+      column(cn, wa.a[2 * NW], wb.a[2 * NW]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < NA; j++) {
+        wa.a[2 * NW][j] = 0.f;
+        wb.a[2 * NW][j] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+      float diag, offd[NB];
+      reg_row<NB>(i, n1, rc, diag, offd);
+      band_add<NW>(side ? wb : wa, i, n1, diag, offd);
+      float dk, ok[NB];
+      ldl_row<NB>(i, n1, diag, offd, side ? Ob : Oa, side ? Db : Da, dk, ok);
+      float* f = side ? F.f1 : F.f0;
+#pragma unroll
+      for (int m = 0; m < NB; m++) f[((long)m * n1 + i) * F.ss] = ok[m];
+      f[((long)NB * n1 + i) * F.ss] = dk;
+      float(&O)[NB][NB] = side ? Ob : Oa;
+      float(&D)[NB] = side ? Db : Da;
+#pragma unroll
+      for (int m = NB - 1; m > 0; m--) {
+        D[m] = D[m - 1];
+#pragma unroll
+        for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
+      }
+      D[0] = dk;
+#pragma unroll
+      for (int q = 0; q < NB; q++) O[0][q] = ok[q];
+    }
+  }
+}
+
+// Forward prediction (predict_step adj=false) of in1 (and, with RHS2, of
+// in1b through the same factor) with a precomputed factor: pwd_set with the
+// stored taps (reversed when forw), the eps2 boundary terms, forward and
+// back substitution.  The operations on the trace are those of predict_fwd.
+// taps/fac point at the slope trace's column 0 with stride F.ss; ys is the
+// chain's scratch (element k at k*yss) for y (and yb).
+template <int NW, bool RHS2>
+__device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps,
+                              const float* __restrict__ fac, long fss, bool forw,
+                              const float* __restrict__ in1, float* __restrict__ out,
+                              float* __restrict__ ys, float* __restrict__ ysb, long yss,
+                              const float* __restrict__ in1b = nullptr,
+                              float* __restrict__ outb = nullptr) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  FilterWin<NW> w1;
+  float x1[NA], xb[NA], t1[NA], tb[NA], Y[NB], YB[NB];
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++) {
+    t1[cc] = 0.f;
+    tb[cc] = 0.f;
+#pragma unroll
+    for (int j = 0; j < NA; j++) w1.a[cc][j] = 0.f;
+  }
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    Y[m] = 0.f;
+    YB[m] = 0.f;
+  }
+  auto load_col = [&](int cn, float* col) {
+    float v[NA];
+#pragma unroll
+    for (int j = 0; j < NA; j++) v[j] = taps[((long)j * n1 + cn) * fss];
+#pragma unroll
+    for (int j = 0; j < NA; j++) col[j] = forw ? v[NA - 1 - j] : v[j];
+  };
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++)
+    if (cc < n1) load_col(cc, w1.a[NW + 1 + cc]);
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    x1[q + 1] = q < n1 ? in1[q] : 0.f;
+    if (RHS2) xb[q + 1] = q < n1 ? in1b[q] : 0.f;
+  }
+  const float b0 = in1[0], b1 = in1[1], b2 = in1[n1 - 2], b3 = in1[n1 - 1];
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+  if (RHS2) {
+    c0 = in1b[0];
+    c1 = in1b[1];
+    c2 = in1b[n1 - 2];
+    c3 = in1b[n1 - 1];
+  }
+  for (int i = 0; i < n1; i++) {
+    const int cn = i + NW;
+    shift_win<NW>(w1);
+#pragma unroll
+    for (int q = 0; q < NA - 1; q++) {
+      x1[q] = x1[q + 1];
+      t1[q] = t1[q + 1];
+      if (RHS2) {
+        xb[q] = xb[q + 1];
+        tb[q] = tb[q + 1];
+      }
+    }
+    const int ln = i + 2 * NW;
+    x1[NA - 1] = ln < n1 ? in1[ln] : 0.f;
+    if (RHS2) xb[NA - 1] = ln < n1 ? in1b[ln] : 0.f;
+    if (cn < n1) {
+      load_col(cn, w1.a[2 * NW]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < NA; j++) w1.a[2 * NW][j] = 0.f;
+    }
+    float s1 = 0.f, sb = 0.f;
+    if (cn >= NW && cn < n1 - NW) {
+#pragma unroll
+      for (int j = 0; j < NA; j++) {
+        s1 = __fadd_rn(s1, __fmul_rn(w1.a[2 * NW][j], x1[j]));
+        if (RHS2) sb = __fadd_rn(sb, __fmul_rn(w1.a[2 * NW][j], xb[j]));
+      }
+    }
+    t1[NA - 1] = s1;
+    if (RHS2) tb[NA - 1] = sb;
+    float o1 = 0.f, ob = 0.f;
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      int k = i + j - NW;
+      if (k >= NW && k < n1 - NW) {
+        o1 = __fadd_rn(o1, __fmul_rn(w1.a[j][j], t1[j]));
+        if (RHS2) ob = __fadd_rn(ob, __fmul_rn(w1.a[j][j], tb[j]));
+      }
+    }
+    float b = o1;
+    if (i == 0) b = __fadd_rn(b, __fmul_rn(eps2, b0));
+    if (i == 1) b = __fadd_rn(b, __fmul_rn(eps2, b1));
+    if (i == n1 - 2) b = __fadd_rn(b, __fmul_rn(eps2, b2));
+    if (i == n1 - 1) b = __fadd_rn(b, __fmul_rn(eps2, b3));
+    if (RHS2) {
+      if (i == 0) ob = __fadd_rn(ob, __fmul_rn(eps2, c0));
+      if (i == 1) ob = __fadd_rn(ob, __fmul_rn(eps2, c1));
+      if (i == n1 - 2) ob = __fadd_rn(ob, __fmul_rn(eps2, c2));
+      if (i == n1 - 1) ob = __fadd_rn(ob, __fmul_rn(eps2, c3));
+    }
+    // forward substitution with o[m][i-1-m] of the stored factor
+    float y = b, y2 = ob;
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < i) {
+        const float om = fac[((long)m * n1 + (i - 1 - m)) * fss];
+        y = __fsub_rn(y, __fmul_rn(om, Y[m]));
+        if (RHS2) y2 = __fsub_rn(y2, __fmul_rn(om, YB[m]));
+      }
+    ys[(long)i * yss] = y;
+    if (RHS2) ysb[(long)i * yss] = y2;
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) {
+      Y[m] = Y[m - 1];
+      if (RHS2) YB[m] = YB[m - 1];
+    }
+    Y[0] = y;
+    if (RHS2) YB[0] = y2;
+  }
+  // back substitution: x[k] = y[k]/d[k] - sum_m o[m][k] x[k+m+1]
+  float X[NB], XB[NB];
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    X[m] = 0.f;
+    XB[m] = 0.f;
+  }
+  for (int k = n1 - 1; k >= 0; k--) {
+    const float dk = fac[((long)NB * n1 + k) * fss];
+    float t = __fdiv_rn(ys[(long)k * yss], dk);
+    float tb2 = RHS2 ? __fdiv_rn(ysb[(long)k * yss], dk) : 0.f;
+#pragma unroll
+    for (int m = 0; m < NB; m++)
+      if (m < n1 - k - 1) {
+        const float om = fac[((long)m * n1 + k) * fss];
+        t = __fsub_rn(t, __fmul_rn(om, X[m]));
+        if (RHS2) tb2 = __fsub_rn(tb2, __fmul_rn(om, XB[m]));
+      }
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) {
+      X[m] = X[m - 1];
+      if (RHS2) XB[m] = XB[m - 1];
+    }
+    X[0] = t;
+    out[k] = t;
+    if (RHS2) {
+      XB[0] = tb2;
+      outb[k] = tb2;
+    }
+  }
+}
+
 // Adjoint prediction in place (predict_step adj=true, sof_cfuns.c:622-649):
 // solve, then the adjoint pwd_set, then the boundary terms.  `tr` is the
 // trace (contiguous), `xs` a per-thread interleaved scratch of n1 floats.

@@ -113,6 +113,97 @@ __global__ void k_spray2_chains(const float* __restrict__ in, const float* __res
   }
 }
 
+// Factor-once form of the forward spray.  The factor store of a section
+// (at scr + sc0) holds, for every trace k, the passfilter taps of its slopes
+// and the LDL' factors of the predictions that use them (forw = false for
+// the chains running towards lower traces, true for the others), each
+// element trace-interleaved; then the chains' y scratch.
+struct FactorLayout {
+  float *taps, *f0, *f1, *y, *yb;
+  long ntr_s;
+};
+template <int NW>
+__device__ __forceinline__ FactorLayout factor_layout(const SprayBufs& bf, const SecDesc& s) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  FactorLayout f;
+  f.ntr_s = (long)s.n2 * s.n3;
+  const long plane = (long)s.n1 * f.ntr_s;
+  f.taps = bf.scr + s.sc0;
+  f.f0 = f.taps + NA * plane;
+  f.f1 = f.f0 + (NB + 1) * plane;
+  f.y = f.f1 + (NB + 1) * plane;
+  f.yb = f.y + 2 * plane;
+  return f;
+}
+
+// Taps and factors of every trace of the batch: thread per trace.
+template <int NW>
+__global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, SprayB b, ApCoef c) {
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= b.ntr) return;
+  long q;
+  const SecDesc& s = trace_section(b, g, q);
+  const FactorLayout f = factor_layout<NW>(bf, s);
+  PredictFactor F{f.taps + q, f.f0 + q, f.f1 + q, f.ntr_s};
+  predict_factor<NW>(s.n1, b.eps, b.eps2, c, dip + s.off + q * s.n1, F);
+}
+
+// Forward spray with the stored factors.  Chains are numbered so that each
+// warp holds 32 consecutive source traces of one direction (coalesced
+// factor and scratch accesses).  MODE as k_spray2_chains.
+template <int NW, int MODE>
+__global__ void k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
+                               SprayBufs bf, SprayB b) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int dir = (int)((t >> 5) & 1);
+  const long g = (t >> 6) * 32 + (t & 31);
+  if (g >= b.ntr) return;
+  long q;
+  const SecDesc& s = trace_section(b, g, q);
+  const int n1 = s.n1, n2 = s.n2;
+  const int i = (int)(q % n2);
+  const long i3 = q / n2;
+  const long n12 = (long)n1 * n2;
+  const long slice_u = s.u0 + i3 * n2 * (long)b.np * n1;
+  float* U = (MODE == 2 ? bf.u1 : bf.u) + slice_u;
+  float* U1 = MODE == 1 ? bf.u1 + slice_u : nullptr;
+  const float* src = MODE == 2 ? ones : in + s.off + i3 * n12 + (long)i * n1;
+  const FactorLayout f = factor_layout<NW>(bf, s);
+  const long cl = dir * f.ntr_s + q, yss = 2 * f.ntr_s;
+  auto slot = [&](float* base, int k, int sl) { return base + ((long)k * b.np + sl) * n1; };
+  const int ns = b.ns;
+  if (dir == 0) {
+    float* cen = slot(U, i, ns);
+    for (int i1 = 0; i1 < n1; i1++) cen[i1] = src[i1];
+    if (MODE == 1) {
+      float* cen1 = slot(U1, i, ns);
+      for (int i1 = 0; i1 < n1; i1++) cen1[i1] = 1.0f;
+    }
+  }
+  const float* prev = src;
+  const float* prevb = ones;
+  for (int is = 0; is < ns; is++) {
+    // dir 0 predicts forward to trace i-is-1 with its own slopes (forw=false);
+    // dir 1 predicts backward to trace i+is+1 with the slopes of ip-1.
+    const int ip = dir == 0 ? i - is - 1 : i + is + 1;
+    if (ip < 0 || ip >= n2) break;
+    const int sl = dir == 0 ? ns - is - 1 : ns + is + 1;
+    const long tk = i3 * n2 + (dir == 0 ? ip : ip - 1);
+    const float* fac = (dir == 0 ? f.f0 : f.f1) + tk;
+    float* out = slot(U, ip, sl);
+    if (MODE == 1) {
+      float* outb = slot(U1, ip, sl);
+      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
+                              f.y + cl, f.yb + cl, yss, prevb, outb);
+      prevb = outb;
+    } else {
+      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
+                               f.y + cl, nullptr, yss);
+    }
+    prev = out;
+  }
+}
+
 // pwsmooth weights w[is] = ns+1-|is-ns| (pwsmooth_init :1055-1058).
 __device__ __forceinline__ float tri_weight(int is, int ns) {
   int a = is - ns;
@@ -267,7 +358,10 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order, bool two_rhs)
     s.u0 = u;
     u += s.n * np;
     s.sc0 = sc;
-    sc += (long)(nb + (two_rhs ? 3 : 2)) * s.n1 * (2L * s.n2 * s.n3);
+    const long plane = (long)s.n1 * s.n2 * s.n3;
+    // per-chain scratch (adjoint mean) or factor store + chain scratch
+    sc += std::max((long)(nb + (two_rhs ? 3 : 2)) * 2 * plane,
+                   (long)(2 * order + 1 + 2 * (nb + 1)) * plane + 4 * plane);
     samp = std::max(samp, s.off + s.n);
     L.n1max = std::max(L.n1max, (long)s.n1);
   }
@@ -325,9 +419,13 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
     return PWD_ECUDA;
   if (w.bf.u1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
     return PWD_ECUDA;
+  const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
+  const unsigned gap = (unsigned)(((L.ntr + 31) / 32 * 64 + bs - 1) / bs);
+  if (filter != kMeanAdj)
+    PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gtr, bs, 0, st>>>(dip, w.bf, b, c));
   if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_chains<NW, 1><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+               k_spray2_apply<NW, 1><<<gap, bs, 0, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
   } else if (filter == kMeanAdj) {
@@ -335,12 +433,11 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                k_spray2_chains<NW, 2><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
-    const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
   } else {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_chains<NW, 0><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+               k_spray2_apply<NW, 0><<<gap, bs, 0, st>>>(data, w.ones, w.bf, b));
     if (option == 1) {
       PWD_KERNEL(PWD_FAM_FILTER, st,
                  k_median_tiles<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
