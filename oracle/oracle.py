@@ -24,6 +24,9 @@ _lib = None
 
 USUM_DOUBLE = 1
 FILTER_REAL = 2
+TRI_CHUNK = 4
+FILTER_FF = 8
+TRI_EXACT = 16  # triangle smoothing in double, rounded once per output
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int

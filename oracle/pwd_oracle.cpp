@@ -41,6 +41,7 @@ enum {
   ORC_FILTER_REAL = 2,   // all-pass filter products in R instead of double
   ORC_TRI_CHUNK = 4,     // triangle running sums as a 32-element chunked scan
   ORC_FILTER_FF = 8,     // filter products in float-float (pair) arithmetic
+  ORC_TRI_EXACT = 16,    // triangle smoothing evaluated in double, rounded once
 };
 
 // Float-float helpers (Dekker / Knuth error-free transformations) used by
@@ -273,7 +274,38 @@ struct Triangle {
     }
   }
   // ps_smooth2 :616-625
+  bool exact = false;  // ORC_TRI_EXACT model (the GPU mixed mode's smoothing)
   void smooth2(long o, long d, R* x) {
+    if (exact) {
+      // the same spread, sums and fold in double, each output rounded once
+      std::vector<double> t(np, 0.0);
+      const double w = 1.0 / ((double)nb * nb);
+      for (int i = 0; i < nx; i++) {
+        const double xi = (double)x[o + i * d];
+        t[i] -= w * xi;
+        t[nb + i] += 2.0 * w * xi;
+        t[2 * nb + i] -= w * xi;
+      }
+      double a = 0;
+      for (int i = 0; i < np; i++) { a += t[i]; t[i] = a; }
+      a = 0;
+      for (int i = np - 1; i >= 0; i--) { a += t[i]; t[i] = a; }
+      std::vector<double> y(nx);
+      for (int i = 0; i < nx; i++) y[i] = t[i + nb];
+      int i, j;
+      for (j = nb + nx; j < np; j += nx) {
+        for (i = 0; i < nx && i < np - j; i++) y[nx - 1 - i] += t[j + i];
+        j += nx;
+        for (i = 0; i < nx && i < np - j; i++) y[i] += t[j + i];
+      }
+      for (j = nb; j >= 0; j -= nx) {
+        for (i = 0; i < nx && i < j; i++) y[i] += t[j - 1 - i];
+        j -= nx;
+        for (i = 0; i < nx && i < j; i++) y[nx - 1 - i] += t[j - 1 - i];
+      }
+      for (i = 0; i < nx; i++) x[o + i * d] = (R)y[i];
+      return;
+    }
     triple2(o, d, x);
     doubint2();
     fold2(o, d, x);
@@ -512,7 +544,10 @@ struct DipState {
     af.init(nw);
     af.real_products = (flags & ORC_FILTER_REAL) != 0;
     af.ff_products = (flags & ORC_FILTER_FF) != 0 && sizeof(R) == 4;
-    for (int i = 0; i < 3; i++) tri.tr[i].chunked = (flags & ORC_TRI_CHUNK) != 0;
+    for (int i = 0; i < 3; i++) {
+      tri.tr[i].chunked = (flags & ORC_TRI_CHUNK) != 0;
+      tri.tr[i].exact = (flags & ORC_TRI_EXACT) != 0;
+    }
     allpass(dip, false, af, nw, n1, n2, n3, u, p, u2.data());
     for (int iter = 0; iter < niter; iter++) {
       allpass(dip, true, af, nw, n1, n2, n3, u, p, u1.data());

@@ -395,6 +395,22 @@ __device__ __forceinline__ bool grid_sum_last(dvec<K> x, double* partials, unsig
 }
 
 // ---------------------------------------------------------------------------
+// 4-byte asynchronous global-to-shared copies (cp.async): a thread stages
+// its own operands a few iterations ahead without holding registers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Workspace carving (256-byte aligned slices of the caller's buffer).
 // ---------------------------------------------------------------------------
 struct Carver {

@@ -737,18 +737,7 @@ __host__ __device__ constexpr int sm_floats(int nb0, int nb1, bool ring) {
          kSmStages * (5 * (kSmB1 + 2 * (nb0 - 1)) + 5 * kSmB1);
 }
 
-// 4-byte asynchronous global-to-shared copies (cp.async, sm_80 and later).
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
+
 enum { SM_IN_ARR = 0, SM_IN_CG1 = 1 };
 enum { SM_OUT_ARR = 0, SM_OUT_CG1 = 1, SM_OUT_CG2 = 2 };
 
@@ -1050,10 +1039,17 @@ __global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBat
     float acc;
     if (NB0 > 0) {
       constexpr int NB0c = NB0 > 0 ? NB0 : 1;
+      // two interleaved accumulators halve the dependent FMA chain
+      float acc2 = 0.f;
       acc = __fmul_rn(tri_tap_c<NB0c>(0), row[0]);
 #pragma unroll
-      for (int k = 1; k < NB0; k++)
-        acc = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc);
+      for (int k = 1; k < NB0; k++) {
+        if (k & 1)
+          acc2 = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc2);
+        else
+          acc = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc);
+      }
+      acc = __fadd_rn(acc, acc2);
     } else {
       acc = __fmul_rn(tri_tap(0, nb0, wt0), row[0]);
       for (int k = 1; k <= h0; k++)
@@ -1088,13 +1084,17 @@ __global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBat
           rg[u] = axis0(step);
           if (step >= 2 * H1) {
             // centre: ring slot of step - H1
-            float acc = __fmul_rn(tri_tap_c<NB1c>(0), rg[(u - H1 + RING) % RING]);
+            float acc = __fmul_rn(tri_tap_c<NB1c>(0), rg[(u - H1 + RING) % RING]), acc2 = 0.f;
 #pragma unroll
-            for (int k = 1; k <= H1; k++)
-              acc = __fmaf_rn(tri_tap_c<NB1c>(k),
-                              __fadd_rn(rg[(u - H1 - k + 2 * RING) % RING],
-                                        rg[(u - H1 + k + RING) % RING]),
-                              acc);
+            for (int k = 1; k <= H1; k++) {
+              const float pr = __fadd_rn(rg[(u - H1 - k + 2 * RING) % RING],
+                                         rg[(u - H1 + k + RING) % RING]);
+              if (k & 1)
+                acc2 = __fmaf_rn(tri_tap_c<NB1c>(k), pr, acc2);
+              else
+                acc = __fmaf_rn(tri_tap_c<NB1c>(k), pr, acc);
+            }
+            acc = __fadd_rn(acc, acc2);
             out_op(step - 2 * H1, acc);
           }
         }

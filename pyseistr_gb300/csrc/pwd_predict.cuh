@@ -445,16 +445,27 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
 // in1b through the same factor) with a precomputed factor: pwd_set with the
 // stored taps (reversed when forw), the eps2 boundary terms, forward and
 // back substitution.  The operations on the trace are those of predict_fwd.
-// taps/fac point at the slope trace's column 0 with stride F.ss; ys is the
-// chain's scratch (element k at k*yss) for y (and yb).
+// taps/fac point at the slope trace's column 0 with stride fss; ys is the
+// chain's scratch (element k at k*yss) for y (and yb).  Every operand of a
+// sample (taps, factor elements, input, y) is staged kApplyStages - 1
+// samples ahead by cp.async into the thread's ring in shared memory: ring
+// element e of slot q at ring[(q*apply_elems(NW) + e)*rs] (rs = threads of the
+// block, so consecutive threads hit consecutive banks).
+constexpr int kApplyStages = 4;
+__host__ __device__ constexpr int apply_elems(int nw) { return 4 * nw + 3; }  // NA + NB + 2
+
 template <int NW, bool RHS2>
 __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps,
                               const float* __restrict__ fac, long fss, bool forw,
                               const float* __restrict__ in1, float* __restrict__ out,
                               float* __restrict__ ys, float* __restrict__ ysb, long yss,
-                              const float* __restrict__ in1b = nullptr,
+                              float* ring, int rs, const float* __restrict__ in1b = nullptr,
                               float* __restrict__ outb = nullptr) {
-  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW, P = kApplyStages, NE = apply_elems(NW);
+  // the input trace (the previous step's output) and, below, the y scratch
+  // were written by this thread's ordinary stores; order them before the
+  // asynchronous copies that read them back
+  __threadfence_block();
   FilterWin<NW> w1;
   float x1[NA], xb[NA], t1[NA], tb[NA], Y[NB], YB[NB];
 #pragma unroll
@@ -469,16 +480,19 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     Y[m] = 0.f;
     YB[m] = 0.f;
   }
-  auto load_col = [&](int cn, float* col) {
-    float v[NA];
-#pragma unroll
-    for (int j = 0; j < NA; j++) v[j] = taps[((long)j * n1 + cn) * fss];
+  auto R = [&](int q, int e) -> float* { return ring + (q * NE + e) * rs; };
+  auto set_col = [&](const float* v, float* col) {
 #pragma unroll
     for (int j = 0; j < NA; j++) col[j] = forw ? v[NA - 1 - j] : v[j];
   };
 #pragma unroll
   for (int cc = 0; cc < NW; cc++)
-    if (cc < n1) load_col(cc, w1.a[NW + 1 + cc]);
+    if (cc < n1) {
+      float v[NA];
+#pragma unroll
+      for (int j = 0; j < NA; j++) v[j] = taps[((long)j * n1 + cc) * fss];
+      set_col(v, w1.a[NW + 1 + cc]);
+    }
 #pragma unroll
   for (int q = 0; q < NB; q++) {
     x1[q + 1] = q < n1 ? in1[q] : 0.f;
@@ -492,23 +506,49 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     c2 = in1b[n1 - 2];
     c3 = in1b[n1 - 1];
   }
+  // forward pass operands of sample i: taps of column i+NW (0..NA), factor
+  // o[m][i-1-m] (NA..NA+NB), inputs in[i+2NW] (NA+NB, +1)
+  auto stage_f = [&](int i) {
+    if (i < n1) {
+      const int q = i % P, cn = i + NW, ln = i + 2 * NW;
+      if (cn < n1)
+#pragma unroll
+        for (int j = 0; j < NA; j++) cp_async4(R(q, j), taps + ((long)j * n1 + cn) * fss);
+#pragma unroll
+      for (int m = 0; m < NB; m++)
+        if (m < i) cp_async4(R(q, NA + m), fac + ((long)m * n1 + (i - 1 - m)) * fss);
+      if (ln < n1) {
+        cp_async4(R(q, NA + NB), in1 + ln);
+        if (RHS2) cp_async4(R(q, NA + NB + 1), in1b + ln);
+      }
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int k = 0; k < P - 1; k++) stage_f(k);
   for (int i = 0; i < n1; i++) {
+    stage_f(i + P - 1);
+    cp_async_wait<P - 1>();
+    const int q = i % P;
     const int cn = i + NW;
     shift_win<NW>(w1);
 #pragma unroll
-    for (int q = 0; q < NA - 1; q++) {
-      x1[q] = x1[q + 1];
-      t1[q] = t1[q + 1];
+    for (int qq = 0; qq < NA - 1; qq++) {
+      x1[qq] = x1[qq + 1];
+      t1[qq] = t1[qq + 1];
       if (RHS2) {
-        xb[q] = xb[q + 1];
-        tb[q] = tb[q + 1];
+        xb[qq] = xb[qq + 1];
+        tb[qq] = tb[qq + 1];
       }
     }
     const int ln = i + 2 * NW;
-    x1[NA - 1] = ln < n1 ? in1[ln] : 0.f;
-    if (RHS2) xb[NA - 1] = ln < n1 ? in1b[ln] : 0.f;
+    x1[NA - 1] = ln < n1 ? *R(q, NA + NB) : 0.f;
+    if (RHS2) xb[NA - 1] = ln < n1 ? *R(q, NA + NB + 1) : 0.f;
     if (cn < n1) {
-      load_col(cn, w1.a[2 * NW]);
+      float v[NA];
+#pragma unroll
+      for (int j = 0; j < NA; j++) v[j] = *R(q, j);
+      set_col(v, w1.a[2 * NW]);
     } else {
 #pragma unroll
       for (int j = 0; j < NA; j++) w1.a[2 * NW][j] = 0.f;
@@ -548,7 +588,7 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
 #pragma unroll
     for (int m = 0; m < NB; m++)
       if (m < i) {
-        const float om = fac[((long)m * n1 + (i - 1 - m)) * fss];
+        const float om = *R(q, NA + m);
         y = __fsub_rn(y, __fmul_rn(om, Y[m]));
         if (RHS2) y2 = __fsub_rn(y2, __fmul_rn(om, YB[m]));
       }
@@ -562,21 +602,42 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     Y[0] = y;
     if (RHS2) YB[0] = y2;
   }
-  // back substitution: x[k] = y[k]/d[k] - sum_m o[m][k] x[k+m+1]
+  cp_async_wait<0>();
+  __threadfence_block();
+  // back substitution: x[k] = y[k]/d[k] - sum_m o[m][k] x[k+m+1]; operands
+  // of row k: o[m][k] (0..NB), d[k] (NB), y[k] (NB+1), yb[k] (NB+2).  The
+  // scratch y written above by this thread is complete (program order).
+  auto stage_b = [&](int step) {
+    if (step < n1) {
+      const int k = n1 - 1 - step, q = step % P;
+#pragma unroll
+      for (int m = 0; m < NB; m++)
+        if (m < n1 - k - 1) cp_async4(R(q, m), fac + ((long)m * n1 + k) * fss);
+      cp_async4(R(q, NB), fac + ((long)NB * n1 + k) * fss);
+      cp_async4(R(q, NB + 1), ys + (long)k * yss);
+      if (RHS2) cp_async4(R(q, NB + 2), ysb + (long)k * yss);
+    }
+    cp_async_commit();
+  };
   float X[NB], XB[NB];
 #pragma unroll
   for (int m = 0; m < NB; m++) {
     X[m] = 0.f;
     XB[m] = 0.f;
   }
-  for (int k = n1 - 1; k >= 0; k--) {
-    const float dk = fac[((long)NB * n1 + k) * fss];
-    float t = __fdiv_rn(ys[(long)k * yss], dk);
-    float tb2 = RHS2 ? __fdiv_rn(ysb[(long)k * yss], dk) : 0.f;
+#pragma unroll
+  for (int k = 0; k < P - 1; k++) stage_b(k);
+  for (int step = 0; step < n1; step++) {
+    stage_b(step + P - 1);
+    cp_async_wait<P - 1>();
+    const int k = n1 - 1 - step, q = step % P;
+    const float dk = *R(q, NB);
+    float t = __fdiv_rn(*R(q, NB + 1), dk);
+    float tb2 = RHS2 ? __fdiv_rn(*R(q, NB + 2), dk) : 0.f;
 #pragma unroll
     for (int m = 0; m < NB; m++)
       if (m < n1 - k - 1) {
-        const float om = fac[((long)m * n1 + k) * fss];
+        const float om = *R(q, m);
         t = __fsub_rn(t, __fmul_rn(om, X[m]));
         if (RHS2) tb2 = __fsub_rn(tb2, __fmul_rn(om, XB[m]));
       }
@@ -592,6 +653,7 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
       outb[k] = tb2;
     }
   }
+  cp_async_wait<0>();
 }
 
 // Adjoint prediction in place (predict_step adj=true, sof_cfuns.c:622-649):

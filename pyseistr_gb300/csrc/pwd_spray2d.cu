@@ -152,8 +152,9 @@ __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, Spr
 // warp holds 32 consecutive source traces of one direction (coalesced
 // factor and scratch accesses).  MODE as k_spray2_chains.
 template <int NW, int MODE>
-__global__ void k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
+__global__ void __launch_bounds__(64, 12) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
                                SprayBufs bf, SprayB b) {
+  extern __shared__ float apply_ring[];  // kApplyStages x apply_elems(NW) per thread
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int dir = (int)((t >> 5) & 1);
   const long g = (t >> 6) * 32 + (t & 31);
@@ -194,11 +195,12 @@ __global__ void k_spray2_apply(const float* __restrict__ in, const float* __rest
     if (MODE == 1) {
       float* outb = slot(U1, ip, sl);
       predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
-                              f.y + cl, f.yb + cl, yss, prevb, outb);
+                              f.y + cl, f.yb + cl, yss, apply_ring + threadIdx.x, blockDim.x,
+                              prevb, outb);
       prevb = outb;
     } else {
       predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
-                               f.y + cl, nullptr, yss);
+                               f.y + cl, nullptr, yss, apply_ring + threadIdx.x, blockDim.x);
     }
     prev = out;
   }
@@ -421,11 +423,12 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
     return PWD_ECUDA;
   const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
   const unsigned gap = (unsigned)(((L.ntr + 31) / 32 * 64 + bs - 1) / bs);
+  const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
   if (filter != kMeanAdj)
     PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gtr, bs, 0, st>>>(dip, w.bf, b, c));
   if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 1><<<gap, bs, 0, st>>>(data, w.ones, w.bf, b));
+               k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
   } else if (filter == kMeanAdj) {
@@ -437,7 +440,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
   } else {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 0><<<gap, bs, 0, st>>>(data, w.ones, w.bf, b));
+               k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     if (option == 1) {
       PWD_KERNEL(PWD_FAM_FILTER, st,
                  k_median_tiles<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
