@@ -446,7 +446,11 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
 // stored taps (reversed when forw), the eps2 boundary terms, forward and
 // back substitution.  The operations on the trace are those of predict_fwd.
 // taps/fac point at the slope trace's column 0 with stride fss; ys is the
-// chain's scratch (element k at k*yss) for y (and yb).  Every operand of a
+// chain's scratch (element k at k*yss) for y (and yb).  The inputs are read
+// with strides ins/insb; the back substitution leaves the predicted trace
+// in ys (ysb) as well as in out (outb), so that the next step of a chain
+// reads its input from the chain-interleaved scratch (coalesced across a
+// warp) rather than from the sprayed panel.  Every operand of a
 // sample (taps, factor elements, input, y) is staged kApplyStages - 1
 // samples ahead by cp.async into the thread's ring in shared memory: ring
 // element e of slot q at ring[(q*apply_elems(NW) + e)*rs] (rs = threads of the
@@ -457,9 +461,9 @@ __host__ __device__ constexpr int apply_elems(int nw) { return 4 * nw + 3; }  //
 template <int NW, bool RHS2>
 __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps,
                               const float* __restrict__ fac, long fss, bool forw,
-                              const float* __restrict__ in1, float* __restrict__ out,
-                              float* __restrict__ ys, float* __restrict__ ysb, long yss,
-                              float* ring, int rs, const float* __restrict__ in1b = nullptr,
+                              const float* in1, long ins, float* __restrict__ out, float* ys,
+                              float* ysb, long yss, float* ring, int rs,
+                              const float* in1b = nullptr, long insb = 1,
                               float* __restrict__ outb = nullptr) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW, P = kApplyStages, NE = apply_elems(NW);
   // the input trace (the previous step's output) and, below, the y scratch
@@ -495,16 +499,16 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     }
 #pragma unroll
   for (int q = 0; q < NB; q++) {
-    x1[q + 1] = q < n1 ? in1[q] : 0.f;
-    if (RHS2) xb[q + 1] = q < n1 ? in1b[q] : 0.f;
+    x1[q + 1] = q < n1 ? in1[q * ins] : 0.f;
+    if (RHS2) xb[q + 1] = q < n1 ? in1b[q * insb] : 0.f;
   }
-  const float b0 = in1[0], b1 = in1[1], b2 = in1[n1 - 2], b3 = in1[n1 - 1];
+  const float b0 = in1[0], b1 = in1[ins], b2 = in1[(n1 - 2) * ins], b3 = in1[(n1 - 1) * ins];
   float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
   if (RHS2) {
     c0 = in1b[0];
-    c1 = in1b[1];
-    c2 = in1b[n1 - 2];
-    c3 = in1b[n1 - 1];
+    c1 = in1b[insb];
+    c2 = in1b[(n1 - 2) * insb];
+    c3 = in1b[(n1 - 1) * insb];
   }
   // forward pass operands of sample i: taps of column i+NW (0..NA), factor
   // o[m][i-1-m] (NA..NA+NB), inputs in[i+2NW] (NA+NB, +1)
@@ -518,8 +522,8 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
       for (int m = 0; m < NB; m++)
         if (m < i) cp_async4(R(q, NA + m), fac + ((long)m * n1 + (i - 1 - m)) * fss);
       if (ln < n1) {
-        cp_async4(R(q, NA + NB), in1 + ln);
-        if (RHS2) cp_async4(R(q, NA + NB + 1), in1b + ln);
+        cp_async4(R(q, NA + NB), in1 + ln * ins);
+        if (RHS2) cp_async4(R(q, NA + NB + 1), in1b + ln * insb);
       }
     }
     cp_async_commit();
@@ -648,9 +652,11 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     }
     X[0] = t;
     out[k] = t;
+    ys[(long)k * yss] = t;  // y[k] is consumed: the slot carries the output
     if (RHS2) {
       XB[0] = tb2;
       outb[k] = tb2;
+      ysb[(long)k * yss] = tb2;
     }
   }
   cp_async_wait<0>();

@@ -152,7 +152,7 @@ __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, Spr
 // warp holds 32 consecutive source traces of one direction (coalesced
 // factor and scratch accesses).  MODE as k_spray2_chains.
 template <int NW, int MODE>
-__global__ void __launch_bounds__(64, 12) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
+__global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
                                SprayBufs bf, SprayB b) {
   extern __shared__ float apply_ring[];  // kApplyStages x apply_elems(NW) per thread
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -181,8 +181,11 @@ __global__ void __launch_bounds__(64, 12) k_spray2_apply(const float* __restrict
       for (int i1 = 0; i1 < n1; i1++) cen1[i1] = 1.0f;
     }
   }
+  // the first step reads the source trace (and the ones); later steps read
+  // the previous prediction from the chain's interleaved scratch
   const float* prev = src;
   const float* prevb = ones;
+  long ps = 1;
   for (int is = 0; is < ns; is++) {
     // dir 0 predicts forward to trace i-is-1 with its own slopes (forw=false);
     // dir 1 predicts backward to trace i+is+1 with the slopes of ip-1.
@@ -194,15 +197,16 @@ __global__ void __launch_bounds__(64, 12) k_spray2_apply(const float* __restrict
     float* out = slot(U, ip, sl);
     if (MODE == 1) {
       float* outb = slot(U1, ip, sl);
-      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
+      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, ps, out,
                               f.y + cl, f.yb + cl, yss, apply_ring + threadIdx.x, blockDim.x,
-                              prevb, outb);
-      prevb = outb;
+                              prevb, ps, outb);
+      prevb = f.yb + cl;
     } else {
-      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, out,
+      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, ps, out,
                                f.y + cl, nullptr, yss, apply_ring + threadIdx.x, blockDim.x);
     }
-    prev = out;
+    prev = f.y + cl;
+    ps = yss;
   }
 }
 
