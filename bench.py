@@ -133,14 +133,26 @@ class DeviceState:
         self.f = torch.empty_like(self.d)
         self.g = torch.empty_like(self.d) if wl.name == "plain2d" else None
         self.D = D
+        self.graph = None
+
+    def capture(self, wl, mixed):
+        """Captures the slope estimation into a CUDA graph on these inputs."""
+        d = wl.dip
+        self.graph = self.D.DipGraph(self.shapes, d["niter"], d["liter"], d["order"], d["rect"],
+                                     mixed=mixed, device=self.d.device)
+        self.graph.data.copy_(self.d)
 
 
 def gpu_step(wl, st, mixed=False):
     D = st.D
     d = wl.dip
     f = wl.filt
-    D.dip_batch(st.d, st.shapes, d["niter"], d["liter"], d["order"], d["rect"], out=st.p,
-                mixed=mixed)
+    if st.graph is not None and bool(st.graph.mixed) == mixed:
+        st.graph()  # replay the captured slope estimation (inputs already in place)
+        st.p.copy_(st.graph.out)
+    else:
+        D.dip_batch(st.d, st.shapes, d["niter"], d["liter"], d["order"], d["rect"], out=st.p,
+                    mixed=mixed)
     if wl.name == "das2d":
         D.sofilter2d_batch(st.d, st.p, st.shapes, f["ns"], f["order"], f["eps"],
                            filter=D.FILTER_MEDIAN, out=st.f)
@@ -416,6 +428,9 @@ def main():
     ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed",
                     help="slope estimation arithmetic: plain (bit-faithful FP32) or mixed "
                          "(FP32 taps, fused convolution smoothing, FP64 reductions)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the slope estimation kernel by kernel instead of replaying "
+                         "its captured CUDA graph")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of single-core CPU work for the cpu_baseline sample")
@@ -445,6 +460,8 @@ def main():
             torch.distributed.barrier()
 
     mixed = args.precision == "mixed"
+    if not args.no_graph:
+        dst.capture(wl, mixed)
     for _ in range(max(3, args.warmup)):
         gpu_step(wl, dst, mixed)
     torch.cuda.synchronize()
@@ -463,6 +480,8 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = _lib.launch_count() - l0
+    if dst.graph is not None:  # replays do not pass through the launch counter
+        launches += dst.graph.launches * args.steps
     barrier()
     ms = ev0.elapsed_time(ev1)
     if world > 1:
@@ -475,10 +494,12 @@ def main():
     # ---- per-family kernel time (CUDA events around each launch) over a
     # repetition of the timed steps ----
     torch.cuda.synchronize()
+    graph, dst.graph = dst.graph, None  # per-launch events need the launches themselves
     with _lib.profile() as prof:
         for _ in range(args.steps):
             gpu_step(wl, dst, mixed)
         torch.cuda.synchronize()
+    dst.graph = graph
     fam_ms = {f: v / args.steps for f, v in prof.ms.items()}
     fam_n = {f: v // args.steps for f, v in prof.launches.items()}
     dom = max(fam_ms, key=lambda f: fam_ms[f])
@@ -551,7 +572,9 @@ def main():
                        else "plain FP32 (bit-faithful to the reference)",
                        l2="inputs larger than L2 (129 MB)" if 4 * wl.samples() > 129e6
                        else "inputs fit in L2; no flush between steps",
-                       parallelism=f"replicas x{world}"),
+                       parallelism=f"replicas x{world}",
+                       slope_launches="replay of the captured CUDA graph" if dst.graph
+                       is not None else "kernel by kernel"),
         "e2e": {"value": e2e, "unit": "samples/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -111,6 +111,22 @@ int pwd_dip_batch(const float *data, const float *mask, float *dip_out,
                   const int rect[3], void *workspace, size_t workspace_bytes,
                   pwd_stream_t stream);
 
+/* pwd_dip_batch / pwd_dip_batch_mixed split in two for CUDA graphs.
+ * pwd_dip_batch_prepare copies the section table into the workspace (a
+ * host-to-device copy on stream; the workspace must be sized for the mode
+ * and mask); pwd_dip_batch_run then enqueues only kernels and memsets, so
+ * a stream capture of it can be replayed for new contents of data (and
+ * mask) at the same addresses.  mixed selects the mixed mode.  No
+ * reference counterpart (the reference has no GPU launch sequence).
+ */
+int pwd_dip_batch_prepare(const pwd_section *sections, int nsec, int order, const int rect[3],
+                          int has_mask, int mixed, void *workspace, size_t workspace_bytes,
+                          pwd_stream_t stream);
+int pwd_dip_batch_run(const float *data, const float *mask, float *dip_out,
+                      const pwd_section *sections, int nsec, int niter, int liter, int order,
+                      const int rect[3], int mixed, void *workspace, size_t workspace_bytes,
+                      pwd_stream_t stream);
+
 /* Mixed mode of pwd_dip_batch (same arguments).  Not bit-faithful: the
  * filter taps are evaluated in FP32, the triangle smoothing of the shaping
  * CG is applied as the equivalent direct convolution (triangle weights

@@ -27,6 +27,8 @@ SIGNATURES = {
     "pwd_dip_batch": ([_P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _S, _P], _I),
     "pwd_dip_batch_mixed_workspace_size": ([_P, _I, _I, _P, _I], _S),
     "pwd_dip_batch_mixed": ([_P, _P, _P, _P, _I, _I, _I, _I, _P, _P, _S, _P], _I),
+    "pwd_dip_batch_prepare": ([_P, _I, _I, _P, _I, _I, _P, _S, _P], _I),
+    "pwd_dip_batch_run": ([_P, _P, _P, _P, _I, _I, _I, _I, _P, _I, _P, _S, _P], _I),
     "pwd_sofilter2d_batch_workspace_size": ([_P, _I, _I, _I, _I, _I, _I], _S),
     "pwd_sofilter2d_batch": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_somean2d_workspace_size": ([_I, _I, _I, _I, _I], _S),

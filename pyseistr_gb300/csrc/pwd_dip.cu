@@ -1535,24 +1535,32 @@ extern "C" size_t pwd_dip_batch_workspace_size(const pwd_section* sections, int 
 
 namespace {
 
+// phase bit 1: upload the section table into the workspace; bit 2: enqueue
+// the estimation (kernels and memsets only, so it can be captured).
+enum { kPrepare = 1, kRun = 2 };
+
 int dip_batch_common(const float* data, const float* mask, float* dip_out,
                      const pwd_section* sections, int nsec, int niter, int liter, int order,
                      const int rect[3], void* workspace, size_t workspace_bytes,
-                     pwd_stream_t stream, bool mixed) {
+                     pwd_stream_t stream, bool mixed, int phase = kPrepare | kRun,
+                     bool has_mask = false) {
   int rc = check_dip_args(niter, liter, order, rect);
   if (rc != PWD_OK) return rc;
-  if (!data || !dip_out) return PWD_EINVAL;
+  if ((phase & kRun) && (!data || !dip_out)) return PWD_EINVAL;
+  if (phase & kRun) has_mask = mask != nullptr;
   std::vector<SecDesc> secs;
   if ((rc = batch_table(sections, nsec, order, secs)) != PWD_OK) return rc;
   DipLayout L = layout(secs, rect);
   size_t need = 0;
-  carve_dip(nullptr, L, nsec, mask != nullptr, &need, mixed);
+  carve_dip(nullptr, L, nsec, has_mask, &need, mixed);
   if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  DipWork w = carve_dip(workspace, L, nsec, mask != nullptr, &need, mixed);
+  DipWork w = carve_dip(workspace, L, nsec, has_mask, &need, mixed);
   cudaStream_t st = (cudaStream_t)stream;
-  if (cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
-      cudaSuccess)
+  if ((phase & kPrepare) &&
+      cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
+          cudaSuccess)
     return PWD_ECUDA;
+  if (!(phase & kRun)) return PWD_OK;
   return dip_enqueue(data, mask, dip_out, L, w, nsec, niter, liter, order, rect, st, mixed);
 }
 
@@ -1564,6 +1572,22 @@ extern "C" int pwd_dip_batch(const float* data, const float* mask, float* dip_ou
                              size_t workspace_bytes, pwd_stream_t stream) {
   return dip_batch_common(data, mask, dip_out, sections, nsec, niter, liter, order, rect,
                           workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int pwd_dip_batch_prepare(const pwd_section* sections, int nsec, int order,
+                                     const int rect[3], int has_mask, int mixed,
+                                     void* workspace, size_t workspace_bytes,
+                                     pwd_stream_t stream) {
+  return dip_batch_common(nullptr, nullptr, nullptr, sections, nsec, 0, 0, order, rect, workspace,
+                          workspace_bytes, stream, mixed != 0, kPrepare, has_mask != 0);
+}
+
+extern "C" int pwd_dip_batch_run(const float* data, const float* mask, float* dip_out,
+                                 const pwd_section* sections, int nsec, int niter, int liter,
+                                 int order, const int rect[3], int mixed, void* workspace,
+                                 size_t workspace_bytes, pwd_stream_t stream) {
+  return dip_batch_common(data, mask, dip_out, sections, nsec, niter, liter, order, rect,
+                          workspace, workspace_bytes, stream, mixed != 0, kRun);
 }
 
 extern "C" size_t pwd_dip_batch_mixed_workspace_size(const pwd_section* sections, int nsec,

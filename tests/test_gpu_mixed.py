@@ -198,3 +198,23 @@ def test_das_full_record_mixed_vs_fp64_and_plain_vs_reference(D):
     assert rel_l2(mixed, g["f64"]) <= 1e-5
     assert rel_l2(plain, g["f64"]) <= 2 * ref_err
     assert rel_l2(plain, g["ref32"]) <= 2 * ref_err
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_dip_graph_replay_equals_direct_call(D, mixed):
+    """The captured launch sequence replayed on new data gives the direct
+    call's slopes bit for bit (plain and mixed), twice in a row."""
+    import torch
+    import workloads
+
+    secs = [s[: max(64, s.shape[0] // 4), : max(20, s.shape[1] // 5)].copy()
+            for s in workloads.batch2d(seed=21, count=4)]
+    shapes = [s.shape for s in secs]
+    flat = [np.concatenate([s.reshape(-1, order="F") for s in secs]).astype(np.float32)]
+    flat.append((flat[0][::-1] * 0.5).copy())
+    g = D.DipGraph(shapes, 3, 6, 2, (10, 10, 1), mixed=mixed)
+    for f in flat:
+        t = torch.from_numpy(f).cuda()
+        want = D.dip_batch(t, shapes, 3, 6, 2, (10, 10, 1), mixed=mixed).cpu().numpy()
+        got = g(t).cpu().numpy()
+        assert np.array_equal(got, want)
