@@ -107,7 +107,53 @@ class Plain2D(Workload):
                             "somf2d (ns 8, order 2, eps 0.01)", "samples_per_step": self.samples()}
 
 
-WORKLOADS = {"batch2d": Batch2D, "das2d": Das2D, "plain2d": Plain2D}
+class Plain3D(Workload):
+    name = "plain3d"
+    dip = dict(niter=5, liter=10, order=2, rect=(5, 5, 5))
+    filt = dict(r1=4, r2=4, order=2, eps=0.01)
+
+    def __init__(self, seed):
+        self.sections = [W.plain3d(seed=seed)]
+
+    def samples(self):
+        return int(self.sections[0].size)
+
+    def config(self):
+        return {"workload": "plain3d: 201 x 60 x 60 cube; dip3d(5,10,order 2,rect 5,5,5) + "
+                            "somean3d + somf3d (r1 = r2 = 4, order 2)",
+                "samples_per_step": self.samples()}
+
+    def cpu_sample(self, budget_s):
+        c = self.sections[0]
+        k = max(4, min(c.shape[2], int(budget_s * 0.02e6 / (c.shape[0] * c.shape[1]))))
+        return [np.ascontiguousarray(c[:, :, :k])], f"sub-cube {c.shape[0]} x {c.shape[1]} x {k}"
+
+
+class Patches3D(Workload):
+    name = "patches3d"
+    dip = dict(niter=5, liter=10, order=2, rect=(5, 5, 5))
+    filt = dict(order=2, niter=20)
+
+    def __init__(self, seed, count=64):
+        pairs = W.patches3d(seed=seed, count=count)
+        self.sections = [d for d, _ in pairs]
+        self.masks = [m for _, m in pairs]
+
+    def samples(self):
+        return int(sum(s.size for s in self.sections))
+
+    def config(self):
+        return {"workload": f"patches3d: {len(self.sections)} cubes n1~U[128,512], "
+                            "n2=n3~U[32,96], 50 % of traces masked; dip3d(5,10,order 2,"
+                            "rect 5,5,5) on all cubes in one batch + soint3d(order 2, niter 20)",
+                "sections": len(self.sections), "samples_per_step": self.samples()}
+
+    def cpu_sample(self, budget_s):
+        return [(self.sections[0], self.masks[0])], "the first patch"
+
+
+WORKLOADS = {"batch2d": Batch2D, "das2d": Das2D, "plain2d": Plain2D, "plain3d": Plain3D,
+             "patches3d": Patches3D}
 
 
 def make_workload(args, rank=0):
@@ -129,9 +175,14 @@ class DeviceState:
         self.shapes = [s.shape for s in wl.sections]
         flat = np.concatenate([s.reshape(-1, order="F") for s in wl.sections])
         self.d = torch.from_numpy(flat).to(dev)
-        self.p = torch.empty_like(self.d)
+        _, _, nout = D.section_table(self.shapes)
+        self.p = torch.empty(nout, dtype=torch.float32, device=dev)
         self.f = torch.empty_like(self.d)
-        self.g = torch.empty_like(self.d) if wl.name == "plain2d" else None
+        self.g = torch.empty_like(self.d) if wl.name in ("plain2d", "plain3d") else None
+        if wl.name == "patches3d":  # interpolation inputs: masked data and the mask
+            m = np.concatenate([x.reshape(-1, order="F") for x in wl.masks])
+            self.m = torch.from_numpy(m).to(dev)
+            self.dm = self.d * self.m
         self.D = D
         self.graph = None
 
@@ -153,7 +204,23 @@ def gpu_step(wl, st, mixed=False):
     else:
         D.dip_batch(st.d, st.shapes, d["niter"], d["liter"], d["order"], d["rect"], out=st.p,
                     mixed=mixed)
-    if wl.name == "das2d":
+    if wl.name == "plain3d":
+        n1, n2, n3 = st.shapes[0]
+        n = n1 * n2 * n3
+        pi, px = st.p[:n], st.p[n:]
+        D.somean3d(st.d, pi, px, n1, n2, n3, f["r1"], f["r2"], f["order"], f["eps"], out=st.f)
+        D.somf3d(st.d, pi, px, n1, n2, n3, f["r1"], f["r2"], 2 * f["r1"] * f["r2"] + 1, 1,
+                 f["order"], f["eps"], out=st.g)
+    elif wl.name == "patches3d":
+        off = po = 0
+        for n1, n2, n3 in st.shapes:
+            n = n1 * n2 * n3
+            D.soint3d(st.dm[off:off + n], st.m[off:off + n], st.p[po:po + n],
+                      st.p[po + n:po + 2 * n], n1, n2, n3, order=f["order"], niter=f["niter"],
+                      out=st.f[off:off + n])
+            off += n
+            po += 2 * n
+    elif wl.name == "das2d":
         D.sofilter2d_batch(st.d, st.p, st.shapes, f["ns"], f["order"], f["eps"],
                            filter=D.FILTER_MEDIAN, out=st.f)
     else:
@@ -172,6 +239,19 @@ def api_step(wl, mixed=False):
     d = wl.dip
     f = wl.filt
     nbytes = sum(s.nbytes for s in wl.sections)
+    if wl.name == "plain3d":
+        c = wl.sections[0]
+        pi, px = ps.dip3dc(c, d["niter"], d["liter"], d["order"], eps_dv=0.01, eps_cg=1,
+                           tol_cg=1e-6, rect=list(d["rect"]))
+        ps.somean3dc(c, pi, px, f["r1"], f["r2"], f["eps"], f["order"])
+        ps.somf3dc(c, pi, px, f["r1"], f["r2"], f["eps"], f["order"])
+        return 7 * nbytes, 4 * nbytes
+    if wl.name == "patches3d":
+        for c, m in zip(wl.sections, wl.masks):
+            pi, px = ps.dip3dc(c, d["niter"], d["liter"], d["order"], eps_dv=0.01, eps_cg=1,
+                               tol_cg=1e-6, rect=list(d["rect"]))
+            ps.soint3dc(c * m, m, pi, px, order=f["order"], niter=f["niter"])
+        return 5 * nbytes, 3 * nbytes
     p, out = ps.dip_somean2d_batch(wl.sections, niter=d["niter"], liter=d["liter"],
                                    order=d["order"], rect=list(d["rect"]), ns=f["ns"],
                                    eps=f["eps"], median=(wl.name == "das2d"), mixed=mixed)
@@ -304,6 +384,18 @@ def cpu_section(args):
     wl = WORKLOADS[wl_name]
     d = wl.dip
     f = wl.filt
+    if wl_name in ("plain3d", "patches3d"):  # the port (float oracle)
+        from oracle import oracle as O
+
+        if wl_name == "plain3d":
+            pi, px = O.dip3d(sec, d["niter"], d["liter"], d["order"], d["rect"])
+            O.somean3d(sec, pi, px, f["r1"], f["r2"], f["order"])
+            O.somf3d(sec, pi, px, f["r1"], f["r2"], f["order"])
+            return sec.size
+        c, m = sec
+        pi, px = O.dip3d(c, d["niter"], d["liter"], d["order"], d["rect"])
+        O.soint3d(c * m, m, pi, px, order=f["order"], niter=f["niter"])
+        return c.size
     n1, n2 = sec.shape
     if kind == "reference":
         path = os.path.join(ROOT, "oracle", "_ref")
@@ -346,6 +438,8 @@ def cpu_section(args):
 
 def cpu_sample(wl, budget_s):
     """Sections of the workload whose CPU processing fits about budget_s."""
+    if hasattr(wl, "cpu_sample"):
+        return wl.cpu_sample(budget_s)
     secs = wl.sections
     if len(secs) == 1:
         return secs, "the whole workload"
@@ -388,7 +482,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     wl = make_workload(args)
-    kind = _ref_modules() or "port"
+    kind = (None if wl.name in ("plain3d", "patches3d") else _ref_modules()) or "port"
     workers = os.cpu_count() or 1
     sample, desc = cpu_sample(wl, budget_s=6.0 * workers)
     for _ in range(args.warmup):
@@ -587,7 +681,7 @@ def main():
     if plain is not None:
         line["plain_fp32"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        kind = _ref_modules() or "port"
+        kind = (None if wl.name in ("plain3d", "patches3d") else _ref_modules()) or "port"
         sample, desc = cpu_sample(wl, args.cpu_budget)
         n, t = time_cpu(wl, sample, kind, 1)
         line["cpu_baseline"] = {"value": n / t, "unit": "samples/s", "cores": 1, "kind": kind,
