@@ -159,6 +159,8 @@ WORKLOADS = {"batch2d": Batch2D, "das2d": Das2D, "plain2d": Plain2D, "plain3d": 
 def make_workload(args, rank=0):
     if args.workload == "batch2d":
         return Batch2D(seed=args.seed + rank, count=args.sections)
+    if args.workload == "patches3d":
+        return Patches3D(seed=args.seed + rank, count=min(args.sections, 64))
     return WORKLOADS[args.workload](seed=args.seed + rank)
 
 
@@ -212,14 +214,8 @@ def gpu_step(wl, st, mixed=False):
         D.somf3d(st.d, pi, px, n1, n2, n3, f["r1"], f["r2"], 2 * f["r1"] * f["r2"] + 1, 1,
                  f["order"], f["eps"], out=st.g)
     elif wl.name == "patches3d":
-        off = po = 0
-        for n1, n2, n3 in st.shapes:
-            n = n1 * n2 * n3
-            D.soint3d(st.dm[off:off + n], st.m[off:off + n], st.p[po:po + n],
-                      st.p[po + n:po + 2 * n], n1, n2, n3, order=f["order"], niter=f["niter"],
-                      out=st.f[off:off + n])
-            off += n
-            po += 2 * n
+        D.soint3d_batch(st.dm, st.m, st.p, st.shapes, order=f["order"], niter=f["niter"],
+                        out=st.f)
     elif wl.name == "das2d":
         D.sofilter2d_batch(st.d, st.p, st.shapes, f["ns"], f["order"], f["eps"],
                            filter=D.FILTER_MEDIAN, out=st.f)
@@ -518,7 +514,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch2d")
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
-                    help="sections of the batch2d workload (smaller counts for profiler captures)")
+                    help="sections of the batch2d workload, patches of patches3d (at most 64); "
+                         "smaller counts for profiler captures")
     ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed",
                     help="slope estimation arithmetic: plain (bit-faithful FP32) or mixed "
                          "(FP32 taps, fused convolution smoothing, FP64 reductions)")

@@ -227,6 +227,19 @@ int pwd_soint3d(const float *data, const float *mask, const float *dip_inline,
                 int nj2, int niter, int drift, int seed, int hasmask, float var,
                 void *workspace, size_t workspace_bytes, pwd_stream_t stream);
 
+/* Many patches of uneven size in one launch sequence (the batched
+ * interpolation workflow): a loop of csoint3d calls over patches without
+ * noise (var = 0).  sections[k].offset places patch k in data, mask and
+ * out; sections[k].out_offset places its slopes in dips as pwd_dip_batch
+ * writes them (inline n, then crossline n), so the two calls chain.  Every
+ * patch gets the results of its own pwd_soint3d call.
+ */
+size_t pwd_soint3d_batch_workspace_size(const pwd_section *sections, int nsec, int order);
+int pwd_soint3d_batch(const float *data, const float *mask, const float *dips, float *out,
+                      const pwd_section *sections, int nsec, int order, int nj1, int nj2,
+                      int niter, int drift, int hasmask, void *workspace,
+                      size_t workspace_bytes, pwd_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Launch accounting and kernel timing (no counterpart in the reference,
  * which has no GPU code).  Kernel families:

@@ -10,88 +10,183 @@
 #include <cmath>
 #include <vector>
 
+#include "pwd_batch.cuh"
 #include "pwd_common.cuh"
 
 namespace pwd {
 namespace {
 
+// Geometry of one patch (section) of the batch.
 struct Op3 {
   int nx, ny, nz, nw, nj1, nj2;
   long n;
   int drift;
 };
 
-struct Coef3 {
-  float* f1;    // [na][n] part-1 (inline) taps, 0 where the row is skipped
-  float* f2;    // [na][n] part-2 (crossline) taps
-  int* id1;     // drift shifts (0 without drift)
-  int* id2;
-  uint8_t* v1;  // row valid flags
-  uint8_t* v2;
+// Per-section solver state.
+struct SolveScalars {
+  double rr0, gsum, g0;
+  float alfa, beta;
+  int done, skip, dmax;
+  unsigned cnt[4];
 };
+
+constexpr int kTile = 8192;  // model samples per tile; tiles never straddle patches
+constexpr int kTileThreads = 256;
+
+// The batch: patches packed in data/mask/out at SecDesc::off (n each) and
+// their slopes at SecDesc::pout (inline n, then crossline n, the layout of
+// pwd_dip_batch's output).  Data-space vectors (2n per patch) live at 2*off,
+// filter taps ([na][n] per part) at na*off.
+struct SoBatch {
+  const SecDesc* secs;
+  const int* tile_sec;
+  int nsec, ntiles, nw, nj1, nj2, drift, hasmask;
+  int xl_after;  // crossline slopes at pp + pout + n (batch layout) instead of qq + pout
+  SolveScalars* S;
+  double* partials;  // [ntiles][6]
+};
+
+struct SoArrays {
+  const float *data, *mask, *pp, *qq, *dd;
+  float *x, *g, *S, *rr, *gg, *Ss, *f1, *f2;
+  int *id1, *id2;
+  uint8_t *v1, *v2, *known;
+};
+
+struct TileRange {
+  int sec;
+  long lo, hi;
+};
+__device__ __forceinline__ TileRange tile_range(const SoBatch& b, int t) {
+  TileRange r;
+  r.sec = b.tile_sec[t];
+  const SecDesc& s = b.secs[r.sec];
+  r.lo = (long)(t - s.tile0) * kTile;
+  r.hi = min(s.n, r.lo + kTile);
+  return r;
+}
+
+__device__ __forceinline__ Op3 geometry(const SoBatch& b, const SecDesc& s) {
+  Op3 g;
+  g.nx = s.n1;
+  g.ny = s.n2;
+  g.nz = s.n3;
+  g.nw = b.nw;
+  g.nj1 = b.nj1;
+  g.nj2 = b.nj2;
+  g.n = s.n;
+  g.drift = b.drift;
+  return g;
+}
+
+// Sum of K doubles over the tiles of one section; true in the block of the
+// section's last tile to finish, which receives the totals.
+template <int K>
+__device__ __forceinline__ bool so_sum_last(dvec<K> x, const SoBatch& b, int t, const SecDesc& s,
+                                            unsigned* counter, dvec<K>& tot) {
+  __shared__ bool s_last;
+  dvec<K> blk = block_sum<K>(x);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) b.partials[(size_t)t * 6 + k] = blk.v[k];
+    __threadfence();
+    unsigned tk = atomicAdd(counter, 1u);
+    s_last = (tk == (unsigned)(s.ntile - 1));
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  dvec<K> y;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < s.ntile; i += blockDim.x)
+      v += __ldcg(b.partials + (size_t)(s.tile0 + i) * 6 + k);
+    y.v[k] = v;
+  }
+  tot = block_sum<K>(y);
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
 
 __device__ __forceinline__ int ps_nint(float x) {
   return (int)(x > 0.0 ? (double)x + 0.5 : (double)x - 0.5);
 }
 
+// allpass3_init's filters (soint3d_cfuns.c:625-660): taps, drift shifts and
+// row validity of both parts, once per call.
 template <int NW>
-__global__ void k_ap3_coef(const float* __restrict__ pp, const float* __restrict__ qq, Op3 g,
-                           ApCoef c, Coef3 cf) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= g.n) return;
-  const int ix = (int)(i % g.nx);
-  const long r = i / g.nx;
-  const int iy = (int)(r % g.ny), iz = (int)(r / g.ny);
-  for (int part = 0; part < 2; part++) {
-    const float* p = part == 0 ? pp : qq;
-    const int nj = part == 0 ? g.nj1 : g.nj2;
-    bool ok = ix >= NW * nj && ix < g.nx - NW * nj && (part == 0 ? iy < g.ny - 1 : iz < g.nz - 1);
-    int id = 0;
-    float pi = p[i];
-    if (ok && g.drift) {
-      // a shift of a trace length or more (or a non-finite slope) always
-      // fails the reference's range test; test it before converting
-      if (!(fabsf(p[i]) < (float)g.nx)) {
-        ok = false;
-      } else {
-        id = ps_nint(p[i]);
-        if (ix - NW * nj - id < 0 || ix + NW * nj - id >= g.nx) ok = false;
-        pi = __fsub_rn(p[i], (float)id);
+__global__ void k_ap3_coef(SoArrays A, SoBatch b, ApCoef c) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const Op3 g = geometry(b, s);
+  constexpr int NA = 2 * NW + 1;
+  const float* pp = A.pp + s.pout;
+  const float* qq = b.xl_after ? pp + s.n : A.qq + s.pout;
+  float *f1 = A.f1 + NA * s.off, *f2 = A.f2 + NA * s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    const int ix = (int)(i % g.nx);
+    const long r = i / g.nx;
+    const int iy = (int)(r % g.ny), iz = (int)(r / g.ny);
+    for (int part = 0; part < 2; part++) {
+      const float* p = part == 0 ? pp : qq;
+      const int nj = part == 0 ? g.nj1 : g.nj2;
+      bool ok = ix >= NW * nj && ix < g.nx - NW * nj && (part == 0 ? iy < g.ny - 1 : iz < g.nz - 1);
+      int id = 0;
+      float pi = p[i];
+      if (ok && g.drift) {
+        // a shift of a trace length or more (or a non-finite slope) always
+        // fails the reference's range test; test it before converting
+        if (!(fabsf(p[i]) < (float)g.nx)) {
+          ok = false;
+        } else {
+          id = ps_nint(p[i]);
+          if (ix - NW * nj - id < 0 || ix + NW * nj - id >= g.nx) ok = false;
+          pi = __fsub_rn(p[i], (float)id);
+        }
+        if (!ok) id = 0;
       }
-      if (!ok) id = 0;
+      float f[NA];
+      if (ok) passfilter<NW>(c, pi, f);
+      float* dst = part == 0 ? f1 : f2;
+      for (int iw = 0; iw < NA; iw++) dst[iw * g.n + i] = ok ? f[iw] : 0.f;
+      (part == 0 ? A.id1 : A.id2)[s.off + i] = id;
+      (part == 0 ? A.v1 : A.v2)[s.off + i] = ok;
     }
-    float f[2 * NW + 1];
-    if (ok) passfilter<NW>(c, pi, f);
-    float* dst = part == 0 ? cf.f1 : cf.f2;
-    for (int iw = 0; iw <= 2 * NW; iw++) dst[iw * g.n + i] = ok ? f[iw] : 0.f;
-    (part == 0 ? cf.id1 : cf.id2)[i] = id;
-    (part == 0 ? cf.v1 : cf.v2)[i] = ok;
   }
 }
 
-// yy (+)= L xx, yy = [inline residual ; crossline residual].
+// yy (+)= L xx, yy = [inline residual ; crossline residual] (allpass3_lop
+// forward, :662-695).
 template <int NW>
-__global__ void k_ap3_fwd(const float* __restrict__ xx, float* __restrict__ yy, Op3 g, Coef3 cf,
-                          int add, const int* done) {
-  if (done && *done) return;
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= g.n) return;
-  for (int part = 0; part < 2; part++) {
-    float* y = yy + (part == 0 ? 0 : g.n);
-    float acc = add ? y[i] : 0.f;
-    const uint8_t ok = (part == 0 ? cf.v1 : cf.v2)[i];
-    if (ok) {
-      const long st = part == 0 ? g.nx : (long)g.nx * g.ny;
-      const int nj = part == 0 ? g.nj1 : g.nj2;
-      const int id = (part == 0 ? cf.id1 : cf.id2)[i];
-      const float* f = part == 0 ? cf.f1 : cf.f2;
+__global__ void k_ap3_fwd(const float* __restrict__ xxb, float* __restrict__ yyb, SoArrays A,
+                          SoBatch b, int add, int use_done) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  if (use_done && b.S[tr.sec].done) return;
+  const Op3 g = geometry(b, s);
+  constexpr int NA = 2 * NW + 1;
+  const float* xx = xxb + s.off;
+  float* yy = yyb + 2 * s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    for (int part = 0; part < 2; part++) {
+      float* y = yy + (part == 0 ? 0 : g.n);
+      float acc = add ? y[i] : 0.f;
+      const uint8_t ok = (part == 0 ? A.v1 : A.v2)[s.off + i];
+      if (ok) {
+        const long st = part == 0 ? g.nx : (long)g.nx * g.ny;
+        const int nj = part == 0 ? g.nj1 : g.nj2;
+        const int id = (part == 0 ? A.id1 : A.id2)[s.off + i];
+        const float* f = (part == 0 ? A.f1 : A.f2) + NA * s.off;
 #pragma unroll
-      for (int iw = 0; iw <= 2 * NW; iw++) {
-        int is = (iw - NW) * nj;
-        acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(xx[i + st + is], xx[i - is - id]), f[iw * g.n + i]));
+        for (int iw = 0; iw < NA; iw++) {
+          int is = (iw - NW) * nj;
+          acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(xx[i + st + is], xx[i - is - id]), f[iw * g.n + i]));
+        }
       }
+      y[i] = acc;
     }
-    y[i] = acc;
   }
 }
 
@@ -148,68 +243,70 @@ __device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, long 
   return acc;
 }
 
+// g = L' rr with the known samples zeroed (ps_solver :1058-1070) and
+// gsum = g.g per patch.
 template <int NW>
-__global__ void k_ap3_adj(float* __restrict__ xx, const float* __restrict__ yy, Op3 g, Coef3 cf,
-                          const uint8_t* __restrict__ known, const int* dmax, const int* done,
-                          double* partials, unsigned* counter, double* out_sum) {
-  if (done && *done) return;
+__global__ void k_ap3_adj(SoArrays A, SoBatch b) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  SolveScalars* S = b.S + tr.sec;
+  if (S->done) return;
+  const Op3 g = geometry(b, s);
+  constexpr int NA = 2 * NW + 1;
+  const int dm = g.drift ? S->dmax : 0;
+  const float* yy = A.rr + 2 * s.off;
+  const float *f1 = A.f1 + NA * s.off, *f2 = A.f2 + NA * s.off;
   dvec<1> acc = {{0.0}};
-  const int dm = g.drift ? *dmax : 0;
-  for (long m = blockIdx.x * (long)blockDim.x + threadIdx.x; m < g.n;
-       m += (long)gridDim.x * blockDim.x) {
+  for (long m = tr.lo + threadIdx.x; m < tr.hi; m += blockDim.x) {
     float a = 0.f;
-    a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, cf.f1, cf.id1, cf.v1, g.n, g.drift, dm, a);
-    a = ap3_adj_part<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, cf.f2, cf.id2, cf.v2, g.n,
-                         g.drift, dm, a);
-    if (known && known[m]) a = 0.f;
-    xx[m] = a;
+    a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, f1, A.id1 + s.off, A.v1 + s.off, g.n, g.drift, dm, a);
+    a = ap3_adj_part<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.id2 + s.off,
+                         A.v2 + s.off, g.n, g.drift, dm, a);
+    if (A.known[s.off + m]) a = 0.f;
+    A.g[s.off + m] = a;
     acc.v[0] += (double)a * (double)a;
   }
-  if (partials) {
-    dvec<1> tot;
-    if (grid_sum_last<1>(acc, partials, counter, tot) && threadIdx.x == 0) *out_sum = tot.v[0];
-  }
+  dvec<1> tot;
+  if (so_sum_last<1>(acc, b, t, s, &S->cnt[0], tot) && threadIdx.x == 0) S->gsum = tot.v[0];
 }
 
-__global__ void k_max_shift(const int* __restrict__ id1, const int* __restrict__ id2, long n,
-                            int* dmax) {
+__global__ void k_max_shift(SoArrays A, SoBatch b) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
   int best = 0;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
-       i += (long)gridDim.x * blockDim.x) {
-    best = max(best, abs(id1[i]));
-    best = max(best, abs(id2[i]));
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    best = max(best, abs(A.id1[s.off + i]));
+    best = max(best, abs(A.id2[s.off + i]));
   }
-  atomicMax(dmax, best);
+  atomicMax(&b.S[tr.sec].dmax, best);
 }
 
-struct SolveScalars {
-  double rr0, gsum, g0;
-  double dots[6];  // gg.gg, Ss.Ss, gg.Ss, gg.rr, Ss.rr, rr.rr
-  float alfa, beta;
-  int done, skip, dmax;
-  unsigned cnt[4];
-};
-
-// gg.gg, Ss.Ss, gg.Ss, gg.rr, Ss.rr, rr.rr over the 2n data space; the last
-// block runs the tolerance test of ps_solver (:1086-1100) and ps_cgstep's
-// scalar part (:835-866).
-__global__ void k_cg3_dots(const float* __restrict__ gg, const float* __restrict__ Ss,
-                           const float* __restrict__ rr, long ny, int iter, SolveScalars* S,
-                           double* partials) {
+// gg.gg, Ss.Ss, gg.Ss, gg.rr, Ss.rr, rr.rr over the patch's 2n data space;
+// the last tile runs the tolerance test of ps_solver (:1086-1100) and
+// ps_cgstep's scalar part (:835-866).
+__global__ void k_cg3_dots(SoArrays A, SoBatch b, int iter) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  SolveScalars* S = b.S + tr.sec;
   if (S->done) return;
   dvec<6> acc = {{0, 0, 0, 0, 0, 0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ny;
-       i += (long)gridDim.x * blockDim.x) {
-    double a = gg[i], s = Ss[i], r = rr[i];
-    acc.v[0] += a * a;
-    acc.v[1] += s * s;
-    acc.v[2] += a * s;
-    acc.v[3] += a * r;
-    acc.v[4] += s * r;
-    acc.v[5] += r * r;
-  }
-  dvec<6> t;
-  if (!(grid_sum_last<6>(acc, partials, &S->cnt[1], t) && threadIdx.x == 0)) return;
+  const float *gg = A.gg + 2 * s.off, *Ss = A.Ss + 2 * s.off, *rr = A.rr + 2 * s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
+#pragma unroll
+    for (int part = 0; part < 2; part++) {
+      const long k = i + part * s.n;
+      double a = gg[k], sv = Ss[k], r = rr[k];
+      acc.v[0] += a * a;
+      acc.v[1] += sv * sv;
+      acc.v[2] += a * sv;
+      acc.v[3] += a * r;
+      acc.v[4] += sv * r;
+      acc.v[5] += r * r;
+    }
+  dvec<6> tt;
+  if (!(so_sum_last<6>(acc, b, t, s, &S->cnt[1], tt) && threadIdx.x == 0)) return;
   const float TOL = 1.e-12f, EPS = 1.e-12f;
   float dpr, dpg;
   if (iter == 0) {
@@ -217,7 +314,7 @@ __global__ void k_cg3_dots(const float* __restrict__ gg, const float* __restrict
     dpr = 1.f;
     dpg = 1.f;
   } else {
-    dpr = __fdiv_rn((float)t.v[5], (float)S->rr0);
+    dpr = __fdiv_rn((float)tt.v[5], (float)S->rr0);
     dpg = __fdiv_rn((float)S->gsum, (float)S->g0);
   }
   if (dpr < TOL || dpg < TOL) {
@@ -228,14 +325,14 @@ __global__ void k_cg3_dots(const float* __restrict__ gg, const float* __restrict
   S->skip = 0;
   if (iter == 0) {  // the first step of a run restarts (forget)
     beta = 0.0;
-    alfa = t.v[0];
+    alfa = tt.v[0];
     if (alfa <= 0.) {
       S->skip = 1;
       return;
     }
-    alfa = -t.v[3] / alfa;
+    alfa = -tt.v[3] / alfa;
   } else {
-    double gdg = t.v[0], sds = t.v[1], gds = t.v[2];
+    double gdg = tt.v[0], sds = tt.v[1], gds = tt.v[2];
     if (gdg == 0. || sds == 0.) {
       S->skip = 1;
       return;
@@ -245,7 +342,7 @@ __global__ void k_cg3_dots(const float* __restrict__ gg, const float* __restrict
       determ *= gdg * sds;
     else
       determ = gdg * sds * (double)EPS;
-    double gdr = -t.v[3], sdr = -t.v[4];
+    double gdr = -tt.v[3], sdr = -tt.v[4];
     alfa = (sds * gdr - gds * sdr) / determ;
     beta = (-gds * gdr + gdg * sdr) / determ;
   }
@@ -253,76 +350,125 @@ __global__ void k_cg3_dots(const float* __restrict__ gg, const float* __restrict
   S->beta = __double2float_rn(beta);
 }
 
-__global__ void k_cg3_update(float* __restrict__ x, float* __restrict__ S_, const float* __restrict__ g,
-                             float* __restrict__ rr, float* __restrict__ Ss,
-                             const float* __restrict__ gg, long nx, int iter, SolveScalars* S) {
+// ps_cgstep's vector part (:867-877).
+__global__ void k_cg3_update(SoArrays A, SoBatch b, int iter) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const SolveScalars* S = b.S + tr.sec;
   if (S->done || S->skip) return;
-  const float a = S->alfa, b = S->beta;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < 2 * nx;
-       i += (long)gridDim.x * blockDim.x) {
-    if (i < nx) {
-      float s = iter == 0 ? 0.f : S_[i];
-      s = __fadd_rn(__fmul_rn(s, b), __fmul_rn(a, g[i]));
-      S_[i] = s;
-      x[i] = __fadd_rn(x[i], s);
+  const float al = S->alfa, be = S->beta;
+  float *x = A.x + s.off, *Sv = A.S + s.off, *rr = A.rr + 2 * s.off, *Ss = A.Ss + 2 * s.off;
+  const float *g = A.g + s.off, *gg = A.gg + 2 * s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    float sv = iter == 0 ? 0.f : Sv[i];
+    sv = __fadd_rn(__fmul_rn(sv, be), __fmul_rn(al, g[i]));
+    Sv[i] = sv;
+    x[i] = __fadd_rn(x[i], sv);
+#pragma unroll
+    for (int part = 0; part < 2; part++) {
+      const long k = i + part * s.n;
+      float s2 = iter == 0 ? 0.f : Ss[k];
+      s2 = __fadd_rn(__fmul_rn(s2, be), __fmul_rn(al, gg[k]));
+      Ss[k] = s2;
+      rr[k] = __fadd_rn(rr[k], s2);
     }
-    float s2 = iter == 0 ? 0.f : Ss[i];
-    s2 = __fadd_rn(__fmul_rn(s2, b), __fmul_rn(a, gg[i]));
-    Ss[i] = s2;
-    rr[i] = __fadd_rn(rr[i], s2);
   }
 }
 
-// rr = -dd; dd = a*randn (zero without noise)
-__global__ void k_init_rr(float* __restrict__ rr, const float* __restrict__ dd, long ny) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < ny) rr[i] = dd ? -dd[i] : -0.0f;
+// x = data, known = mask != 0 (or data != 0), rr = -dd (-0 without noise),
+// S = Ss = 0 (ps_cgstep's restart, :838-839).
+__global__ void k_init(SoArrays A, SoBatch b) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    const long m = s.off + i;
+    const float di = A.data[m];
+    A.x[m] = di;
+    A.known[m] = b.hasmask == 1 ? (A.mask[m] != 0.f) : (di != 0.f);
+    A.S[m] = 0.f;
+#pragma unroll
+    for (int part = 0; part < 2; part++) {
+      const long k = 2 * s.off + i + part * s.n;
+      A.rr[k] = A.dd ? -A.dd[k] : -0.0f;
+      A.Ss[k] = 0.f;
+    }
+  }
 }
 
-__global__ void k_init_x(const float* __restrict__ din, const float* __restrict__ mask,
-                         float* __restrict__ x, uint8_t* __restrict__ known, long n, int hasmask) {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  x[i] = din[i];
-  known[i] = hasmask == 1 ? (mask[i] != 0.f) : (din[i] != 0.f);
-}
-
-__global__ void k_rr0(const float* __restrict__ rr, long ny, SolveScalars* S, double* partials) {
+// rr0 = rr.rr per patch.
+__global__ void k_rr0(SoArrays A, SoBatch b) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
+  const SecDesc& s = b.secs[tr.sec];
+  SolveScalars* S = b.S + tr.sec;
   dvec<1> acc = {{0.0}};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ny;
-       i += (long)gridDim.x * blockDim.x)
-    acc.v[0] += (double)rr[i] * (double)rr[i];
-  dvec<1> t;
-  if (grid_sum_last<1>(acc, partials, &S->cnt[2], t) && threadIdx.x == 0) S->rr0 = t.v[0];
+  const float* rr = A.rr + 2 * s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
+#pragma unroll
+    for (int part = 0; part < 2; part++) {
+      const double r = rr[i + part * s.n];
+      acc.v[0] += r * r;
+    }
+  dvec<1> tot;
+  if (so_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0) S->rr0 = tot.v[0];
 }
 
-struct Soint3Work {
-  float *g, *rr, *gg, *S, *Ss, *dd, *f1, *f2;
-  int *id1, *id2;
-  uint8_t *v1, *v2, *known;
-  SolveScalars* sc;
-  double* partials;
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsec) return;
+  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
+}
+
+struct SoLayout {
+  long ntot;  // model samples spanned (data, mask, out)
+  int ntiles;
 };
 
-Soint3Work carve_soint3(void* ws, long n, int order, bool noise, size_t* total) {
+SoLayout so_layout(std::vector<SecDesc>& secs) {
+  SoLayout L{};
+  int tiles = 0;
+  for (auto& s : secs) {
+    s.n = (long)s.n1 * s.n2 * s.n3;
+    s.tile0 = tiles;
+    s.ntile = (int)((s.n + kTile - 1) / kTile);
+    tiles += s.ntile;
+    L.ntot = std::max(L.ntot, s.off + s.n);
+  }
+  L.ntiles = tiles;
+  return L;
+}
+
+struct SoWork {
+  SoArrays a;
+  SecDesc* secs;
+  int* tile_sec;
+  SolveScalars* S;
+  double* partials;
+  float* dd;
+};
+
+SoWork carve_soint3(void* ws, const SoLayout& L, int nsec, int order, bool noise, size_t* total) {
   const int na = 2 * order + 1;
+  const long n = L.ntot;
   Carver cv(ws);
-  Soint3Work w;
-  w.g = cv.take<float>(n);
-  w.rr = cv.take<float>(2 * n);
-  w.gg = cv.take<float>(2 * n);
-  w.S = cv.take<float>(n);
-  w.Ss = cv.take<float>(2 * n);
+  SoWork w{};
+  w.a.g = cv.take<float>(n);
+  w.a.rr = cv.take<float>(2 * n);
+  w.a.gg = cv.take<float>(2 * n);
+  w.a.S = cv.take<float>(n);
+  w.a.Ss = cv.take<float>(2 * n);
   w.dd = noise ? cv.take<float>(2 * n) : nullptr;
-  w.f1 = cv.take<float>(na * n);
-  w.f2 = cv.take<float>(na * n);
-  w.id1 = cv.take<int>(n);
-  w.id2 = cv.take<int>(n);
-  w.v1 = cv.take<uint8_t>(n);
-  w.v2 = cv.take<uint8_t>(n);
-  w.known = cv.take<uint8_t>(n);
-  w.sc = cv.take<SolveScalars>(1);
-  w.partials = cv.take<double>(6 * (size_t)kRedGridMax);
+  w.a.f1 = cv.take<float>(na * n);
+  w.a.f2 = cv.take<float>(na * n);
+  w.a.id1 = cv.take<int>(n);
+  w.a.id2 = cv.take<int>(n);
+  w.a.v1 = cv.take<uint8_t>(n);
+  w.a.v2 = cv.take<uint8_t>(n);
+  w.a.known = cv.take<uint8_t>(n);
+  w.secs = cv.take<SecDesc>(nsec);
+  w.tile_sec = cv.take<int>(L.ntiles);
+  w.S = cv.take<SolveScalars>(nsec);
+  w.partials = cv.take<double>((size_t)L.ntiles * 6);
   *total = cv.size();
   return w;
 }
@@ -391,40 +537,79 @@ void make_noise(std::vector<float>& dd, int seed, float var) {
 }
 
 template <int NW>
-int soint3_run(const float* data, const float* mask, const float* pp, const float* qq, float* x,
-               Op3 g, int niter, int seed, int hasmask, float var, const Soint3Work& w,
-               cudaStream_t st) {
-  const long n = g.n, ny = 2 * n;
-  const int b = 256;
-  const unsigned gn = (unsigned)((n + b - 1) / b), g2 = (unsigned)((ny + b - 1) / b);
-  const int gr = red_grid(n), gr2 = red_grid(ny);
-  Coef3 cf{w.f1, w.f2, w.id1, w.id2, w.v1, w.v2};
-  if (cudaMemsetAsync(w.sc, 0, sizeof(SolveScalars), st) != cudaSuccess) return PWD_ECUDA;
-  // ps_cgstep's restart zeroes the step vectors (:838-839)
-  if (cudaMemsetAsync(w.S, 0, sizeof(float) * n, st) != cudaSuccess) return PWD_ECUDA;
-  if (cudaMemsetAsync(w.Ss, 0, sizeof(float) * ny, st) != cudaSuccess) return PWD_ECUDA;
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_coef<NW><<<gn, b, 0, st>>>(pp, qq, g, make_apcoef(NW), cf));
-  if (g.drift) PWD_KERNEL(PWD_FAM_SOINT, st, k_max_shift<<<gr, kRedBlock, 0, st>>>(w.id1, w.id2, n, &w.sc->dmax));
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_init_x<<<gn, b, 0, st>>>(data, mask, x, w.known, n, hasmask));
-  if (var != 0.f) {
-    std::vector<float> dd((size_t)ny);
-    make_noise(dd, seed, var);
-    if (cudaMemcpyAsync(w.dd, dd.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
-      return PWD_ECUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return PWD_ECUDA;
-  }
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_init_rr<<<g2, b, 0, st>>>(w.rr, var != 0.f ? w.dd : nullptr, ny));
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gn, b, 0, st>>>(x, w.rr, g, cf, 1, nullptr));
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_rr0<<<gr2, kRedBlock, 0, st>>>(w.rr, ny, w.sc, w.partials));
+int soint3_run(const SoArrays& A, const SoBatch& b, int niter, cudaStream_t st) {
+  const unsigned gt = (unsigned)b.ntiles;
+  const int bs = kTileThreads;
+  PWD_KERNEL(PWD_FAM_OTHER, st,
+             k_tile_map<<<(b.nsec + 127) / 128, 128, 0, st>>>(b.secs, b.nsec,
+                                                              const_cast<int*>(b.tile_sec)));
+  if (cudaMemsetAsync(b.S, 0, sizeof(SolveScalars) * b.nsec, st) != cudaSuccess) return PWD_ECUDA;
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_coef<NW><<<gt, bs, 0, st>>>(A, b, make_apcoef(NW)));
+  if (b.drift) PWD_KERNEL(PWD_FAM_SOINT, st, k_max_shift<<<gt, bs, 0, st>>>(A, b));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_init<<<gt, bs, 0, st>>>(A, b));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.x, A.rr, A, b, 1, 0));
+  PWD_KERNEL(PWD_FAM_SOINT, st, k_rr0<<<gt, bs, 0, st>>>(A, b));
   for (int iter = 0; iter < niter; iter++) {
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_adj<NW><<<gr, kRedBlock, 0, st>>>(w.g, w.rr, g, cf, w.known, &w.sc->dmax, &w.sc->done,
-                                            w.partials, &w.sc->cnt[0], &w.sc->gsum));
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gn, b, 0, st>>>(w.g, w.gg, g, cf, 0, &w.sc->done));
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_dots<<<gr2, kRedBlock, 0, st>>>(w.gg, w.Ss, w.rr, ny, iter, w.sc, w.partials));
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_update<<<g2, b, 0, st>>>(x, w.S, w.g, w.rr, w.Ss, w.gg, n, iter, w.sc));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_adj<NW><<<gt, bs, 0, st>>>(A, b));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.g, A.gg, A, b, 0, 1));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_dots<<<gt, bs, 0, st>>>(A, b, iter));
+    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_update<<<gt, bs, 0, st>>>(A, b, iter));
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
+}
+
+int soint3_dispatch(int order, const SoArrays& A, const SoBatch& b, int niter, cudaStream_t st) {
+  switch (order) {
+    case 1: return soint3_run<1>(A, b, niter, st);
+    case 2: return soint3_run<2>(A, b, niter, st);
+    case 3: return soint3_run<3>(A, b, niter, st);
+    case 4: return soint3_run<4>(A, b, niter, st);
+  }
+  return PWD_ENOTSUP;
+}
+
+// Validates and completes the section table of a batch.
+int so_table(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
+  if (!in || nsec < 1) return PWD_EINVAL;
+  secs.assign(nsec, SecDesc{});
+  for (int i = 0; i < nsec; i++) {
+    if (in[i].n1 < 1 || in[i].n2 < 1 || in[i].n3 < 1 || in[i].offset < 0 || in[i].out_offset < 0 ||
+        (long)in[i].n1 * in[i].n2 * in[i].n3 >= (1L << 31))
+      return PWD_EINVAL;
+    secs[i].off = in[i].offset;
+    secs[i].pout = in[i].out_offset;
+    secs[i].n1 = in[i].n1;
+    secs[i].n2 = in[i].n2;
+    secs[i].n3 = in[i].n3;
+  }
+  return PWD_OK;
+}
+
+// Runs a batch: table on the device, noise (single patch only) uploaded.
+int so_enqueue(const std::vector<SecDesc>& secs, const SoLayout& L, SoWork& w, const float* data,
+               const float* mask, const float* pp, const float* qq, float* out, int order,
+               int nj1, int nj2, int niter, int drift, int hasmask, int xl_after,
+               const std::vector<float>* noise, cudaStream_t st) {
+  const int nsec = (int)secs.size();
+  if (cudaMemcpyAsync(w.secs, secs.data(), sizeof(SecDesc) * nsec, cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return PWD_ECUDA;
+  if (noise) {
+    if (cudaMemcpyAsync(w.dd, noise->data(), sizeof(float) * noise->size(),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return PWD_ECUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PWD_ECUDA;  // noise is a local buffer
+  }
+  SoArrays A = w.a;
+  A.data = data;
+  A.mask = mask;
+  A.pp = pp;
+  A.qq = qq;
+  A.dd = noise ? w.dd : nullptr;
+  A.x = out;
+  SoBatch b{w.secs, w.tile_sec, nsec, L.ntiles, order, nj1, nj2, drift != 0, hasmask, xl_after,
+            w.S, w.partials};
+  return soint3_dispatch(order, A, b, niter, st);
 }
 
 }  // namespace
@@ -434,8 +619,13 @@ using namespace pwd;
 
 extern "C" size_t pwd_soint3d_workspace_size(int n1, int n2, int n3, int order) {
   if (n1 < 1 || n2 < 1 || n3 < 1 || order < 1 || order > PWD_MAX_ORDER) return 0;
+  std::vector<SecDesc> secs(1, SecDesc{});
+  secs[0].n1 = n1;
+  secs[0].n2 = n2;
+  secs[0].n3 = n3;
+  SoLayout L = so_layout(secs);
   size_t t = 0;
-  carve_soint3(nullptr, (long)n1 * n2 * n3, order, true, &t);
+  carve_soint3(nullptr, L, 1, order, true, &t);
   return t;
 }
 
@@ -449,20 +639,50 @@ extern "C" int pwd_soint3d(const float* data, const float* mask, const float* di
     return PWD_EINVAL;
   if (hasmask == 1 && !mask) return PWD_EINVAL;
   if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
-  const long n = (long)n1 * n2 * n3;
+  if ((long)n1 * n2 * n3 >= (1L << 31)) return PWD_EINVAL;
+  std::vector<SecDesc> secs(1, SecDesc{});
+  secs[0].n1 = n1;
+  secs[0].n2 = n2;
+  secs[0].n3 = n3;
+  SoLayout L = so_layout(secs);
   size_t need = 0;
-  carve_soint3(nullptr, n, order, true, &need);
+  carve_soint3(nullptr, L, 1, order, true, &need);
   if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
-  Soint3Work w = carve_soint3(workspace, n, order, true, &need);
-  Op3 g;
-  g.nx = n1; g.ny = n2; g.nz = n3; g.nw = order; g.nj1 = nj1; g.nj2 = nj2; g.n = n;
-  g.drift = drift != 0;
-  cudaStream_t st = (cudaStream_t)stream;
-  switch (order) {
-    case 1: return soint3_run<1>(data, mask, dip_inline, dip_xline, out, g, niter, seed, hasmask, var, w, st);
-    case 2: return soint3_run<2>(data, mask, dip_inline, dip_xline, out, g, niter, seed, hasmask, var, w, st);
-    case 3: return soint3_run<3>(data, mask, dip_inline, dip_xline, out, g, niter, seed, hasmask, var, w, st);
-    case 4: return soint3_run<4>(data, mask, dip_inline, dip_xline, out, g, niter, seed, hasmask, var, w, st);
+  SoWork w = carve_soint3(workspace, L, 1, order, true, &need);
+  std::vector<float> dd;
+  if (var != 0.f) {
+    dd.resize(2 * (size_t)L.ntot);
+    make_noise(dd, seed, var);
   }
-  return PWD_ENOTSUP;
+  return so_enqueue(secs, L, w, data, mask, dip_inline, dip_xline, out, order, nj1, nj2, niter,
+                    drift, hasmask, 0, var != 0.f ? &dd : nullptr, (cudaStream_t)stream);
+}
+
+extern "C" size_t pwd_soint3d_batch_workspace_size(const pwd_section* sections, int nsec,
+                                                   int order) {
+  std::vector<SecDesc> secs;
+  if (order < 1 || order > PWD_MAX_ORDER || so_table(sections, nsec, secs) != PWD_OK) return 0;
+  SoLayout L = so_layout(secs);
+  size_t t = 0;
+  carve_soint3(nullptr, L, nsec, order, false, &t);
+  return t;
+}
+
+extern "C" int pwd_soint3d_batch(const float* data, const float* mask, const float* dips,
+                                 float* out, const pwd_section* sections, int nsec, int order,
+                                 int nj1, int nj2, int niter, int drift, int hasmask,
+                                 void* workspace, size_t workspace_bytes, pwd_stream_t stream) {
+  if (!data || !dips || !out || order < 1 || nj1 < 1 || nj2 < 1 || niter < 0) return PWD_EINVAL;
+  if (hasmask == 1 && !mask) return PWD_EINVAL;
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  std::vector<SecDesc> secs;
+  int rc = so_table(sections, nsec, secs);
+  if (rc != PWD_OK) return rc;
+  SoLayout L = so_layout(secs);
+  size_t need = 0;
+  carve_soint3(nullptr, L, nsec, order, false, &need);
+  if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
+  SoWork w = carve_soint3(workspace, L, nsec, order, false, &need);
+  return so_enqueue(secs, L, w, data, mask, dips, nullptr, out, order, nj1, nj2, niter, drift,
+                    hasmask, 1, nullptr, (cudaStream_t)stream);
 }

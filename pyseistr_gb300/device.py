@@ -246,6 +246,24 @@ class DipGraph:
         return self.out
 
 
+def soint3d_batch(data, mask, dips, shapes, order=1, niter=100, nj1=1, nj2=1, drift=0,
+                  hasmask=1, out=None, workspace=None):
+    """Interpolation of many cubes packed one after another in `data` and
+    `mask`, with their slopes `dips` as dip_batch returns them."""
+    L = _lib.load()
+    tab, ntot, nout = section_table(shapes)
+    data = _as_flat(data, ntot, "data")
+    mask = _as_flat(mask, ntot, "mask") if mask is not None else None
+    dips = _as_flat(dips, nout, "dips")
+    ws = _workspace(L.pwd_soint3d_batch_workspace_size(tab, len(shapes), order), data.device,
+                    workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_soint3d_batch(_ptr(data), _ptr(mask), _ptr(dips), _ptr(out), tab, len(shapes),
+                                   order, nj1, nj2, niter, int(drift), int(hasmask), _ptr(ws),
+                                   ws.numel(), _stream()), "soint3d_batch")
+    return out
+
+
 FILTER_MEAN, FILTER_MEAN_ADJ, FILTER_MEDIAN = 1, 2, 3
 
 
