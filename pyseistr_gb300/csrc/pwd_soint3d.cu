@@ -243,10 +243,33 @@ __device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, long 
   return acc;
 }
 
+// The same without drift: every "+" row (m - st - is) precedes every "-"
+// row (m + is), because a valid row has st > 2 NW nj, so the scatter order
+// is the "+" terms with iw descending, then the "-" terms with iw ascending.
+template <int NW>
+__device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ y, long m,
+                                                      long st, int nj,
+                                                      const float* __restrict__ f,
+                                                      const uint8_t* __restrict__ v, long n,
+                                                      float acc) {
+  constexpr int NA = 2 * NW + 1;
+#pragma unroll
+  for (int iw = NA - 1; iw >= 0; iw--) {
+    const long i = m - st - (long)(iw - NW) * nj;
+    if (i >= 0 && i < n && v[i]) acc = __fadd_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
+  }
+#pragma unroll
+  for (int iw = 0; iw < NA; iw++) {
+    const long i = m + (long)(iw - NW) * nj;
+    if (i >= 0 && i < n && v[i]) acc = __fsub_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
+  }
+  return acc;
+}
+
 // g = L' rr with the known samples zeroed (ps_solver :1058-1070) and
 // gsum = g.g per patch.
-template <int NW>
-__global__ void k_ap3_adj(SoArrays A, SoBatch b) {
+template <int NW, bool DRIFT>
+__global__ void __launch_bounds__(kTileThreads, 4) k_ap3_adj(SoArrays A, SoBatch b) {
   const int t = blockIdx.x;
   const TileRange tr = tile_range(b, t);
   const SecDesc& s = b.secs[tr.sec];
@@ -257,16 +280,23 @@ __global__ void k_ap3_adj(SoArrays A, SoBatch b) {
   const int dm = g.drift ? S->dmax : 0;
   const float* yy = A.rr + 2 * s.off;
   const float *f1 = A.f1 + NA * s.off, *f2 = A.f2 + NA * s.off;
-  dvec<1> acc = {{0.0}};
+  ffacc a0;
   for (long m = tr.lo + threadIdx.x; m < tr.hi; m += blockDim.x) {
     float a = 0.f;
-    a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, f1, A.id1 + s.off, A.v1 + s.off, g.n, g.drift, dm, a);
-    a = ap3_adj_part<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.id2 + s.off,
-                         A.v2 + s.off, g.n, g.drift, dm, a);
+    if (DRIFT) {
+      a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, f1, A.id1 + s.off, A.v1 + s.off, g.n, 1, dm, a);
+      a = ap3_adj_part<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.id2 + s.off,
+                           A.v2 + s.off, g.n, 1, dm, a);
+    } else {
+      a = ap3_adj_part_nodrift<NW>(yy, m, g.nx, g.nj1, f1, A.v1 + s.off, g.n, a);
+      a = ap3_adj_part_nodrift<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.v2 + s.off,
+                                   g.n, a);
+    }
     if (A.known[s.off + m]) a = 0.f;
     A.g[s.off + m] = a;
-    acc.v[0] += (double)a * (double)a;
+    a0.add_prod(a, a);
   }
+  dvec<1> acc = {{a0.value()}};
   dvec<1> tot;
   if (so_sum_last<1>(acc, b, t, s, &S->cnt[0], tot) && threadIdx.x == 0) S->gsum = tot.v[0];
 }
@@ -291,20 +321,23 @@ __global__ void k_cg3_dots(SoArrays A, SoBatch b, int iter) {
   const SecDesc& s = b.secs[tr.sec];
   SolveScalars* S = b.S + tr.sec;
   if (S->done) return;
-  dvec<6> acc = {{0, 0, 0, 0, 0, 0}};
+  // float-float per-thread accumulation (exact products, ~2^-45 sums),
+  // double across threads and tiles: no per-sample FP64 arithmetic
+  ffacc c0, c1, c2, c3, c4, c5;
   const float *gg = A.gg + 2 * s.off, *Ss = A.Ss + 2 * s.off, *rr = A.rr + 2 * s.off;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
 #pragma unroll
     for (int part = 0; part < 2; part++) {
       const long k = i + part * s.n;
-      double a = gg[k], sv = Ss[k], r = rr[k];
-      acc.v[0] += a * a;
-      acc.v[1] += sv * sv;
-      acc.v[2] += a * sv;
-      acc.v[3] += a * r;
-      acc.v[4] += sv * r;
-      acc.v[5] += r * r;
+      const float a = gg[k], sv = Ss[k], r = rr[k];
+      c0.add_prod(a, a);
+      c1.add_prod(sv, sv);
+      c2.add_prod(a, sv);
+      c3.add_prod(a, r);
+      c4.add_prod(sv, r);
+      c5.add_prod(r, r);
     }
+  dvec<6> acc = {{c0.value(), c1.value(), c2.value(), c3.value(), c4.value(), c5.value()}};
   dvec<6> tt;
   if (!(so_sum_last<6>(acc, b, t, s, &S->cnt[1], tt) && threadIdx.x == 0)) return;
   const float TOL = 1.e-12f, EPS = 1.e-12f;
@@ -401,14 +434,15 @@ __global__ void k_rr0(SoArrays A, SoBatch b) {
   const TileRange tr = tile_range(b, t);
   const SecDesc& s = b.secs[tr.sec];
   SolveScalars* S = b.S + tr.sec;
-  dvec<1> acc = {{0.0}};
+  ffacc c0;
   const float* rr = A.rr + 2 * s.off;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
 #pragma unroll
     for (int part = 0; part < 2; part++) {
-      const double r = rr[i + part * s.n];
-      acc.v[0] += r * r;
+      const float r = rr[i + part * s.n];
+      c0.add_prod(r, r);
     }
+  dvec<1> acc = {{c0.value()}};
   dvec<1> tot;
   if (so_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0) S->rr0 = tot.v[0];
 }
@@ -550,7 +584,10 @@ int soint3_run(const SoArrays& A, const SoBatch& b, int niter, cudaStream_t st) 
   PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.x, A.rr, A, b, 1, 0));
   PWD_KERNEL(PWD_FAM_SOINT, st, k_rr0<<<gt, bs, 0, st>>>(A, b));
   for (int iter = 0; iter < niter; iter++) {
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_adj<NW><<<gt, bs, 0, st>>>(A, b));
+    if (b.drift)
+      PWD_KERNEL(PWD_FAM_SOINT, st, (k_ap3_adj<NW, true><<<gt, bs, 0, st>>>(A, b)));
+    else
+      PWD_KERNEL(PWD_FAM_SOINT, st, (k_ap3_adj<NW, false><<<gt, bs, 0, st>>>(A, b)));
     PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.g, A.gg, A, b, 0, 1));
     PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_dots<<<gt, bs, 0, st>>>(A, b, iter));
     PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_update<<<gt, bs, 0, st>>>(A, b, iter));
