@@ -218,6 +218,28 @@ def _unpack(t, shapes):
     return out
 
 
+def dip_somean2d_packed(data, shapes, niter=5, liter=10, order=2, rect=[10, 10, 1], ns=6,
+                        eps=0.01, median=False, mixed=False, out=None):
+    """dip_somean2d_batch on sections already packed one after another in a
+    flat float32 tensor (each section column-major): a CPU tensor, pinned
+    for full-speed copies, or a CUDA tensor.  Returns (slopes, filtered) as
+    flat CPU tensors (pinned), or fills `out` = (slopes, filtered) when
+    given.  One host-to-device copy in, two device-to-host copies out."""
+    if not isinstance(data, torch.Tensor) or data.dtype != torch.float32 or data.dim() != 1:
+        raise TypeError("data must be a flat float32 tensor")
+    d = data if data.is_cuda else data.to(_dev(), non_blocking=True)
+    p = D.dip_batch(d, shapes, niter, liter, order, rect, mixed=mixed)
+    f = D.sofilter2d_batch(d, p, shapes, ns, order, eps,
+                           filter=D.FILTER_MEDIAN if median else D.FILTER_MEAN)
+    if out is None:
+        out = (torch.empty(p.shape, dtype=torch.float32, pin_memory=True),
+               torch.empty(f.shape, dtype=torch.float32, pin_memory=True))
+    out[0].copy_(p, non_blocking=True)
+    out[1].copy_(f, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return out
+
+
 def dip2dc_batch(sections, niter=5, liter=20, order=2, rect=[10, 10, 1], mixed=False):
     """dip2dc over a list of 2-D sections, all in one launch sequence;
     returns the list of slopes (each equal to dip2dc of its section, or its

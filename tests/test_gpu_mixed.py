@@ -218,3 +218,24 @@ def test_dip_graph_replay_equals_direct_call(D, mixed):
         want = D.dip_batch(t, shapes, 3, 6, 2, (10, 10, 1), mixed=mixed).cpu().numpy()
         got = g(t).cpu().numpy()
         assert np.array_equal(got, want)
+
+
+def test_packed_host_api_equals_list_api(D):
+    """dip_somean2d_packed on a pinned packed tensor returns the list API's
+    slopes and filtered sections."""
+    import torch
+    import workloads
+    import pyseistr_gb300 as ps
+
+    secs = [s[: max(64, s.shape[0] // 4), : max(20, s.shape[1] // 5)].copy()
+            for s in workloads.batch2d(seed=17, count=3)]
+    shapes = [s.shape for s in secs]
+    packed = torch.from_numpy(np.concatenate([s.reshape(-1, order="F") for s in secs])).pin_memory()
+    for median in (False, True):
+        p, f = ps.dip_somean2d_packed(packed, shapes, 3, 6, 2, [10, 10, 1], ns=4, median=median)
+        pl, fl = ps.dip_somean2d_batch(secs, 3, 6, 2, [10, 10, 1], ns=4, median=median)
+        k = 0
+        for s, a, b in zip(secs, pl, fl):
+            assert np.array_equal(p[k:k + s.size].numpy().reshape(s.shape, order="F"), a)
+            assert np.array_equal(f[k:k + s.size].numpy().reshape(s.shape, order="F"), b)
+            k += s.size
