@@ -252,11 +252,11 @@ def api_step(wl, mixed=False, host=None):
         ps.somf3dc(c, pi, px, f["r1"], f["r2"], f["eps"], f["order"])
         return 7 * nbytes, 4 * nbytes
     if wl.name == "patches3d":
-        for c, m in zip(wl.sections, wl.masks):
-            pi, px = ps.dip3dc(c, d["niter"], d["liter"], d["order"], eps_dv=0.01, eps_cg=1,
-                               tol_cg=1e-6, rect=list(d["rect"]))
-            ps.soint3dc(c * m, m, pi, px, order=f["order"], niter=f["niter"])
-        return 5 * nbytes, 3 * nbytes
+        (data, mask), out = host
+        ps.dip_soint3d_packed(data, mask, [s.shape for s in wl.sections], d["niter"],
+                              d["liter"], d["order"], list(d["rect"]), f["order"], f["niter"],
+                              mixed=mixed, out=out)
+        return 2 * nbytes, nbytes
     p, out = ps.dip_somean2d_batch(wl.sections, niter=d["niter"], liter=d["liter"],
                                    order=d["order"], rect=list(d["rect"]), ns=f["ns"],
                                    eps=f["eps"], median=(wl.name == "das2d"), mixed=mixed)
@@ -626,11 +626,16 @@ def main():
 
     # ---- end to end through the public API on host arrays ----
     host = None
-    if wl.name in ("batch2d", "das2d"):  # inputs in pinned host memory, outputs to pinned
+    if wl.name in ("batch2d", "das2d", "patches3d"):  # pinned host inputs and outputs
         hd = torch.from_numpy(np.concatenate([s.reshape(-1, order="F") for s in wl.sections]))
         hd = hd.pin_memory()
-        host = (hd, (torch.empty(hd.shape, dtype=torch.float32, pin_memory=True),
-                     torch.empty(hd.shape, dtype=torch.float32, pin_memory=True)))
+        if wl.name == "patches3d":
+            hm = torch.from_numpy(np.concatenate([m.reshape(-1, order="F") for m in wl.masks]))
+            host = ((hd, hm.pin_memory()), torch.empty(hd.shape, dtype=torch.float32,
+                                                       pin_memory=True))
+        else:
+            host = (hd, (torch.empty(hd.shape, dtype=torch.float32, pin_memory=True),
+                         torch.empty(hd.shape, dtype=torch.float32, pin_memory=True)))
         api_step(wl, mixed, host)  # warm the workspaces of the packed path
     torch.cuda.synchronize()
     barrier()

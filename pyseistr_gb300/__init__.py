@@ -11,8 +11,9 @@ sm_103a kernels of libpwd_gb300.so:
     csomean3d, csomf3d, csoint3d   entries
     dip2dc_batch, somean2dc_batch, many sections of uneven size in one
     somf2dc_batch,                 launch sequence (same results as one
-    dip_somean2d_batch,            call per section); the packed form takes
-    dip_somean2d_packed            one flat (pinned) host tensor
+    dip_somean2d_batch,            call per section); the packed forms take
+    dip_somean2d_packed,           flat (pinned) host tensors
+    dip_soint3d_packed
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -26,6 +27,7 @@ from .api import (  # noqa: F401
     dip2dc_batch,
     dip_somean2d_batch,
     dip_somean2d_packed,
+    dip_soint3d_packed,
     dip3dc,
     dipc,
     soint3dc,

@@ -240,6 +240,29 @@ def dip_somean2d_packed(data, shapes, niter=5, liter=10, order=2, rect=[10, 10, 
     return out
 
 
+def dip_soint3d_packed(data, mask, shapes, niter=5, liter=10, order=2, rect=[5, 5, 5],
+                       soint_order=2, soint_niter=20, mixed=False, out=None):
+    """Slopes of many cubes (dip3dc on each) followed by their interpolation
+    (soint3dc with the cube's mask, order soint_order, niter soint_niter),
+    on cubes packed one after another in flat float32 tensors `data` and
+    `mask` (CPU, pinned for full-speed copies, or CUDA).  The slopes are
+    estimated on data as given; the interpolation sees data * mask.
+    Returns the interpolated cubes as one flat CPU tensor (pinned), or fills
+    `out`.  One copy of data and mask in, one copy out."""
+    for t, name in ((data, "data"), (mask, "mask")):
+        if not isinstance(t, torch.Tensor) or t.dtype != torch.float32 or t.dim() != 1:
+            raise TypeError(f"{name} must be a flat float32 tensor")
+    d = data if data.is_cuda else data.to(_dev(), non_blocking=True)
+    m = mask if mask.is_cuda else mask.to(_dev(), non_blocking=True)
+    p = D.dip_batch(d, shapes, niter, liter, order, rect, mixed=mixed)
+    x = D.soint3d_batch(d * m, m, p, shapes, order=soint_order, niter=soint_niter)
+    if out is None:
+        out = torch.empty(x.shape, dtype=torch.float32, pin_memory=True)
+    out.copy_(x, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return out
+
+
 def dip2dc_batch(sections, niter=5, liter=20, order=2, rect=[10, 10, 1], mixed=False):
     """dip2dc over a list of 2-D sections, all in one launch sequence;
     returns the list of slopes (each equal to dip2dc of its section, or its

@@ -63,3 +63,21 @@ def test_soint3d_batch_vs_oracle():
         got = out[off:off + d.size]
         assert rel_l2(got, want) <= 1e-5
         off += d.size
+
+
+def test_packed_dip_soint3d_equals_device_calls():
+    need_gpu()
+    import torch
+    import workloads
+    import pyseistr_gb300 as ps
+    from pyseistr_gb300 import device as D
+
+    pairs = workloads.patches3d(seed=13, count=3, n1_range=(48, 64), n23_range=(8, 12))
+    shapes = [d.shape for d, _ in pairs]
+    data = torch.from_numpy(_pack([d for d, _ in pairs])).pin_memory()
+    mask = torch.from_numpy(_pack([m for _, m in pairs])).pin_memory()
+    got = ps.dip_soint3d_packed(data, mask, shapes, 2, 4, 2, [3, 3, 3], 2, 6).numpy()
+    dd, mm = data.cuda(), mask.cuda()
+    dips = D.dip_batch(dd, shapes, 2, 4, 2, (3, 3, 3))
+    want = D.soint3d_batch(dd * mm, mm, dips, shapes, order=2, niter=6).cpu().numpy()
+    assert np.array_equal(got, want)
