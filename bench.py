@@ -475,6 +475,18 @@ def time_cpu(wl, sample, kind, workers):
 
 
 # --------------------------------------------------------------------------
+def max_over_ranks(value, device):
+    """The maximum of a per-rank float over the process group (itself when
+    there is no group)."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -583,11 +595,7 @@ def main():
     if dst.graph is not None:  # replays do not pass through the launch counter
         launches += dst.graph.launches * args.steps
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     ms_step = ms / args.steps
     value = world * wl.samples() / (ms_step / 1e3)
 
@@ -644,11 +652,7 @@ def main():
     for _ in range(args.steps):
         h2d, d2h = api_step(wl, mixed, host)
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dev)
     e2e = world * wl.samples() / e2e_s
 
     plain = None
