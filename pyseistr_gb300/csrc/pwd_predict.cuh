@@ -133,24 +133,20 @@ __device__ __forceinline__ void ldl_row(int k, int n1, float diag, const float* 
 
 // Forward prediction into `out` (predict_step adj=false, predict1_step,
 // predict2_step).  in1/in2 input traces, pp1/pp2 slope traces, contiguous.
-// forw1/forw2 select the reversed filter (pwd_define adj flag).  With RHS2
-// a second input in1b is predicted into outb through the same factor (the
-// reference factorises again for it; the factor is the same).
-template <int NW, bool TWO, bool RHS2 = false>
+// forw1/forw2 select the reversed filter (pwd_define adj flag).
+template <int NW, bool TWO>
 __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
                             const float* __restrict__ in1, const float* __restrict__ pp1,
                             bool forw1, const float* __restrict__ in2,
                             const float* __restrict__ pp2, bool forw2, float* __restrict__ out,
-                            const PredictScratch& sc, const float* __restrict__ in1b = nullptr,
-                            float* __restrict__ outb = nullptr, float* __restrict__ yb = nullptr) {
-  static_assert(!(TWO && RHS2), "two predictions with two right-hand sides is not used");
+                            const PredictScratch& sc) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
   const RegConst rc = reg_const(eps, eps2);
   FilterWin<NW> w1, w2;
-  float x1[NA], x2[NA], xb[NA];  // input windows in[i .. i+2NW]
-  float t1[NA], t2[NA], tb[NA];  // pwd_set intermediates tmp[i-NW .. i+NW]
-  float O[NB][NB], D[NB];        // previous LDL' columns
-  float Y[NB], YB[NB];           // previous forward-substituted values y[k-1-c]
+  float x1[NA], x2[NA];  // input windows in[i .. i+2NW]
+  float t1[NA], t2[NA];  // pwd_set intermediates tmp[i-NW .. i+NW]
+  float O[NB][NB], D[NB];  // previous LDL' columns
+  float Y[NB];             // previous forward-substituted values y[k-1-c]
 
 #pragma unroll
   for (int cc = 0; cc < NA; cc++)
@@ -163,13 +159,11 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
   for (int cc = 0; cc < NA; cc++) {
     t1[cc] = 0.f;
     t2[cc] = 0.f;
-    tb[cc] = 0.f;
   }
 #pragma unroll
   for (int m = 0; m < NB; m++) {
     D[m] = 0.f;
     Y[m] = 0.f;
-    YB[m] = 0.f;
 #pragma unroll
     for (int q = 0; q < NB; q++) O[m][q] = 0.f;
   }
@@ -186,10 +180,8 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
   for (int q = 0; q < NB; q++) {
     x1[q + 1] = q < n1 ? in1[q] : 0.f;
     if (TWO) x2[q + 1] = q < n1 ? in2[q] : 0.f;
-    if (RHS2) xb[q + 1] = q < n1 ? in1b[q] : 0.f;
   }
   float b0, b1, b2, b3;  // boundary values t0..t3
-  float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
   if (TWO) {
     b0 = __fmul_rn(0.5f, __fadd_rn(in1[0], in2[0]));
     b1 = __fmul_rn(0.5f, __fadd_rn(in1[1], in2[1]));
@@ -200,12 +192,6 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
     b1 = in1[1];
     b2 = in1[n1 - 2];
     b3 = in1[n1 - 1];
-  }
-  if (RHS2) {
-    c0 = in1b[0];
-    c1 = in1b[1];
-    c2 = in1b[n1 - 2];
-    c3 = in1b[n1 - 1];
   }
 
   for (int i = 0; i < n1; i++) {
@@ -221,15 +207,10 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
         x2[q] = x2[q + 1];
         t2[q] = t2[q + 1];
       }
-      if (RHS2) {
-        xb[q] = xb[q + 1];
-        tb[q] = tb[q + 1];
-      }
     }
     const int ln = i + 2 * NW;  // newest input sample
     x1[NA - 1] = ln < n1 ? in1[ln] : 0.f;
     if (TWO) x2[NA - 1] = ln < n1 ? in2[ln] : 0.f;
-    if (RHS2) xb[NA - 1] = ln < n1 ? in1b[ln] : 0.f;
     if (cn < n1) {
       filter_column<NW>(c, pp1[cn], forw1, w1.a[2 * NW]);
       if (TWO) filter_column<NW>(c, pp2[cn], forw2, w2.a[2 * NW]);
@@ -241,18 +222,16 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
       }
     }
     // pwd_set forward, first loop: tmp[cn] = sum_j a[j][cn] * in[cn+j-NW]
-    float s1 = 0.f, s2 = 0.f, sb = 0.f;
+    float s1 = 0.f, s2 = 0.f;
     if (cn >= NW && cn < n1 - NW) {
 #pragma unroll
       for (int j = 0; j < NA; j++) {
         s1 = __fadd_rn(s1, __fmul_rn(w1.a[2 * NW][j], x1[j]));
         if (TWO) s2 = __fadd_rn(s2, __fmul_rn(w2.a[2 * NW][j], x2[j]));
-        if (RHS2) sb = __fadd_rn(sb, __fmul_rn(w1.a[2 * NW][j], xb[j]));
       }
     }
     t1[NA - 1] = s1;
     if (TWO) t2[NA - 1] = s2;
-    if (RHS2) tb[NA - 1] = sb;
 
     // band row i: regularization + pwd_define of each filter
     float diag, offd[NB];
@@ -261,14 +240,13 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
     if (TWO) band_add<NW>(w2, i, n1, diag, offd);
 
     // pwd_set forward, second loop: out[i] = sum_j a[j][k] tmp[k], k=i+j-NW
-    float o1 = 0.f, o2 = 0.f, ob = 0.f;
+    float o1 = 0.f, o2 = 0.f;
 #pragma unroll
     for (int j = 0; j < NA; j++) {
       int k = i + j - NW;
       if (k >= NW && k < n1 - NW) {
         o1 = __fadd_rn(o1, __fmul_rn(w1.a[j][j], t1[j]));
         if (TWO) o2 = __fadd_rn(o2, __fmul_rn(w2.a[j][j], t2[j]));
-        if (RHS2) ob = __fadd_rn(ob, __fmul_rn(w1.a[j][j], tb[j]));
       }
     }
     float b = TWO ? __fadd_rn(o1, o2) : o1;
@@ -276,74 +254,47 @@ __device__ void predict_fwd(int n1, float eps, float eps2, const ApCoef& c,
     if (i == 1) b = __fadd_rn(b, __fmul_rn(eps2, b1));
     if (i == n1 - 2) b = __fadd_rn(b, __fmul_rn(eps2, b2));
     if (i == n1 - 1) b = __fadd_rn(b, __fmul_rn(eps2, b3));
-    if (RHS2) {
-      if (i == 0) ob = __fadd_rn(ob, __fmul_rn(eps2, c0));
-      if (i == 1) ob = __fadd_rn(ob, __fmul_rn(eps2, c1));
-      if (i == n1 - 2) ob = __fadd_rn(ob, __fmul_rn(eps2, c2));
-      if (i == n1 - 1) ob = __fadd_rn(ob, __fmul_rn(eps2, c3));
-    }
 
     // LDL' row and forward substitution
     float dk, ok[NB];
     ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);
-    float y = b, y2 = ob;
+    float y = b;
 #pragma unroll
     for (int m = 0; m < NB; m++)
-      if (m < i) {
-        y = __fsub_rn(y, __fmul_rn(O[m][m], Y[m]));
-        if (RHS2) y2 = __fsub_rn(y2, __fmul_rn(O[m][m], YB[m]));
-      }
+      if (m < i) y = __fsub_rn(y, __fmul_rn(O[m][m], Y[m]));
     // store the factor column and y for the descending pass
 #pragma unroll
     for (int m = 0; m < NB; m++) sc.o[((long)m * n1 + i) * sc.ss] = ok[m];
     sc.d[(long)i * sc.ss] = dk;
     sc.y[(long)i * sc.ss] = y;
-    if (RHS2) yb[(long)i * sc.ss] = y2;
     // shift the LDL' windows: column i becomes c=0
 #pragma unroll
     for (int m = NB - 1; m > 0; m--) {
       D[m] = D[m - 1];
       Y[m] = Y[m - 1];
-      if (RHS2) YB[m] = YB[m - 1];
 #pragma unroll
       for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
     }
     D[0] = dk;
     Y[0] = y;
-    if (RHS2) YB[0] = y2;
 #pragma unroll
     for (int q = 0; q < NB; q++) O[0][q] = ok[q];
   }
 
   // back substitution: x[k] = y[k]/d[k] - sum_m o[m][k] x[k+m+1]
-  float X[NB], XB[NB];
+  float X[NB];
 #pragma unroll
-  for (int m = 0; m < NB; m++) {
-    X[m] = 0.f;
-    XB[m] = 0.f;
-  }
+  for (int m = 0; m < NB; m++) X[m] = 0.f;
   for (int k = n1 - 1; k >= 0; k--) {
     const float dk = sc.d[(long)k * sc.ss];
     float t = __fdiv_rn(sc.y[(long)k * sc.ss], dk);
-    float tb2 = RHS2 ? __fdiv_rn(yb[(long)k * sc.ss], dk) : 0.f;
 #pragma unroll
     for (int m = 0; m < NB; m++)
-      if (m < n1 - k - 1) {
-        const float om = sc.o[((long)m * n1 + k) * sc.ss];
-        t = __fsub_rn(t, __fmul_rn(om, X[m]));
-        if (RHS2) tb2 = __fsub_rn(tb2, __fmul_rn(om, XB[m]));
-      }
+      if (m < n1 - k - 1) t = __fsub_rn(t, __fmul_rn(sc.o[((long)m * n1 + k) * sc.ss], X[m]));
 #pragma unroll
-    for (int m = NB - 1; m > 0; m--) {
-      X[m] = X[m - 1];
-      if (RHS2) XB[m] = XB[m - 1];
-    }
+    for (int m = NB - 1; m > 0; m--) X[m] = X[m - 1];
     X[0] = t;
     out[k] = t;
-    if (RHS2) {
-      XB[0] = tb2;
-      outb[k] = tb2;
-    }
   }
 }
 

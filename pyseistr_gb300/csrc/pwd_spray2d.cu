@@ -43,74 +43,18 @@ __device__ __forceinline__ const SecDesc& trace_section(const SprayB& b, long g,
   return b.secs[si];
 }
 
+// Per-thread prediction scratch of the adjoint chains (thread-interleaved).
 template <int NB>
 __device__ __forceinline__ PredictScratch chain_scratch(float* scr, const SecDesc& s, long tl,
-                                                        long nthr_s, float** y2) {
+                                                        long nthr_s) {
   PredictScratch my;
   float* base = scr + s.sc0;
   const long stride = (long)s.n1 * nthr_s;
   my.o = base + tl;
   my.d = base + NB * stride + tl;
   my.y = base + (NB + 1) * stride + tl;
-  if (y2) *y2 = base + (NB + 2) * stride + tl;
   my.ss = nthr_s;
   return my;
-}
-
-// Forward spray (pwspray_lop adj=false).  Thread (trace g, dir).  MODE 0:
-// data only; MODE 1: data and ones together (u and u1); MODE 2: ones only
-// into u1.
-template <int NW, int MODE>
-__global__ void k_spray2_chains(const float* __restrict__ in, const float* __restrict__ ones,
-                                const float* __restrict__ dip, SprayBufs bf, SprayB b, ApCoef c) {
-  long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= 2 * b.ntr) return;
-  const int dir = (int)(t & 1);
-  long q;
-  const SecDesc& s = trace_section(b, t >> 1, q);
-  const int n1 = s.n1, n2 = s.n2;
-  const int i = (int)(q % n2);
-  const long i3 = q / n2;
-  const long n12 = (long)n1 * n2;
-  const float* pp = dip + s.off + i3 * n12;
-  const long slice_u = s.u0 + i3 * n2 * (long)b.np * n1;
-  float* U = (MODE == 2 ? bf.u1 : bf.u) + slice_u;
-  float* U1 = MODE == 1 ? bf.u1 + slice_u : nullptr;
-  const float* src = MODE == 2 ? ones : in + s.off + i3 * n12 + (long)i * n1;
-  float* y2 = nullptr;
-  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, t - 2 * s.tr0, 2L * n2 * s.n3,
-                                            MODE == 1 ? &y2 : nullptr);
-  auto slot = [&](float* base, int k, int sl) { return base + ((long)k * b.np + sl) * n1; };
-  const int ns = b.ns;
-  if (dir == 0) {
-    float* cen = slot(U, i, ns);
-    for (int i1 = 0; i1 < n1; i1++) cen[i1] = src[i1];
-    if (MODE == 1) {
-      float* cen1 = slot(U1, i, ns);
-      for (int i1 = 0; i1 < n1; i1++) cen1[i1] = 1.0f;
-    }
-  }
-  const float* prev = src;
-  const float* prevb = ones;
-  for (int is = 0; is < ns; is++) {
-    // dir 0 predicts forward to trace i-is-1 with its own slopes (forw=false);
-    // dir 1 predicts backward to trace i+is+1 with the slopes of ip-1.
-    const int ip = dir == 0 ? i - is - 1 : i + is + 1;
-    if (ip < 0 || ip >= n2) break;
-    const int sl = dir == 0 ? ns - is - 1 : ns + is + 1;
-    const float* pq = pp + (long)(dir == 0 ? ip : ip - 1) * n1;
-    float* out = slot(U, ip, sl);
-    if (MODE == 1) {
-      float* outb = slot(U1, ip, sl);
-      predict_fwd<NW, false, true>(n1, b.eps, b.eps2, c, prev, pq, dir == 1, nullptr, nullptr,
-                                   false, out, my, prevb, outb, y2);
-      prevb = outb;
-    } else {
-      predict_fwd<NW, false>(n1, b.eps, b.eps2, c, prev, pq, dir == 1, nullptr, nullptr, false,
-                             out, my);
-    }
-    prev = out;
-  }
 }
 
 // Factor-once form of the forward spray.  The factor store of a section
@@ -150,7 +94,8 @@ __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, Spr
 
 // Forward spray with the stored factors.  Chains are numbered so that each
 // warp holds 32 consecutive source traces of one direction (coalesced
-// factor and scratch accesses).  MODE as k_spray2_chains.
+// factor and scratch accesses).  MODE 0: data only into u; MODE 1: data and
+// the trace of ones together (u and u1); MODE 2: ones only into u1.
 template <int NW, int MODE>
 __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
                                SprayBufs bf, SprayB b) {
@@ -292,7 +237,7 @@ __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restr
   const float* W = bf.w1 + s.off + i3 * n12;
   float* tr = bf.tbuf + s.off + q * n1;
   const long nthr_s = 2L * n2 * s.n3;
-  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, q, nthr_s, nullptr);
+  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, q, nthr_s);
   float* o = out + s.pout + i3 * n12 + (long)i * n1;
   auto add_slot = [&](int ip, int sl) {
     const float wv = tri_weight(sl, b.ns);
@@ -349,7 +294,7 @@ struct SprayLayout {
   long ntr, nu, nscr, n1max, nsamp;
 };
 
-SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order, bool two_rhs) {
+SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
   SprayLayout L{};
   const int np = 2 * ns + 1, nb = 2 * order;
   long u = 0, sc = 0, tr = 0, samp = 0;
@@ -365,8 +310,9 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order, bool two_rhs)
     u += s.n * np;
     s.sc0 = sc;
     const long plane = (long)s.n1 * s.n2 * s.n3;
-    // per-chain scratch (adjoint mean) or factor store + chain scratch
-    sc += std::max((long)(nb + (two_rhs ? 3 : 2)) * 2 * plane,
+    // factor store + chain scratch, or the adjoint mean's per-chain scratch
+    // (o, d, y for 2 n2 n3 chains), whichever is larger
+    sc += std::max((long)(nb + 2) * 2 * plane,
                    (long)(2 * order + 1 + 2 * (nb + 1)) * plane + 4 * plane);
     samp = std::max(samp, s.off + s.n);
     L.n1max = std::max(L.n1max, (long)s.n1);
@@ -415,7 +361,6 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   const ApCoef c = make_apcoef(NW);
   SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, ns, 2 * ns + 1, eps * eps, eps * eps};
   const int bs = 64;
-  const unsigned gch = (unsigned)((2 * L.ntr + bs - 1) / bs);
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
   PWD_KERNEL(PWD_FAM_OTHER, st,
@@ -428,8 +373,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
   const unsigned gap = (unsigned)(((L.ntr + 31) / 32 * 64 + bs - 1) / bs);
   const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
-  if (filter != kMeanAdj)
-    PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gtr, bs, 0, st>>>(dip, w.bf, b, c));
+  PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gtr, bs, 0, st>>>(dip, w.bf, b, c));
   if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
@@ -437,9 +381,10 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
   } else if (filter == kMeanAdj) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_chains<NW, 2><<<gch, bs, 0, st>>>(data, w.ones, dip, w.bf, b, c));
+               k_spray2_apply<NW, 2><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
+    // the adjoint chains reuse the scratch region as their per-chain scratch
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
   } else {
@@ -488,7 +433,7 @@ std::vector<SecDesc> single(int n1, int n2, int n3) {
 
 size_t need_single(int n1, int n2, int n3, int ns, int order, int filter, int option) {
   std::vector<SecDesc> secs = single(n1, n2, n3);
-  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
   carve2(nullptr, L, 1, filter, option, &need);
   return need;
@@ -498,7 +443,7 @@ int run_single(const float* data, const float* dip, float* out, int n1, int n2, 
                int order, float eps, int filter, int option, int nmf, void* ws, size_t wsb,
                cudaStream_t st) {
   std::vector<SecDesc> secs = single(n1, n2, n3);
-  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
   carve2(nullptr, L, 1, filter, option, &need);
   if (!ws || wsb < need || ((uintptr_t)ws & 255)) return PWD_EWORKSPACE;
@@ -568,7 +513,7 @@ extern "C" size_t pwd_sofilter2d_batch_workspace_size(const pwd_section* section
   if (ns < 0 || order < 1 || order > PWD_MAX_ORDER || filter < 1 || filter > 3) return 0;
   if (filter == kMedian && !median_args_ok(nmf, option)) return 0;
   if (batch_table2(sections, nsec, secs) != PWD_OK) return 0;
-  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
   carve2(nullptr, L, nsec, filter, option, &need);
   return need;
@@ -584,7 +529,7 @@ extern "C" int pwd_sofilter2d_batch(const float* data, const float* dip, float* 
   std::vector<SecDesc> secs;
   int rc = batch_table2(sections, nsec, secs);
   if (rc != PWD_OK) return rc;
-  SprayLayout L = layout2(secs, ns, order, filter == kMean);
+  SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
   carve2(nullptr, L, nsec, filter, option, &need);
   if (!workspace || workspace_bytes < need || ((uintptr_t)workspace & 255)) return PWD_EWORKSPACE;
