@@ -12,9 +12,10 @@ struct SecDesc {
   int n1, n2, n3;
   int tile0;      // first elementwise tile of the section
   int ntile;      // tiles of the section
-  int ftile0;     // first 2-D smoothing tile (mixed-mode slope estimation)
-  int nftile;     // 2-D smoothing tiles of the section
-  int pad[2];
+  int ftile0;     // first column-strip tile (mixed-mode slope estimation)
+  int nftile;     // column-strip tiles of the section
+  int ctile0;     // first row-segment tile (mixed-mode slope estimation)
+  int nctile;     // row-segment tiles of the section
   long line0[3];  // first global triangle line of each smoothed axis
   long scr0[3];   // triangle scratch offset of each smoothed axis
   long tr0;       // spray: first global trace (n2*n3 traces per section)

@@ -47,6 +47,7 @@ struct DipArrays {
   const uint8_t* mask;
   float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
   float *x2, *r2;  // mixed mode: second buffers of x (dp) and r
+  float* t2;       // mixed mode: axes 0-1 result of cubes
 };
 
 struct TileRange {
@@ -718,25 +719,18 @@ __global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
 // |k| < nb, of the line extended by half-sample mirroring (x[-1-i] = x[i],
 // x[2L-1-i] = x[i], repeated when nb > L): triple2's spread, the two running
 // sums and fold2's reflections are that operator.  The mixed mode applies it
-// as a direct convolution: axes 0 and 1 in one pass over a 2-D tile with a
-// halo staged in shared memory (axis 2 of cubes in a second, elementwise
-// pass), and folds the CG vector updates into the same passes, so that one
-// CG iteration reads and writes each vector about once: two launches for
-// 2-D sections instead of three elementwise kernels and four line sweeps.
-// The x and r vectors are double-buffered across iterations because the
-// halo of a tile reads neighbours that another tile steps.
+// as a direct convolution, axis by axis: axis 0 in row segments staged in
+// shared memory (the CG input operation applied while loading), axis 1 by
+// one thread per column streaming down the rows with the CG output
+// operation and its dot products (axis 2 of cubes in a third, elementwise
+// pass).  One CG iteration of a 2-D section is four launches instead of
+// three elementwise kernels and four line sweeps.  The x and r vectors are
+// double-buffered across iterations because a segment's halo reads
+// neighbours that another segment steps.
 // ---------------------------------------------------------------------------
-// k_smooth12 strips: kSmB1 columns (one thread each) by up to kSmB2 rows,
-// input rows staged kSmStages - 1 steps ahead.
-constexpr int kSmB1 = 64, kSmB2 = 128, kSmThreads = kSmB1, kSmStages = 4;
-
-// Shared-memory floats of one k_smooth12 block for radii nb0, nb1: row
-// buffers, ring (runtime radii), staging.
-__host__ __device__ constexpr int sm_floats(int nb0, int nb1, bool ring) {
-  return 2 * (kSmB1 + 2 * (nb0 - 1)) + (ring ? (2 * nb1 - 1) * kSmB1 : 0) +
-         kSmStages * (5 * (kSmB1 + 2 * (nb0 - 1)) + 5 * kSmB1);
-}
-
+// Column strips of the axis-1 pass: kSmStrip columns (one thread each) by up
+// to kSmB2 rows; inputs staged kSmStages - 1 rows ahead.
+constexpr int kSmStrip = 64, kSmB2 = 128, kSmStages = 4;
 
 enum { SM_IN_ARR = 0, SM_IN_CG1 = 1 };
 enum { SM_OUT_ARR = 0, SM_OUT_CG1 = 1, SM_OUT_CG2 = 2 };
@@ -889,176 +883,174 @@ struct CgOut {
   }
 };
 
-// Smoothing along axes 0 and 1 of a strip of kSmB1 columns (samples along
-// axis 0) by up to kSmB2 rows (traces) of one slice, with the input and
-// output operations of the CG folded in.  One thread per output column
-// streams down the rows: the input row (with the axis-0 halo) goes through
-// a double-buffered shared row, the axis-0 result of each row enters the
-// thread's ring of the last 2 nb1 - 1 rows, and the axis-1 result of the
-// row nb1 - 1 behind is formed from the ring.  The next row's loads are in
-// flight while the current row is smoothed.  NB0, NB1 > 0 fix the radii at
-// compile time (constant taps, the ring in registers); 0 takes them from q
-// (the ring in shared memory, the thread's own column).
-template <int IN, int OUT, int NB0, int NB1>
-__global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBatch b, SmParams q) {
+// Axis 0 of the mixed-mode smoothing: one block per segment of kC0Seg samples
+// of one trace (with the axis-0 halo, mirrored at the trace ends), the CG
+// input operation applied while loading; each thread then forms 4
+// consecutive outputs from a register window read as float4.  NB0 > 0 fixes
+// the radius at compile time.
+constexpr int kC0Seg = 1024, kC0Threads = 256;
+
+template <int IN, int NB0>
+__global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, SmParams q) {
+  extern __shared__ __align__(16) float buf[];  // [kC0Seg + 2 h0 + 8]
+  const int t = blockIdx.x;
+  const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ctile0; });
+  const SecDesc& s = b.secs[si];
+  if (!sm_selected(q.sel, s)) return;
+  DipScalars* S = b.S + si;
+  const int n1 = s.n1;
+  const int nseg = (n1 + kC0Seg - 1) / kC0Seg;
+  const int lt = t - s.ctile0;
+  const int o1 = (lt % nseg) * kC0Seg;
+  const long ro = s.off + (long)(lt / nseg) * n1;  // this trace
+  const int len = min(kC0Seg, n1 - o1);
+  if (S->cg_done) {
+    // a stopped section keeps its x and r: carry them to the new buffers
+    if (IN == SM_IN_CG1)
+      for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        q.xn[ro + o1 + i] = q.xo[ro + o1 + i];
+        q.rn[ro + o1 + i] = q.ro[ro + o1 + i];
+      }
+    return;
+  }
+  const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
+  const float st = (IN == SM_IN_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
+  for (int idx = threadIdx.x; idx < len + 2 * h0; idx += blockDim.x) {
+    const int pos = o1 - h0 + idx;
+    const long i = ro + mirror_idx(pos, n1);
+    float v;
+    if (IN == SM_IN_ARR) {
+      v = q.in[i];
+    } else {
+      float xi = q.xo[i], ri = q.ro[i];
+      if (q.iter > 0) {
+        xi = __fmaf_rn(st, a.sx[i], xi);
+        ri = __fmaf_rn(st, a.sr[i], ri);
+      }
+      v = __fmaf_rn(ri, a.u1[i], -xi);  // gx = -eps x + W' r
+      if (idx >= h0 && idx < h0 + len) {
+        q.xn[i] = xi;
+        q.rn[i] = ri;
+      }
+    }
+    buf[idx] = v;
+  }
+  __syncthreads();
+  const int j0 = 4 * threadIdx.x;  // outputs o1 + j0 .. o1 + j0 + 3, centres at buf[j0 + h0]
+  if (j0 >= len) return;
+  float res[4];
+  if (NB0 > 0) {
+    constexpr int NB0c = NB0 > 0 ? NB0 : 1, H0 = NB0c - 1, NV = (4 + 2 * H0 + 3) / 4;
+    float v[4 * NV];
+    const float4* p4 = reinterpret_cast<const float4*>(buf + j0);
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      const float4 x4 = p4[k];
+      v[4 * k] = x4.x;
+      v[4 * k + 1] = x4.y;
+      v[4 * k + 2] = x4.z;
+      v[4 * k + 3] = x4.w;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int c = H0 + u;
+      float acc = __fmul_rn(tri_tap_c<NB0c>(0), v[c]), acc2 = 0.f;
+#pragma unroll
+      for (int k = 1; k <= H0; k++) {
+        const float pr = __fadd_rn(v[c - k], v[c + k]);
+        if (k & 1)
+          acc2 = __fmaf_rn(tri_tap_c<NB0c>(k), pr, acc2);
+        else
+          acc = __fmaf_rn(tri_tap_c<NB0c>(k), pr, acc);
+      }
+      res[u] = __fadd_rn(acc, acc2);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float* row = buf + j0 + u + h0;
+      float acc = __fmul_rn(tri_tap(0, q.nb0, q.wt0), row[0]);
+      for (int k = 1; k <= h0; k++)
+        acc = __fmaf_rn(tri_tap(k, q.nb0, q.wt0), __fadd_rn(row[-k], row[k]), acc);
+      res[u] = acc;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+    if (j0 + u < len) q.out[ro + o1 + j0 + u] = res[u];
+}
+
+// Axis 1 of the mixed-mode smoothing with the CG output operation: one
+// thread per column of a strip of kSmStrip columns by up to kSmB2 rows
+// streams down the rows (its input column, mirrored at the section's first
+// and last traces, staged kSmStages - 1 rows ahead by cp.async together with
+// the output operands), keeps the last 2 nb1 - 1 rows in a ring (registers
+// for a compiled radius) and forms each output row's axis-1 sum.  Threads
+// share nothing until the closing reductions.
+template <int OUT, int NB1>
+__global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b, SmParams q) {
   extern __shared__ float sm[];
   const int t = blockIdx.x;
   const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
   const SecDesc& s = b.secs[si];
   if (!sm_selected(q.sel, s)) return;
   DipScalars* S = b.S + si;
+  if (S->cg_done) return;
   const int n1 = s.n1, n2 = s.n2;
-  const int nt1 = (n1 + kSmB1 - 1) / kSmB1, nt2 = (n2 + kSmB2 - 1) / kSmB2;
+  const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + kSmB2 - 1) / kSmB2;
   const int lt = t - s.ftile0;
   const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
-  const int o1 = t1 * kSmB1, o2 = t2 * kSmB2;
+  const int o2 = t2 * kSmB2;
   const int rows = min(kSmB2, n2 - o2);
-  const long so = s.off + (long)i3 * n1 * n2;  // slice start
+  const long so = s.off + (long)i3 * n1 * n2;
   const int j = threadIdx.x;
-  const int g1 = o1 + j;                       // this thread's output column
+  const int g1 = t1 * kSmStrip + j;
   const bool colok = g1 < n1;
-  if (S->cg_done) {
-    // a stopped section keeps its x and r: carry them to the new buffers
-    if (IN == SM_IN_CG1 && colok)
-      for (int r = 0; r < rows; r++) {
-        const long i = so + (long)(o2 + r) * n1 + g1;
-        q.xn[i] = q.xo[i];
-        q.rn[i] = q.ro[i];
-      }
-    return;
-  }
-  const int nb0 = NB0 > 0 ? NB0 : q.nb0, nb1 = NB1 > 0 ? NB1 : q.nb1;
-  const int h0 = nb0 - 1, h1 = nb1 - 1;
-  const int W0 = kSmB1 + 2 * h0;
-  float* rowbuf = sm;          // [2][W0]
-  float* sring = sm + 2 * W0;  // runtime radii: [2 h1 + 1][kSmB1]
-  const float st = (q.iter > 0 && (IN == SM_IN_CG1 || OUT == SM_OUT_CG1))
-                       ? __double2float_rn(S->step) : 0.f;
+  const int nb1 = NB1 > 0 ? NB1 : q.nb1, h1 = nb1 - 1;
+  const float st = (OUT == SM_OUT_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
   const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
-  const float wt0 = NB0 > 0 ? (float)(1.0 / (NB0 * NB0)) : q.wt0;
-  const float wt1 = NB1 > 0 ? (float)(1.0 / (NB1 * NB1)) : q.wt1;
-  // input columns of this thread: c = j + m kSmB1 (< W0)
-  constexpr int kCols = NB0 > 0 ? (kSmB1 + 2 * (NB0 - 1) + kSmB1 - 1) / kSmB1 : 3;
-  int gcol[kCols];
-  bool own[kCols];
-#pragma unroll
-  for (int m = 0; m < kCols; m++) {
-    const int c = j + m * kSmB1;
-    gcol[m] = c < W0 ? mirror_idx(o1 - h0 + c, n1) : -1;
-    own[m] = c >= h0 && c < h0 + kSmB1 && o1 - h0 + c < n1;
-  }
-  // Rows are staged in shared memory kSmStages - 1 steps ahead by cp.async
-  // (4-byte copies, each thread its own columns and its own output operands,
-  // so a thread only waits for its own copies): stage [NARR][W0] of the
-  // input row, then [5][kSmB1] of the output operands.
-  constexpr int NARR = IN == SM_IN_ARR ? 1 : 5;
-  const int stage_f = NARR * W0 + 5 * kSmB1;
-  float* stg = sring + (NB1 > 0 ? 0 : (2 * h1 + 1) * kSmB1);
+  // staging slot: [6][kSmStrip] = input, then 5 output operands
+  constexpr int SE = 6 * kSmStrip;
+  float* stg = sm;
+  float* sring = sm + kSmStages * SE;  // runtime radius: [2 h1 + 1][kSmStrip]
   const int nsteps = rows + 2 * h1;
   auto issue = [&](int step) {
-    if (step < nsteps) {
-      float* sg = stg + (step % kSmStages) * stage_f;
+    if (step < nsteps && colok) {
+      float* sg = stg + (step % kSmStages) * SE + j;
       const int g2 = mirror_idx(o2 - h1 + step, n2);
-      const long rowo = so + (long)g2 * n1;
-#pragma unroll
-      for (int m = 0; m < kCols; m++) {
-        if (gcol[m] < 0) continue;
-        const long i = rowo + gcol[m];
-        const int c = j + m * kSmB1;
-        if (IN == SM_IN_ARR) {
-          cp_async4(sg + c, q.in + i);
-        } else {
-          cp_async4(sg + c, q.xo + i);
-          cp_async4(sg + W0 + c, q.ro + i);
-          cp_async4(sg + 2 * W0 + c, a.u1 + i);
-          if (q.iter > 0) {
-            cp_async4(sg + 3 * W0 + c, a.sx + i);
-            cp_async4(sg + 4 * W0 + c, a.sr + i);
-          }
-        }
-      }
+      cp_async4(sg, q.in + so + (long)g2 * n1 + g1);
       const int orow = step - 2 * h1;
-      if (OUT != SM_OUT_ARR && orow >= 0 && colok) {
+      if (OUT != SM_OUT_ARR && orow >= 0) {
         const long i = so + (long)(o2 + orow) * n1 + g1;
-        float* so_ = sg + NARR * W0 + j;
         if (OUT == SM_OUT_CG1) {
-          cp_async4(so_, a.pcg + i);
-          if (q.iter > 0) cp_async4(so_ + kSmB1, a.sp + i);
+          cp_async4(sg + kSmStrip, a.pcg + i);
+          if (q.iter > 0) cp_async4(sg + 2 * kSmStrip, a.sp + i);
         } else {
-          cp_async4(so_, q.in + i);
-          cp_async4(so_ + kSmB1, a.u1 + i);
+          cp_async4(sg + kSmStrip, q.gpc + i);
+          cp_async4(sg + 2 * kSmStrip, a.u1 + i);
           if (q.iter > 0) {
-            cp_async4(so_ + 2 * kSmB1, a.sp + i);
-            cp_async4(so_ + 3 * kSmB1, a.sx + i);
-            cp_async4(so_ + 4 * kSmB1, a.sr + i);
+            cp_async4(sg + 3 * kSmStrip, a.sp + i);
+            cp_async4(sg + 4 * kSmStrip, a.sx + i);
+            cp_async4(sg + 5 * kSmStrip, a.sr + i);
           }
         }
       }
     }
-    cp_async_commit();  // one group per step, empty past the end
+    cp_async_commit();
   };
-  float ov[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // operands of this step's output operation
-  // 1. input operation of one row (staged) into the shared row buffer
-  auto in_row = [&](int step) {
+  CgOut co;
+  float ov[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  // this step's staged input and output operands
+  auto take = [&](int step) -> float {
     issue(step + kSmStages - 1);
-    cp_async_wait<kSmStages - 1>();  // this step's row has landed
-    const float* sg = stg + (step % kSmStages) * stage_f;
-    const int r = o2 - h1 + step;  // input row (unmirrored)
-    const bool ownrow = r >= o2 && r < o2 + rows;
-    const long rowo = so + (long)r * n1;
-    float* rb = rowbuf + (step & 1) * W0;
-#pragma unroll
-    for (int m = 0; m < kCols; m++) {
-      if (gcol[m] < 0) continue;
-      const int c = j + m * kSmB1;
-      float v;
-      if (IN == SM_IN_ARR) {
-        v = sg[c];
-      } else {
-        float xi = sg[c], ri = sg[W0 + c];
-        if (q.iter > 0) {
-          xi = __fmaf_rn(st, sg[3 * W0 + c], xi);
-          ri = __fmaf_rn(st, sg[4 * W0 + c], ri);
-        }
-        v = __fmaf_rn(ri, sg[2 * W0 + c], -xi);  // gx = -eps x + W' r
-        if (ownrow && own[m]) {
-          q.xn[rowo + gcol[m]] = xi;
-          q.rn[rowo + gcol[m]] = ri;
-        }
-      }
-      rb[c] = v;
-    }
+    cp_async_wait<kSmStages - 1>();
+    const float* sg = stg + (step % kSmStages) * SE + j;
     if (OUT != SM_OUT_ARR) {
 #pragma unroll
-      for (int k = 0; k < 5; k++) ov[k] = sg[NARR * W0 + k * kSmB1 + j];
+      for (int k = 0; k < 5; k++) ov[k] = sg[(k + 1) * kSmStrip];
     }
+    return sg[0];
   };
-  // 2. axis 0 at this thread's column
-  auto axis0 = [&](int step) -> float {
-    const float* row = rowbuf + (step & 1) * W0 + j + h0;
-    float acc;
-    if (NB0 > 0) {
-      constexpr int NB0c = NB0 > 0 ? NB0 : 1;
-      // two interleaved accumulators halve the dependent FMA chain
-      float acc2 = 0.f;
-      acc = __fmul_rn(tri_tap_c<NB0c>(0), row[0]);
-#pragma unroll
-      for (int k = 1; k < NB0; k++) {
-        if (k & 1)
-          acc2 = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc2);
-        else
-          acc = __fmaf_rn(tri_tap_c<NB0c>(k), __fadd_rn(row[-k], row[k]), acc);
-      }
-      acc = __fadd_rn(acc, acc2);
-    } else {
-      acc = __fmul_rn(tri_tap(0, nb0, wt0), row[0]);
-      for (int k = 1; k <= h0; k++)
-        acc = __fmaf_rn(tri_tap(k, nb0, wt0), __fadd_rn(row[-k], row[k]), acc);
-    }
-    return acc;
-  };
-  // 3. output operation of output row orow
-  CgOut co;
   auto out_op = [&](int orow, float acc) {
     if (!colok) return;
     const long i = so + (long)(o2 + orow) * n1 + g1;
@@ -1071,19 +1063,15 @@ __global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBat
   };
   for (int k = 0; k < kSmStages - 1; k++) issue(k);
   if (NB1 > 0) {
-    constexpr int H1 = NB1 > 0 ? NB1 - 1 : 0, RING = 2 * H1 + 1;
-    constexpr int NB1c = NB1 > 0 ? NB1 : 1;
+    constexpr int NB1c = NB1 > 0 ? NB1 : 1, H1 = NB1c - 1, RING = 2 * H1 + 1;
     float rg[RING];
     for (int step0 = 0; step0 < nsteps; step0 += RING) {
 #pragma unroll
       for (int u = 0; u < RING; u++) {
         const int step = step0 + u;
         if (step < nsteps) {
-          in_row(step);
-          __syncthreads();
-          rg[u] = axis0(step);
+          rg[u] = take(step);
           if (step >= 2 * H1) {
-            // centre: ring slot of step - H1
             float acc = __fmul_rn(tri_tap_c<NB1c>(0), rg[(u - H1 + RING) % RING]), acc2 = 0.f;
 #pragma unroll
             for (int k = 1; k <= H1; k++) {
@@ -1094,35 +1082,33 @@ __global__ void __launch_bounds__(kSmThreads, 16) k_smooth12(DipArrays a, DipBat
               else
                 acc = __fmaf_rn(tri_tap_c<NB1c>(k), pr, acc);
             }
-            acc = __fadd_rn(acc, acc2);
-            out_op(step - 2 * H1, acc);
+            out_op(step - 2 * H1, __fadd_rn(acc, acc2));
           }
         }
       }
     }
   } else {
     const int RING = 2 * h1 + 1;
-    int slot = 0;  // ring slot of the current input row
+    int slot = 0;
     for (int step = 0; step < nsteps; step++) {
-      in_row(step);
-      __syncthreads();
-      sring[slot * kSmB1 + j] = axis0(step);
+      sring[slot * kSmStrip + j] = take(step);
       if (step >= 2 * h1) {
         int c = slot - h1;
         if (c < 0) c += RING;
-        float acc = __fmul_rn(tri_tap(0, nb1, wt1), sring[c * kSmB1 + j]);
+        float acc = __fmul_rn(tri_tap(0, nb1, q.wt1), sring[c * kSmStrip + j]);
         int lo = c, hi = c;
         for (int k = 1; k <= h1; k++) {
           lo = lo == 0 ? RING - 1 : lo - 1;
           hi = hi == RING - 1 ? 0 : hi + 1;
-          acc = __fmaf_rn(tri_tap(k, nb1, wt1),
-                          __fadd_rn(sring[lo * kSmB1 + j], sring[hi * kSmB1 + j]), acc);
+          acc = __fmaf_rn(tri_tap(k, nb1, q.wt1),
+                          __fadd_rn(sring[lo * kSmStrip + j], sring[hi * kSmStrip + j]), acc);
         }
         out_op(step - 2 * h1, acc);
       }
       slot = slot == RING - 1 ? 0 : slot + 1;
     }
   }
+  cp_async_wait<0>();
   if (OUT == SM_OUT_CG1) {
     dvec<1> acc = {{co.a0.value()}};
     dvec<1> tot;
@@ -1187,7 +1173,8 @@ __global__ void k_smooth3(DipArrays a, DipBatch b, SmParams q) {
 struct DipLayout {
   long ntot;  // elements spanned by the input arrays
   int ntiles;
-  int nftiles;  // 2-D smoothing tiles (mixed mode)
+  int nftiles;  // column-strip tiles (mixed mode)
+  int nctiles;  // row-segment tiles (mixed mode)
   long scr_total;
   long nlines[3];
   bool any3d, any2d;
@@ -1207,8 +1194,11 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
     s.ntile = (int)((s.n + kTile - 1) / kTile);
     tiles += s.ntile;
     s.ftile0 = L.nftiles;
-    s.nftile = ((s.n1 + kSmB1 - 1) / kSmB1) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
+    s.nftile = ((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
     L.nftiles += s.nftile;
+    s.ctile0 = L.nctiles;
+    s.nctile = ((s.n1 + kC0Seg - 1) / kC0Seg) * s.n2 * s.n3;
+    L.nctiles += s.nctile;
     const int len[3] = {s.n1, s.n2, s.n3};
     for (int a = 0; a < 3; a++) {
       s.line0[a] = lines[a];
@@ -1255,6 +1245,7 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.tri = mixed ? nullptr : cv.take<float>(L.scr_total);
   w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.r2 = mixed ? cv.take<float>(n) : nullptr;
+  w.a.t2 = mixed && L.any3d ? cv.take<float>(n) : nullptr;
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.m1 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.secs = cv.take<SecDesc>(nsec);
@@ -1320,13 +1311,19 @@ int dip3_run(DipArrays a, int dip, int niter, int liter, const int rect[3], cons
 
 typedef void (*SmKernel)(DipArrays, DipBatch, SmParams);
 
-// The k_smooth12 instance for radii nb0, nb1: compiled radii for the common
-// 10 x 10 (2-D sections) and 5 x 5 (cubes), runtime radii otherwise.
-template <int IN, int OUT>
-SmKernel sm_kernel(int nb0, int nb1) {
-  if (nb0 == 10 && nb1 == 10) return k_smooth12<IN, OUT, 10, 10>;
-  if (nb0 == 5 && nb1 == 5) return k_smooth12<IN, OUT, 5, 5>;
-  return k_smooth12<IN, OUT, 0, 0>;
+// Instances for radius nb: compiled for the common 10 (2-D sections) and 5
+// (cubes), runtime otherwise.
+template <int IN>
+SmKernel conv0_kernel(int nb) {
+  if (nb == 10) return k_conv0<IN, 10>;
+  if (nb == 5) return k_conv0<IN, 5>;
+  return k_conv0<IN, 0>;
+}
+template <int OUT>
+SmKernel conv1_kernel(int nb) {
+  if (nb == 10) return k_conv1<OUT, 10>;
+  if (nb == 5) return k_conv1<OUT, 5>;
+  return k_conv1<OUT, 0>;
 }
 
 // Mixed mode of dip3: FP32 filter taps, the fused smoothing passes of the
@@ -1344,14 +1341,19 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   q.wt2 = (float)(1.0 / ((double)q.nb2 * q.nb2));
   const bool ax2 = q.nb2 > 1 && L.any3d;
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
-  const bool compiled = (q.nb0 == 10 && q.nb1 == 10) || (q.nb0 == 5 && q.nb1 == 5);
-  const size_t smem = sizeof(float) * (size_t)sm_floats(q.nb0, q.nb1, !compiled);
-  const SmKernel k_cg1 = sm_kernel<SM_IN_CG1, SM_OUT_CG1>(q.nb0, q.nb1);
-  const SmKernel k_cg2 = sm_kernel<SM_IN_ARR, SM_OUT_CG2>(q.nb0, q.nb1);
-  const SmKernel k_in1 = sm_kernel<SM_IN_CG1, SM_OUT_ARR>(q.nb0, q.nb1);
-  const SmKernel k_arr = sm_kernel<SM_IN_ARR, SM_OUT_ARR>(q.nb0, q.nb1);
-  for (SmKernel k : {k_cg1, k_cg2, k_in1, k_arr})
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const unsigned gc = (unsigned)L.nctiles;
+  const size_t smem0 = sizeof(float) * (kC0Seg + 2 * (q.nb0 - 1) + 8);
+  const bool ring1 = !(q.nb1 == 10 || q.nb1 == 5);
+  const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
+                                        (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));
+  const SmKernel c0_cg = conv0_kernel<SM_IN_CG1>(q.nb0), c0_arr = conv0_kernel<SM_IN_ARR>(q.nb0);
+  const SmKernel c1_cg1 = conv1_kernel<SM_OUT_CG1>(q.nb1),
+                 c1_cg2 = conv1_kernel<SM_OUT_CG2>(q.nb1),
+                 c1_arr = conv1_kernel<SM_OUT_ARR>(q.nb1);
+  for (SmKernel k : {c0_cg, c0_arr})
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
+  for (SmKernel k : {c1_cg1, c1_cg2, c1_arr})
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   float* X[2] = {a.dp, a.x2};
   float* Rv[2] = {a.r, a.r2};
   PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW, true><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
@@ -1365,29 +1367,38 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       q.xn = X[(it + 1) & 1];
       q.rn = Rv[(it + 1) & 1];
       // 2-D sections (every section when no cube is smoothed along axis 2):
-      // both passes fused; the axis-2 smoothing of a length-1 line is the
-      // identity
+      // axis 0 with the input operation, axis 1 with the output operation;
+      // the axis-2 smoothing of a length-1 line is the identity
       if (!ax2 || L.any2d) {
         q.sel = ax2 ? 1 : 0;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   (k_cg1<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        q.out = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        q.in = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg1<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
         q.in = a.gp;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   (k_cg2<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        q.out = a.tmp;
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        q.in = a.tmp;
+        q.gpc = a.gp;
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg2<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
       }
-      if (ax2) {  // cubes: axes 0-1 pass, then the axis-2 pass with the CG operation
+      if (ax2) {  // cubes: axes 0 and 1, then axis 2 with the CG operation
         q.sel = 2;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   (k_in1<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
         q.in = a.tmp;
+        q.out = a.t2;
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        q.in = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st,
                    k_smooth3<SM_OUT_CG1><<<gt, kTileThreads, 0, st>>>(a, b, q));
         q.in = a.gp;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   (k_arr<<<gf, kSmThreads, smem, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
         q.in = a.tmp;
+        q.out = a.t2;
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        q.in = a.t2;
         q.gpc = a.gp;
         PWD_KERNEL(PWD_FAM_CG, st,
                    k_smooth3<SM_OUT_CG2><<<gt, kTileThreads, 0, st>>>(a, b, q));
