@@ -883,41 +883,84 @@ struct CgOut {
   }
 };
 
-// Axis 0 of the mixed-mode smoothing: one block per segment of kC0Seg samples
-// of one trace (with the axis-0 halo, mirrored at the trace ends), the CG
-// input operation applied while loading; each thread then forms 4
-// consecutive outputs from a register window read as float4.  NB0 > 0 fixes
-// the radius at compile time.
+// Axis 0 of the mixed-mode smoothing.  A tile is either several whole
+// traces of a section (traces of up to kC0Seg samples, as many as 256
+// threads x 4 outputs and the buffer hold) or one kC0Seg-sample segment of a
+// longer trace.  Each line (trace or segment) is staged in shared memory
+// with h0 samples of margin on both sides holding the mirrored neighbours,
+// the CG input operation applied while loading, at a row stride that keeps
+// every 4-output window 16-byte aligned; each thread then forms 4
+// consecutive outputs of one line from a float4 register window.  NB0 > 0
+// fixes the radius at compile time.
 constexpr int kC0Seg = 1024, kC0Threads = 256;
+
+// Lines per tile for traces of n1 <= kC0Seg samples (1 for longer traces,
+// which are cut into segments) and the buffer stride of a line.
+__host__ __device__ inline int conv0_stride(int n1, int h0) {
+  return (min(n1, kC0Seg) + 2 * h0 + 3) & ~3;
+}
+__host__ __device__ inline int conv0_lines(int n1, int h0) {
+  if (n1 > kC0Seg) return 1;
+  const int by_threads = kC0Threads / ((n1 + 3) / 4);
+  const int by_buffer = (kC0Seg + 2 * h0 + 8) / conv0_stride(n1, h0);
+  return max(1, min(by_threads, by_buffer));
+}
+// Tiles of one section.
+__host__ __device__ inline int conv0_tiles(int n1, long ntr, int h0) {
+  if (n1 > kC0Seg) return (int)(ntr * ((n1 + kC0Seg - 1) / kC0Seg));
+  const int lt = conv0_lines(n1, h0);
+  return (int)((ntr + lt - 1) / lt);
+}
 
 template <int IN, int NB0>
 __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, SmParams q) {
-  extern __shared__ __align__(16) float buf[];  // [kC0Seg + 2 h0 + 8]
+  // [kC0Seg + 2 h0 + 16]: lines fill at most kC0Seg + 2 h0 + 8, and the last
+  // window's float4 reads run up to 8 floats past its line
+  extern __shared__ __align__(16) float buf[];
   const int t = blockIdx.x;
   const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ctile0; });
   const SecDesc& s = b.secs[si];
   if (!sm_selected(q.sel, s)) return;
   DipScalars* S = b.S + si;
   const int n1 = s.n1;
-  const int nseg = (n1 + kC0Seg - 1) / kC0Seg;
+  const long ntr = s.n / n1;
+  const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
+  const int stride = conv0_stride(n1, h0);
   const int lt = t - s.ctile0;
-  const int o1 = (lt % nseg) * kC0Seg;
-  const long ro = s.off + (long)(lt / nseg) * n1;  // this trace
-  const int len = min(kC0Seg, n1 - o1);
+  // lines of this tile: traces tr0 .. tr0 + nl - 1, samples o1 .. o1 + len - 1 of each
+  long tr0;
+  int nl, o1, len;
+  if (n1 > kC0Seg) {
+    const int nseg = (n1 + kC0Seg - 1) / kC0Seg;
+    tr0 = lt / nseg;
+    nl = 1;
+    o1 = (lt % nseg) * kC0Seg;
+    len = min(kC0Seg, n1 - o1);
+  } else {
+    const int lpt = conv0_lines(n1, h0);
+    tr0 = (long)lt * lpt;
+    nl = (int)min((long)lpt, ntr - tr0);
+    o1 = 0;
+    len = n1;
+  }
+  const long so = s.off;
   if (S->cg_done) {
     // a stopped section keeps its x and r: carry them to the new buffers
     if (IN == SM_IN_CG1)
-      for (int i = threadIdx.x; i < len; i += blockDim.x) {
-        q.xn[ro + o1 + i] = q.xo[ro + o1 + i];
-        q.rn[ro + o1 + i] = q.ro[ro + o1 + i];
-      }
+      for (int k = 0; k < nl; k++)
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+          const long e = so + (tr0 + k) * n1 + o1 + i;
+          q.xn[e] = q.xo[e];
+          q.rn[e] = q.ro[e];
+        }
     return;
   }
-  const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
   const float st = (IN == SM_IN_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
-  for (int idx = threadIdx.x; idx < len + 2 * h0; idx += blockDim.x) {
-    const int pos = o1 - h0 + idx;
-    const long i = ro + mirror_idx(pos, n1);
+  const int w = len + 2 * h0;  // staged samples per line
+  for (int idx = threadIdx.x; idx < nl * w; idx += blockDim.x) {
+    const int k = idx / w, c = idx - k * w;  // line, slot (sample o1 - h0 + c)
+    const int pos = o1 - h0 + c;
+    const long i = so + (tr0 + k) * n1 + mirror_idx(pos, n1);
     float v;
     if (IN == SM_IN_ARR) {
       v = q.in[i];
@@ -928,56 +971,59 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
         ri = __fmaf_rn(st, a.sr[i], ri);
       }
       v = __fmaf_rn(ri, a.u1[i], -xi);  // gx = -eps x + W' r
-      if (idx >= h0 && idx < h0 + len) {
+      if (c >= h0 && c < h0 + len) {    // this tile's own sample
         q.xn[i] = xi;
         q.rn[i] = ri;
       }
     }
-    buf[idx] = v;
+    buf[k * stride + c] = v;
   }
   __syncthreads();
-  const int j0 = 4 * threadIdx.x;  // outputs o1 + j0 .. o1 + j0 + 3, centres at buf[j0 + h0]
-  if (j0 >= len) return;
+  const int gpl = (len + 3) / 4;  // 4-output groups per line
+  if ((int)threadIdx.x >= nl * gpl) return;
+  const int k = threadIdx.x / gpl, j0 = 4 * (threadIdx.x - k * gpl);
+  const float* wv = buf + k * stride + j0;  // window: outputs j0 .. j0+3 centred at wv[h0 + u]
   float res[4];
   if (NB0 > 0) {
     constexpr int NB0c = NB0 > 0 ? NB0 : 1, H0 = NB0c - 1, NV = (4 + 2 * H0 + 3) / 4;
     float v[4 * NV];
-    const float4* p4 = reinterpret_cast<const float4*>(buf + j0);
+    const float4* p4 = reinterpret_cast<const float4*>(wv);
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-      const float4 x4 = p4[k];
-      v[4 * k] = x4.x;
-      v[4 * k + 1] = x4.y;
-      v[4 * k + 2] = x4.z;
-      v[4 * k + 3] = x4.w;
+    for (int e = 0; e < NV; e++) {
+      const float4 x4 = p4[e];
+      v[4 * e] = x4.x;
+      v[4 * e + 1] = x4.y;
+      v[4 * e + 2] = x4.z;
+      v[4 * e + 3] = x4.w;
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const int c = H0 + u;
       float acc = __fmul_rn(tri_tap_c<NB0c>(0), v[c]), acc2 = 0.f;
 #pragma unroll
-      for (int k = 1; k <= H0; k++) {
-        const float pr = __fadd_rn(v[c - k], v[c + k]);
-        if (k & 1)
-          acc2 = __fmaf_rn(tri_tap_c<NB0c>(k), pr, acc2);
+      for (int kk = 1; kk <= H0; kk++) {
+        const float pr = __fadd_rn(v[c - kk], v[c + kk]);
+        if (kk & 1)
+          acc2 = __fmaf_rn(tri_tap_c<NB0c>(kk), pr, acc2);
         else
-          acc = __fmaf_rn(tri_tap_c<NB0c>(k), pr, acc);
+          acc = __fmaf_rn(tri_tap_c<NB0c>(kk), pr, acc);
       }
       res[u] = __fadd_rn(acc, acc2);
     }
   } else {
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const float* row = buf + j0 + u + h0;
-      float acc = __fmul_rn(tri_tap(0, q.nb0, q.wt0), row[0]);
-      for (int k = 1; k <= h0; k++)
-        acc = __fmaf_rn(tri_tap(k, q.nb0, q.wt0), __fadd_rn(row[-k], row[k]), acc);
+      const float* row = wv + h0 + u;
+      float acc = __fmul_rn(tri_tap(0, h0 + 1, q.wt0), row[0]);
+      for (int kk = 1; kk <= h0; kk++)
+        acc = __fmaf_rn(tri_tap(kk, h0 + 1, q.wt0), __fadd_rn(row[-kk], row[kk]), acc);
       res[u] = acc;
     }
   }
+  const long ro = so + (tr0 + k) * n1 + o1 + j0;
 #pragma unroll
   for (int u = 0; u < 4; u++)
-    if (j0 + u < len) q.out[ro + o1 + j0 + u] = res[u];
+    if (j0 + u < len) q.out[ro + u] = res[u];
 }
 
 // Axis 1 of the mixed-mode smoothing with the CG output operation: one
@@ -1197,7 +1243,7 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
     s.nftile = ((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
     L.nftiles += s.nftile;
     s.ctile0 = L.nctiles;
-    s.nctile = ((s.n1 + kC0Seg - 1) / kC0Seg) * s.n2 * s.n3;
+    s.nctile = conv0_tiles(s.n1, (long)s.n2 * s.n3, std::max(rect[0], 1) - 1);
     L.nctiles += s.nctile;
     const int len[3] = {s.n1, s.n2, s.n3};
     for (int a = 0; a < 3; a++) {
@@ -1342,7 +1388,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const bool ax2 = q.nb2 > 1 && L.any3d;
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
   const unsigned gc = (unsigned)L.nctiles;
-  const size_t smem0 = sizeof(float) * (kC0Seg + 2 * (q.nb0 - 1) + 8);
+  const size_t smem0 = sizeof(float) * (kC0Seg + 2 * (q.nb0 - 1) + 16);
   const bool ring1 = !(q.nb1 == 10 || q.nb1 == 5);
   const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));
