@@ -957,26 +957,29 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
   }
   const float st = (IN == SM_IN_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
   const int w = len + 2 * h0;  // staged samples per line
-  for (int idx = threadIdx.x; idx < nl * w; idx += blockDim.x) {
-    const int k = idx / w, c = idx - k * w;  // line, slot (sample o1 - h0 + c)
-    const int pos = o1 - h0 + c;
-    const long i = so + (tr0 + k) * n1 + mirror_idx(pos, n1);
-    float v;
-    if (IN == SM_IN_ARR) {
-      v = q.in[i];
-    } else {
-      float xi = q.xo[i], ri = q.ro[i];
-      if (q.iter > 0) {
-        xi = __fmaf_rn(st, a.sx[i], xi);
-        ri = __fmaf_rn(st, a.sr[i], ri);
+  for (int k = 0; k < nl; k++) {
+    const long line = so + (tr0 + k) * n1;
+    float* bl = buf + k * stride;
+    for (int c = threadIdx.x; c < w; c += blockDim.x) {  // slot c: sample o1 - h0 + c
+      const int pos = o1 - h0 + c;
+      const long i = line + ((unsigned)pos < (unsigned)n1 ? pos : mirror_idx(pos, n1));
+      float v;
+      if (IN == SM_IN_ARR) {
+        v = q.in[i];
+      } else {
+        float xi = q.xo[i], ri = q.ro[i];
+        if (q.iter > 0) {
+          xi = __fmaf_rn(st, a.sx[i], xi);
+          ri = __fmaf_rn(st, a.sr[i], ri);
+        }
+        v = __fmaf_rn(ri, a.u1[i], -xi);  // gx = -eps x + W' r
+        if (c >= h0 && c < h0 + len) {    // this tile's own sample
+          q.xn[i] = xi;
+          q.rn[i] = ri;
+        }
       }
-      v = __fmaf_rn(ri, a.u1[i], -xi);  // gx = -eps x + W' r
-      if (c >= h0 && c < h0 + len) {    // this tile's own sample
-        q.xn[i] = xi;
-        q.rn[i] = ri;
-      }
+      bl[c] = v;
     }
-    buf[k * stride + c] = v;
   }
   __syncthreads();
   const int gpl = (len + 3) / 4;  // 4-output groups per line
