@@ -263,20 +263,20 @@ __global__ void k_cg_stepgrad(DipArrays a, DipBatch b, int iter) {
   }
 }
 
-// The step of the last iteration when the CG ran all liter iterations.
+// The step of the last iteration when the CG ran all liter iterations
+// (:364-368).  Only x, the CG's result, is read afterwards (the line search
+// of dip3 uses it; p and r are discarded when ps_conjgrad returns), so only
+// x is stepped.
 __global__ void k_cg_step(DipArrays a, DipBatch b) {
   const TileRange tr = tile_range(b, blockIdx.x);
   const SecDesc& s = b.secs[tr.sec];
   const DipScalars* S = b.S + tr.sec;
   if (S->cg_done) return;
   const float st = __double2float_rn(S->step);
-  float *pcg = a.pcg + s.off, *x = a.dp + s.off, *r = a.r + s.off;
-  const float *sp = a.sp + s.off, *sx = a.sx + s.off, *sr = a.sr + s.off;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
-    pcg[i] = __fadd_rn(pcg[i], __fmul_rn(st, sp[i]));
+  float* x = a.dp + s.off;
+  const float* sx = a.sx + s.off;
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
     x[i] = __fadd_rn(x[i], __fmul_rn(st, sx[i]));
-    r[i] = __fadd_rn(r[i], __fmul_rn(st, sr[i]));
-  }
 }
 
 // gp = eps*p + S' gx; gn = gp.gp; convergence test (:319, :328-345).
