@@ -286,17 +286,25 @@ def family_bytes(wl, launches, mixed=False):
             # read u, p0, dp, write p (16 B)
             trials = max(0, cnt - 1 - niter)
             bps = (12.0 + 24.0 * niter + 16.0 * trials) / max(1, 1 + niter + trials)
+        elif fam == "cg" and mixed and d["rect"][2] > 1 and wl.name in ("plain3d", "patches3d"):
+            # cubes, per CG iteration: axis 0 with the step and gradient 32
+            # (24 first), axis 1 8, axis 2 with gp 20 (12 first), axis 0 8,
+            # axis 1 8, axis 2 with the update 36 (24 first); scale 28 and
+            # final step 12 per Gauss-Newton iteration
+            per_outer = 28 + (24 + 8 + 12 + 8 + 8 + 24) + (liter - 1) * 112 + 12
+            bps = per_outer / (2.0 + 6.0 * liter)
         elif fam == "cg" and mixed:
-            # per Gauss-Newton iteration: scale 28; fused pass 1 (step,
-            # gradient, smoothing, gp) 28 then 44; fused pass 2 (smoothing,
-            # conjugate update) 20 then 32; final step 36
-            per_outer = 28 + 28 + 44 * (liter - 1) + 20 + 32 * (liter - 1) + 36
-            bps = per_outer / (2.0 + 2.0 * liter)
+            # per CG iteration: axis 0 with the step and gradient 32 (24
+            # first), axis 1 with gp 20 (12 first), axis 0 of gp 8, axis 1
+            # with the conjugate update 36 (24 first); scale 28 and final
+            # step 12 per Gauss-Newton iteration
+            per_outer = 28 + (24 + 12 + 8 + 24) + (liter - 1) * 96 + 12
+            bps = per_outer / (2.0 + 4.0 * liter)
         elif fam == "cg":
             # per Gauss-Newton iteration: scale 28, first gradient 16, later
             # step+gradient 44, gp 16, first update 24, later updates 36,
-            # final step 36 (bytes per sample)
-            per_outer = 28 + 16 + 44 * (liter - 1) + 16 * liter + 24 + 36 * (liter - 1) + 36
+            # final step 12 (bytes per sample)
+            per_outer = 28 + 16 + 44 * (liter - 1) + 16 * liter + 24 + 36 * (liter - 1) + 12
             bps = per_outer / (2.0 + 3.0 * liter)
         elif fam == "triangle":
             bps = 8.0  # each line sweep reads and writes its axis once
