@@ -892,7 +892,7 @@ struct CgOut {
 // every 4-output window 16-byte aligned; each thread then forms 4
 // consecutive outputs of one line from a float4 register window.  NB0 > 0
 // fixes the radius at compile time.
-constexpr int kC0Seg = 1024, kC0Threads = 256;
+constexpr int kC0Seg = 512, kC0Threads = 128;
 
 // Lines per tile for traces of n1 <= kC0Seg samples (1 for longer traces,
 // which are cut into segments) and the buffer stride of a line.
