@@ -48,6 +48,7 @@ struct DipArrays {
   float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
   float *x2, *r2;  // mixed mode: second buffers of x (dp) and r
   float* t2;       // mixed mode: axes 0-1 result of cubes
+  int4* c0map;     // mixed mode: tile table of the axis-0 pass
 };
 
 struct TileRange {
@@ -745,6 +746,8 @@ struct SmParams {
   const float* gpc;  // gp, read at the output sample by SM_OUT_CG2 of axis 2
   const float *xo, *ro;
   float *xn, *rn;
+  const int4* c0map;  // axis-0 tiles: section, first trace, first sample, lines << 16 | length
+  int c0buf;          // floats per axis-0 staging buffer
 };
 
 __device__ __forceinline__ bool sm_selected(int sel, const SecDesc& s) {
@@ -884,14 +887,15 @@ struct CgOut {
 };
 
 // Axis 0 of the mixed-mode smoothing.  A tile is either several whole
-// traces of a section (traces of up to kC0Seg samples, as many as 256
+// traces of a section (traces of up to kC0Seg samples, as many as the
 // threads x 4 outputs and the buffer hold) or one kC0Seg-sample segment of a
-// longer trace.  Each line (trace or segment) is staged in shared memory
-// with h0 samples of margin on both sides holding the mirrored neighbours,
-// the CG input operation applied while loading, at a row stride that keeps
-// every 4-output window 16-byte aligned; each thread then forms 4
-// consecutive outputs of one line from a float4 register window.  NB0 > 0
-// fixes the radius at compile time.
+// longer trace; a table built once per call gives every tile's section,
+// first trace, first sample, line count and line length.  Each line (trace
+// or segment) is copied to shared memory by cp.async with h0 samples of
+// margin on both sides holding the mirrored neighbours, at a row stride that
+// keeps every 4-output window 16-byte aligned; the CG input operation then
+// runs in place; each thread finally forms 4 consecutive outputs of one line
+// from a float4 register window.  NB0 > 0 fixes the radius at compile time.
 constexpr int kC0Seg = 512, kC0Threads = 128;
 
 // Lines per tile for traces of n1 <= kC0Seg samples (1 for longer traces,
@@ -911,77 +915,105 @@ __host__ __device__ inline int conv0_tiles(int n1, long ntr, int h0) {
   const int lt = conv0_lines(n1, h0);
   return (int)((ntr + lt - 1) / lt);
 }
+// Floats per staging buffer: lines fill at most kC0Seg + 2 h0 + 8, and the
+// last window's float4 reads run up to 8 floats past its line.
+__host__ __device__ inline int conv0_buffer(int h0) { return (kC0Seg + 2 * h0 + 16 + 3) & ~3; }
 
-template <int IN, int NB0>
-__global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, SmParams q) {
-  // [kC0Seg + 2 h0 + 16]: lines fill at most kC0Seg + 2 h0 + 8, and the last
-  // window's float4 reads run up to 8 floats past its line
-  extern __shared__ __align__(16) float buf[];
-  const int t = blockIdx.x;
-  const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ctile0; });
-  const SecDesc& s = b.secs[si];
-  if (!sm_selected(q.sel, s)) return;
-  DipScalars* S = b.S + si;
-  const int n1 = s.n1;
-  const long ntr = s.n / n1;
-  const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
-  const int stride = conv0_stride(n1, h0);
-  const int lt = t - s.ctile0;
-  // lines of this tile: traces tr0 .. tr0 + nl - 1, samples o1 .. o1 + len - 1 of each
-  long tr0;
-  int nl, o1, len;
+// The tile table of the axis-0 pass (one thread per tile).
+__global__ void k_conv0_map(const SecDesc* secs, int nsec, int ntiles, int h0, int4* map) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const int si = find_section(nsec, (long)t, [&](int k) { return (long)secs[k].ctile0; });
+  const SecDesc& s = secs[si];
+  const int n1 = s.n1, lt = t - s.ctile0;
+  int tr0, nl, o1, len;
   if (n1 > kC0Seg) {
     const int nseg = (n1 + kC0Seg - 1) / kC0Seg;
     tr0 = lt / nseg;
     nl = 1;
-    o1 = (lt % nseg) * kC0Seg;
+    o1 = (lt - tr0 * nseg) * kC0Seg;
     len = min(kC0Seg, n1 - o1);
   } else {
     const int lpt = conv0_lines(n1, h0);
-    tr0 = (long)lt * lpt;
-    nl = (int)min((long)lpt, ntr - tr0);
+    tr0 = lt * lpt;
+    nl = min(lpt, s.n2 * s.n3 - tr0);
     o1 = 0;
     len = n1;
   }
-  const long so = s.off;
+  map[t] = make_int4(si, tr0, o1, (nl << 16) | len);
+}
+
+template <int IN, int NB0>
+__global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, SmParams q) {
+  // buffers of q.c0buf floats: the input (SM_IN_ARR); x (becoming gx), r,
+  // u1, sx, sr (SM_IN_CG1)
+  extern __shared__ __align__(16) float buf[];
+  const int4 tm = q.c0map[blockIdx.x];
+  const SecDesc& s = b.secs[tm.x];
+  if (!sm_selected(q.sel, s)) return;
+  DipScalars* S = b.S + tm.x;
+  const int n1 = s.n1;
+  const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
+  const int stride = conv0_stride(n1, h0);
+  const int o1 = tm.z, nl = tm.w >> 16, len = tm.w & 0xffff;
+  // indices below are relative to the tile's first trace (a section holds
+  // fewer than 2^31 samples)
+  const long so = s.off + (long)tm.y * n1;
   if (S->cg_done) {
     // a stopped section keeps its x and r: carry them to the new buffers
     if (IN == SM_IN_CG1)
       for (int k = 0; k < nl; k++)
-        for (int i = threadIdx.x; i < len; i += blockDim.x) {
-          const long e = so + (tr0 + k) * n1 + o1 + i;
+        for (int i = threadIdx.x; i < len; i += kC0Threads) {
+          const long e = so + k * n1 + o1 + i;
           q.xn[e] = q.xo[e];
           q.rn[e] = q.ro[e];
         }
     return;
   }
-  const float st = (IN == SM_IN_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
   const int w = len + 2 * h0;  // staged samples per line
+  const int nbuf = q.c0buf;
+  const bool stepped = IN == SM_IN_CG1 && q.iter > 0;
   for (int k = 0; k < nl; k++) {
-    const long line = so + (tr0 + k) * n1;
     float* bl = buf + k * stride;
-    for (int c = threadIdx.x; c < w; c += blockDim.x) {  // slot c: sample o1 - h0 + c
+    for (int c = threadIdx.x; c < w; c += kC0Threads) {  // slot c: sample o1 - h0 + c
       const int pos = o1 - h0 + c;
-      const long i = line + ((unsigned)pos < (unsigned)n1 ? pos : mirror_idx(pos, n1));
-      float v;
+      const int i = k * n1 + ((unsigned)pos < (unsigned)n1 ? pos : mirror_idx(pos, n1));
       if (IN == SM_IN_ARR) {
-        v = q.in[i];
+        cp_async4(bl + c, q.in + so + i);
       } else {
-        float xi = q.xo[i], ri = q.ro[i];
-        if (q.iter > 0) {
-          xi = __fmaf_rn(st, a.sx[i], xi);
-          ri = __fmaf_rn(st, a.sr[i], ri);
-        }
-        v = __fmaf_rn(ri, a.u1[i], -xi);  // gx = -eps x + W' r
-        if (c >= h0 && c < h0 + len) {    // this tile's own sample
-          q.xn[i] = xi;
-          q.rn[i] = ri;
+        cp_async4(bl + c, q.xo + so + i);
+        cp_async4(bl + nbuf + c, q.ro + so + i);
+        cp_async4(bl + 2 * nbuf + c, a.u1 + so + i);
+        if (stepped) {
+          cp_async4(bl + 3 * nbuf + c, a.sx + so + i);
+          cp_async4(bl + 4 * nbuf + c, a.sr + so + i);
         }
       }
-      bl[c] = v;
     }
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
+  if (IN == SM_IN_CG1) {
+    const float st = stepped ? __double2float_rn(S->step) : 0.f;
+    for (int k = 0; k < nl; k++) {
+      float* bl = buf + k * stride;
+      for (int c = threadIdx.x; c < w; c += kC0Threads) {
+        float xi = bl[c], ri = bl[nbuf + c];
+        if (stepped) {
+          xi = __fmaf_rn(st, bl[3 * nbuf + c], xi);
+          ri = __fmaf_rn(st, bl[4 * nbuf + c], ri);
+        }
+        bl[c] = __fmaf_rn(ri, bl[2 * nbuf + c], -xi);  // gx = -eps x + W' r
+        if (c >= h0 && c < h0 + len) {                  // this tile's own sample
+          const long e = so + k * n1 + o1 - h0 + c;
+          q.xn[e] = xi;
+          q.rn[e] = ri;
+        }
+      }
+    }
+    __syncthreads();
+  }
   const int gpl = (len + 3) / 4;  // 4-output groups per line
   if ((int)threadIdx.x >= nl * gpl) return;
   const int k = threadIdx.x / gpl, j0 = 4 * (threadIdx.x - k * gpl);
@@ -1023,10 +1055,10 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
       res[u] = acc;
     }
   }
-  const long ro = so + (tr0 + k) * n1 + o1 + j0;
+  float* out = q.out + so + k * n1 + o1 + j0;
 #pragma unroll
   for (int u = 0; u < 4; u++)
-    if (j0 + u < len) q.out[ro + u] = res[u];
+    if (j0 + u < len) out[u] = res[u];
 }
 
 // Axis 1 of the mixed-mode smoothing with the CG output operation: one
@@ -1295,6 +1327,7 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.r2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.t2 = mixed && L.any3d ? cv.take<float>(n) : nullptr;
+  w.a.c0map = mixed ? cv.take<int4>(L.nctiles) : nullptr;
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.m1 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.secs = cv.take<SecDesc>(nsec);
@@ -1391,7 +1424,9 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const bool ax2 = q.nb2 > 1 && L.any3d;
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
   const unsigned gc = (unsigned)L.nctiles;
-  const size_t smem0 = sizeof(float) * (kC0Seg + 2 * (q.nb0 - 1) + 16);
+  q.c0map = a.c0map;
+  q.c0buf = conv0_buffer(q.nb0 - 1);
+  const size_t smem0 = sizeof(float) * q.c0buf, smem0cg = 5 * smem0;
   const bool ring1 = !(q.nb1 == 10 || q.nb1 == 5);
   const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));
@@ -1399,12 +1434,15 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const SmKernel c1_cg1 = conv1_kernel<SM_OUT_CG1>(q.nb1),
                  c1_cg2 = conv1_kernel<SM_OUT_CG2>(q.nb1),
                  c1_arr = conv1_kernel<SM_OUT_ARR>(q.nb1);
-  for (SmKernel k : {c0_cg, c0_arr})
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
+  cudaFuncSetAttribute(c0_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0cg);
+  cudaFuncSetAttribute(c0_arr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
   for (SmKernel k : {c1_cg1, c1_cg2, c1_arr})
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   float* X[2] = {a.dp, a.x2};
   float* Rv[2] = {a.r, a.r2};
+  PWD_KERNEL(PWD_FAM_OTHER, st,
+             k_conv0_map<<<(gc + 255) / 256, 256, 0, st>>>(b.secs, b.nsec, (int)gc, q.nb0 - 1,
+                                                             a.c0map));
   PWD_KERNEL(PWD_FAM_PWD, st, k_residual<NW, true><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
   for (int iter = 0; iter < niter; iter++) {
     PWD_KERNEL(PWD_FAM_PWD, st, k_prep<NW, true><<<gt, kTileThreads, 0, st>>>(a, b, c, dip));
@@ -1421,7 +1459,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       if (!ax2 || L.any2d) {
         q.sel = ax2 ? 1 : 0;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_cg1<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
         q.in = a.gp;
@@ -1434,7 +1472,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       if (ax2) {  // cubes: axes 0 and 1, then axis 2 with the CG operation
         q.sel = 2;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
         q.out = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
