@@ -888,15 +888,25 @@ struct CgOut {
 
 // Axis 0 of the mixed-mode smoothing.  A tile is either several whole
 // traces of a section (traces of up to kC0Seg samples, as many as the
-// threads x 4 outputs and the buffer hold) or one kC0Seg-sample segment of a
+// threads x outputs and the buffer hold) or one kC0Seg-sample segment of a
 // longer trace; a table built once per call gives every tile's section,
 // first trace, first sample, line count and line length.  Each line (trace
 // or segment) is copied to shared memory by cp.async with h0 samples of
 // margin on both sides holding the mirrored neighbours, at a row stride that
-// keeps every 4-output window 16-byte aligned; the CG input operation then
-// runs in place; each thread finally forms 4 consecutive outputs of one line
-// from a float4 register window.  NB0 > 0 fixes the radius at compile time.
-constexpr int kC0Seg = 512, kC0Threads = 128;
+// keeps every output window 16-byte aligned; the CG input operation then
+// runs in place; each thread finally forms consecutive outputs of one line
+// from a float4 register window: 8 per thread for the plain array pass (64
+// threads), 4 for the pass with the CG input operation (128 threads, five
+// staged arrays).  NB0 > 0 fixes the radius at compile time.
+constexpr int kC0Seg = 512;
+template <int IN>
+__host__ __device__ constexpr int conv0_outs() {
+  return IN == SM_IN_ARR ? 8 : 4;
+}
+template <int IN>
+__host__ __device__ constexpr int conv0_threads() {
+  return kC0Seg / conv0_outs<IN>();
+}
 
 // Lines per tile for traces of n1 <= kC0Seg samples (1 for longer traces,
 // which are cut into segments) and the buffer stride of a line.
@@ -905,7 +915,8 @@ __host__ __device__ inline int conv0_stride(int n1, int h0) {
 }
 __host__ __device__ inline int conv0_lines(int n1, int h0) {
   if (n1 > kC0Seg) return 1;
-  const int by_threads = kC0Threads / ((n1 + 3) / 4);
+  // 8-output groups bound the line count of both passes: ceil(n1/4) <= 2 ceil(n1/8)
+  const int by_threads = conv0_threads<SM_IN_ARR>() / ((n1 + 7) / 8);
   const int by_buffer = (kC0Seg + 2 * h0 + 8) / conv0_stride(n1, h0);
   return max(1, min(by_threads, by_buffer));
 }
@@ -916,8 +927,8 @@ __host__ __device__ inline int conv0_tiles(int n1, long ntr, int h0) {
   return (int)((ntr + lt - 1) / lt);
 }
 // Floats per staging buffer: lines fill at most kC0Seg + 2 h0 + 8, and the
-// last window's float4 reads run up to 8 floats past its line.
-__host__ __device__ inline int conv0_buffer(int h0) { return (kC0Seg + 2 * h0 + 16 + 3) & ~3; }
+// last window's float4 reads run up to 10 floats past its line.
+__host__ __device__ inline int conv0_buffer(int h0) { return (kC0Seg + 2 * h0 + 24 + 3) & ~3; }
 
 // The tile table of the axis-0 pass (one thread per tile).
 __global__ void k_conv0_map(const SecDesc* secs, int nsec, int ntiles, int h0, int4* map) {
@@ -944,7 +955,9 @@ __global__ void k_conv0_map(const SecDesc* secs, int nsec, int ntiles, int h0, i
 }
 
 template <int IN, int NB0>
-__global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, SmParams q) {
+__global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipBatch b,
+                                                              SmParams q) {
+  constexpr int NT = conv0_threads<IN>(), OUTS = conv0_outs<IN>();
   // buffers of q.c0buf floats: the input (SM_IN_ARR); x (becoming gx), r,
   // u1, sx, sr (SM_IN_CG1)
   extern __shared__ __align__(16) float buf[];
@@ -963,7 +976,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
     // a stopped section keeps its x and r: carry them to the new buffers
     if (IN == SM_IN_CG1)
       for (int k = 0; k < nl; k++)
-        for (int i = threadIdx.x; i < len; i += kC0Threads) {
+        for (int i = threadIdx.x; i < len; i += NT) {
           const long e = so + k * n1 + o1 + i;
           q.xn[e] = q.xo[e];
           q.rn[e] = q.ro[e];
@@ -975,7 +988,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
   const bool stepped = IN == SM_IN_CG1 && q.iter > 0;
   for (int k = 0; k < nl; k++) {
     float* bl = buf + k * stride;
-    for (int c = threadIdx.x; c < w; c += kC0Threads) {  // slot c: sample o1 - h0 + c
+    for (int c = threadIdx.x; c < w; c += NT) {  // slot c: sample o1 - h0 + c
       const int pos = o1 - h0 + c;
       const int i = k * n1 + ((unsigned)pos < (unsigned)n1 ? pos : mirror_idx(pos, n1));
       if (IN == SM_IN_ARR) {
@@ -998,7 +1011,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
     const float st = stepped ? __double2float_rn(S->step) : 0.f;
     for (int k = 0; k < nl; k++) {
       float* bl = buf + k * stride;
-      for (int c = threadIdx.x; c < w; c += kC0Threads) {
+      for (int c = threadIdx.x; c < w; c += NT) {
         float xi = bl[c], ri = bl[nbuf + c];
         if (stepped) {
           xi = __fmaf_rn(st, bl[3 * nbuf + c], xi);
@@ -1014,13 +1027,16 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
     }
     __syncthreads();
   }
-  const int gpl = (len + 3) / 4;  // 4-output groups per line
+  const int gpl = (len + OUTS - 1) / OUTS;  // output groups per line
   if ((int)threadIdx.x >= nl * gpl) return;
-  const int k = threadIdx.x / gpl, j0 = 4 * (threadIdx.x - k * gpl);
-  const float* wv = buf + k * stride + j0;  // window: outputs j0 .. j0+3 centred at wv[h0 + u]
-  float res[4];
+  // line of this thread: (tid + 1/2) / gpl is at least 1/(2 gpl) from an
+  // integer, far above the error of the approximate quotient
+  const int k = nl == 1 ? 0 : (int)__fdividef((float)threadIdx.x + 0.5f, (float)gpl);
+  const int j0 = OUTS * (threadIdx.x - k * gpl);
+  const float* wv = buf + k * stride + j0;  // window: outputs j0 .. centred at wv[h0 + u]
+  float res[OUTS];
   if (NB0 > 0) {
-    constexpr int NB0c = NB0 > 0 ? NB0 : 1, H0 = NB0c - 1, NV = (4 + 2 * H0 + 3) / 4;
+    constexpr int NB0c = NB0 > 0 ? NB0 : 1, H0 = NB0c - 1, NV = (OUTS + 2 * H0 + 3) / 4;
     float v[4 * NV];
     const float4* p4 = reinterpret_cast<const float4*>(wv);
 #pragma unroll
@@ -1032,7 +1048,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
       v[4 * e + 3] = x4.w;
     }
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < OUTS; u++) {
       const int c = H0 + u;
       float acc = __fmul_rn(tri_tap_c<NB0c>(0), v[c]), acc2 = 0.f;
 #pragma unroll
@@ -1047,7 +1063,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
     }
   } else {
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < OUTS; u++) {
       const float* row = wv + h0 + u;
       float acc = __fmul_rn(tri_tap(0, h0 + 1, q.wt0), row[0]);
       for (int kk = 1; kk <= h0; kk++)
@@ -1057,7 +1073,7 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
   }
   float* out = q.out + so + k * n1 + o1 + j0;
 #pragma unroll
-  for (int u = 0; u < 4; u++)
+  for (int u = 0; u < OUTS; u++)
     if (j0 + u < len) out[u] = res[u];
 }
 
@@ -1065,9 +1081,9 @@ __global__ void __launch_bounds__(kC0Threads) k_conv0(DipArrays a, DipBatch b, S
 // thread per column of a strip of kSmStrip columns by up to kSmB2 rows
 // streams down the rows (its input column, mirrored at the section's first
 // and last traces, staged kSmStages - 1 rows ahead by cp.async together with
-// the output operands), keeps the last 2 nb1 - 1 rows in a ring (registers
-// for a compiled radius) and forms each output row's axis-1 sum.  Threads
-// share nothing until the closing reductions.
+// the output operands), keeps the last 2 nb1 - 1 rows (in registers for a
+// compiled radius, in a shared-memory ring otherwise) and forms each output
+// row's axis-1 sum.  Threads share nothing until the closing reductions.
 template <int OUT, int NB1>
 __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b, SmParams q) {
   extern __shared__ float sm[];
@@ -1459,12 +1475,12 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       if (!ax2 || L.any2d) {
         q.sel = ax2 ? 1 : 0;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0cg, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, conv0_threads<SM_IN_CG1>(), smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_cg1<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
         q.in = a.gp;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
         q.in = a.tmp;
         q.gpc = a.gp;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_cg2<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
@@ -1472,7 +1488,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       if (ax2) {  // cubes: axes 0 and 1, then axis 2 with the CG operation
         q.sel = 2;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, kC0Threads, smem0cg, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, conv0_threads<SM_IN_CG1>(), smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
         q.out = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
@@ -1481,7 +1497,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
                    k_smooth3<SM_OUT_CG1><<<gt, kTileThreads, 0, st>>>(a, b, q));
         q.in = a.gp;
         q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, kC0Threads, smem0, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
         q.in = a.tmp;
         q.out = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
