@@ -21,6 +21,7 @@ struct SecDesc {
   long tr0;       // spray: first global trace (n2*n3 traces per section)
   long u0;        // spray: offset of the section's sprayed panels
   long sc0;       // spray: offset of the section's per-chain scratch
+  long tp0;       // spray: first trace in the numbering padded to 32 per section
 };
 
 // Section holding global item g, given each section's first item (sorted).

@@ -25,6 +25,7 @@ struct SprayB {
   const int* tile_sec;
   int nsec, ntiles;
   long ntr;  // traces over the batch (n2*n3 per section)
+  long ntp;  // the same with each section's traces padded to a multiple of 32
   int ns, np;
   float eps, eps2;
 };
@@ -58,20 +59,24 @@ __device__ __forceinline__ PredictScratch chain_scratch(float* scr, const SecDes
 }
 
 // Factor-once form of the forward spray.  The factor store of a section
-// (at scr + sc0) holds, for every trace k, the passfilter taps of its slopes
-// and the LDL' factors of the predictions that use them (forw = false for
-// the chains running towards lower traces, true for the others), each
-// element trace-interleaved; then the chains' y scratch.
+// (at scr + sc0, 128-byte aligned) holds, for every trace k, the
+// passfilter taps of its slopes and the LDL' factors of the predictions
+// that use them (forw = false for the chains running towards lower traces,
+// true for the others), each element trace-interleaved with the section's
+// traces padded to a multiple of 32 (ntp), so that a warp of 32 traces
+// reads whole 128-byte lines; then the chains' y scratch, interleaved the
+// same way over the 2 ntp chains.
 struct FactorLayout {
   float *taps, *f0, *f1, *y, *yb;
-  long ntr_s;
+  long ntp;
 };
+__host__ __device__ inline long padded_traces(long ntr) { return (ntr + 31) / 32 * 32; }
 template <int NW>
 __device__ __forceinline__ FactorLayout factor_layout(const SprayBufs& bf, const SecDesc& s) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
   FactorLayout f;
-  f.ntr_s = (long)s.n2 * s.n3;
-  const long plane = (long)s.n1 * f.ntr_s;
+  f.ntp = padded_traces((long)s.n2 * s.n3);
+  const long plane = (long)s.n1 * f.ntp;
   f.taps = bf.scr + s.sc0;
   f.f0 = f.taps + NA * plane;
   f.f1 = f.f0 + (NB + 1) * plane;
@@ -80,21 +85,30 @@ __device__ __forceinline__ FactorLayout factor_layout(const SprayBufs& bf, const
   return f;
 }
 
-// Taps and factors of every trace of the batch: thread per trace.
+// The section of padded trace g and its trace q there (q >= n2 n3 is
+// padding).
+__device__ __forceinline__ const SecDesc& padded_section(const SprayB& b, long g, long& q) {
+  const int si = find_section(b.nsec, g, [&](int k) { return b.secs[k].tp0; });
+  q = g - b.secs[si].tp0;
+  return b.secs[si];
+}
+
+// Taps and factors of every trace of the batch: thread per padded trace.
 template <int NW>
 __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, SprayB b, ApCoef c) {
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (g >= b.ntr) return;
+  if (g >= b.ntp) return;
   long q;
-  const SecDesc& s = trace_section(b, g, q);
+  const SecDesc& s = padded_section(b, g, q);
+  if (q >= (long)s.n2 * s.n3) return;
   const FactorLayout f = factor_layout<NW>(bf, s);
-  PredictFactor F{f.taps + q, f.f0 + q, f.f1 + q, f.ntr_s};
+  PredictFactor F{f.taps + q, f.f0 + q, f.f1 + q, f.ntp};
   predict_factor<NW>(s.n1, b.eps, b.eps2, c, dip + s.off + q * s.n1, F);
 }
 
 // Forward spray with the stored factors.  Chains are numbered so that each
-// warp holds 32 consecutive source traces of one direction (coalesced
-// factor and scratch accesses).  MODE 0: data only into u; MODE 1: data and
+// warp holds 32 consecutive (padded) source traces of one section and one
+// direction (whole-line factor and scratch accesses).  MODE 0: data only into u; MODE 1: data and
 // the trace of ones together (u and u1); MODE 2: ones only into u1.
 template <int NW, int MODE>
 __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
@@ -103,9 +117,10 @@ __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int dir = (int)((t >> 5) & 1);
   const long g = (t >> 6) * 32 + (t & 31);
-  if (g >= b.ntr) return;
+  if (g >= b.ntp) return;
   long q;
-  const SecDesc& s = trace_section(b, g, q);
+  const SecDesc& s = padded_section(b, g, q);
+  if (q >= (long)s.n2 * s.n3) return;
   const int n1 = s.n1, n2 = s.n2;
   const int i = (int)(q % n2);
   const long i3 = q / n2;
@@ -115,7 +130,7 @@ __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict
   float* U1 = MODE == 1 ? bf.u1 + slice_u : nullptr;
   const float* src = MODE == 2 ? ones : in + s.off + i3 * n12 + (long)i * n1;
   const FactorLayout f = factor_layout<NW>(bf, s);
-  const long cl = dir * f.ntr_s + q, yss = 2 * f.ntr_s;
+  const long cl = dir * f.ntp + q, yss = 2 * f.ntp;
   auto slot = [&](float* base, int k, int sl) { return base + ((long)k * b.np + sl) * n1; };
   const int ns = b.ns;
   if (dir == 0) {
@@ -142,12 +157,12 @@ __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict
     float* out = slot(U, ip, sl);
     if (MODE == 1) {
       float* outb = slot(U1, ip, sl);
-      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, ps, out,
+      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntp, dir == 1, prev, ps, out,
                               f.y + cl, f.yb + cl, yss, apply_ring + threadIdx.x, blockDim.x,
                               prevb, ps, outb);
       prevb = f.yb + cl;
     } else {
-      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntr_s, dir == 1, prev, ps, out,
+      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntp, dir == 1, prev, ps, out,
                                f.y + cl, nullptr, yss, apply_ring + threadIdx.x, blockDim.x);
     }
     prev = f.y + cl;
@@ -291,13 +306,13 @@ enum Filter { kMean = 1, kMeanAdj = 2, kMedian = 3 };
 
 struct SprayLayout {
   int ntiles;
-  long ntr, nu, nscr, n1max, nsamp;
+  long ntr, ntp, nu, nscr, n1max, nsamp;
 };
 
 SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
   SprayLayout L{};
   const int np = 2 * ns + 1, nb = 2 * order;
-  long u = 0, sc = 0, tr = 0, samp = 0;
+  long u = 0, sc = 0, tr = 0, tp = 0, samp = 0;
   int tiles = 0;
   for (auto& s : secs) {
     s.n = (long)s.n1 * s.n2 * s.n3;
@@ -306,19 +321,25 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
     tiles += s.ntile;
     s.tr0 = tr;
     tr += (long)s.n2 * s.n3;
+    s.tp0 = tp;
+    tp += padded_traces((long)s.n2 * s.n3);
     s.u0 = u;
     u += s.n * np;
     s.sc0 = sc;
     const long plane = (long)s.n1 * s.n2 * s.n3;
-    // factor store + chain scratch, or the adjoint mean's per-chain scratch
-    // (o, d, y for 2 n2 n3 chains), whichever is larger
+    const long pplane = (long)s.n1 * padded_traces((long)s.n2 * s.n3);
+    // factor store + chain scratch (padded traces), or the adjoint mean's
+    // per-chain scratch (o, d, y for 2 n2 n3 chains), whichever is larger;
+    // every section's store starts on a 128-byte boundary
     sc += std::max((long)(nb + 2) * 2 * plane,
-                   (long)(2 * order + 1 + 2 * (nb + 1)) * plane + 4 * plane);
+                   (long)(2 * order + 1 + 2 * (nb + 1)) * pplane + 4 * pplane);
+    sc = (sc + 31) / 32 * 32;
     samp = std::max(samp, s.off + s.n);
     L.n1max = std::max(L.n1max, (long)s.n1);
   }
   L.ntiles = tiles;
   L.ntr = tr;
+  L.ntp = tp;
   L.nu = u;
   L.nscr = sc;
   L.nsamp = samp;
@@ -359,7 +380,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                int ns, float eps, cudaStream_t st) {
   const int nsec = (int)secs.size();
   const ApCoef c = make_apcoef(NW);
-  SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, ns, 2 * ns + 1, eps * eps, eps * eps};
+  SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, L.ntp, ns, 2 * ns + 1, eps * eps, eps * eps};
   const int bs = 64;
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
@@ -371,9 +392,10 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   if (w.bf.u1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
     return PWD_ECUDA;
   const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
-  const unsigned gap = (unsigned)(((L.ntr + 31) / 32 * 64 + bs - 1) / bs);
+  const unsigned gfa = (unsigned)((L.ntp + bs - 1) / bs);
+  const unsigned gap = (unsigned)((2 * L.ntp + bs - 1) / bs);
   const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
-  PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gtr, bs, 0, st>>>(dip, w.bf, b, c));
+  PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gfa, bs, 0, st>>>(dip, w.bf, b, c));
   if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
