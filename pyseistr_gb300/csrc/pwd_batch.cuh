@@ -22,6 +22,7 @@ struct SecDesc {
   long u0;        // spray: offset of the section's sprayed panels
   long sc0;       // spray: offset of the section's per-chain scratch
   long tp0;       // spray: first trace in the numbering padded to 32 per section
+  int cord;       // spray: the section at this position of the padded numbering
 };
 
 // Section holding global item g, given each section's first item (sorted).

@@ -86,11 +86,14 @@ __device__ __forceinline__ FactorLayout factor_layout(const SprayBufs& bf, const
 }
 
 // The section of padded trace g and its trace q there (q >= n2 n3 is
-// padding).
+// padding).  The padded numbering takes the sections longest traces first
+// (position k holds section secs[k].cord), so that the long chains start
+// in the first waves and the short ones fill the last.
 __device__ __forceinline__ const SecDesc& padded_section(const SprayB& b, long g, long& q) {
-  const int si = find_section(b.nsec, g, [&](int k) { return b.secs[k].tp0; });
-  q = g - b.secs[si].tp0;
-  return b.secs[si];
+  const int k = find_section(b.nsec, g, [&](int p) { return b.secs[b.secs[p].cord].tp0; });
+  const SecDesc& s = b.secs[b.secs[k].cord];
+  q = g - s.tp0;
+  return s;
 }
 
 // Taps and factors of every trace of the batch: thread per padded trace.
@@ -321,8 +324,6 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
     tiles += s.ntile;
     s.tr0 = tr;
     tr += (long)s.n2 * s.n3;
-    s.tp0 = tp;
-    tp += padded_traces((long)s.n2 * s.n3);
     s.u0 = u;
     u += s.n * np;
     s.sc0 = sc;
@@ -336,6 +337,17 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
     sc = (sc + 31) / 32 * 32;
     samp = std::max(samp, s.off + s.n);
     L.n1max = std::max(L.n1max, (long)s.n1);
+  }
+  // padded chain numbering: sections by decreasing trace length
+  std::vector<int> ord(secs.size());
+  for (size_t k = 0; k < ord.size(); k++) ord[k] = (int)k;
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int a, int c) { return secs[a].n1 > secs[c].n1; });
+  for (size_t k = 0; k < ord.size(); k++) {
+    SecDesc& s = secs[ord[k]];
+    s.tp0 = tp;
+    tp += padded_traces((long)s.n2 * s.n3);
+    secs[k].cord = ord[k];
   }
   L.ntiles = tiles;
   L.ntr = tr;
