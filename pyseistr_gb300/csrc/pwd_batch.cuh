@@ -16,6 +16,8 @@ struct SecDesc {
   int nftile;     // column-strip tiles of the section
   int ctile0;     // first row-segment tile (mixed-mode slope estimation)
   int nctile;     // row-segment tiles of the section
+  int gtile0;     // first axis-2 strip tile (mixed mode, cubes)
+  int ngtile;     // axis-2 strip tiles of the section (0 unless n3 > 1)
   long line0[3];  // first global triangle line of each smoothed axis
   long scr0[3];   // triangle scratch offset of each smoothed axis
   long tr0;       // spray: first global trace (n2*n3 traces per section)

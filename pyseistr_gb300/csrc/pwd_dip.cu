@@ -1077,25 +1077,30 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
     if (j0 + u < len) out[u] = res[u];
 }
 
-// Axis 1 of the mixed-mode smoothing with the CG output operation: one
+// Axis 1 of the mixed-mode smoothing with the CG output operation (AX =
+// 1), or axis 2 of a cube (AX = 2: the cube seen as a section of n1 n2
+// samples by n3 traces, whose axis 1 is the cube's axis 2): one
 // thread per column of a strip of kSmStrip columns by up to kSmB2 rows
 // streams down the rows (its input column, mirrored at the section's first
 // and last traces, staged kSmStages - 1 rows ahead by cp.async together with
 // the output operands), keeps the last 2 nb1 - 1 rows (in registers for a
 // compiled radius, in a shared-memory ring otherwise) and forms each output
 // row's axis-1 sum.  Threads share nothing until the closing reductions.
-template <int OUT, int NB1>
+template <int OUT, int NB1, int AX = 1>
 __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b, SmParams q) {
   extern __shared__ float sm[];
   const int t = blockIdx.x;
-  const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
+  const int si = find_section(b.nsec, (long)t, [&](int k) {
+    return (long)(AX == 1 ? b.secs[k].ftile0 : b.secs[k].gtile0);
+  });
   const SecDesc& s = b.secs[si];
   if (!sm_selected(q.sel, s)) return;
   DipScalars* S = b.S + si;
   if (S->cg_done) return;
-  const int n1 = s.n1, n2 = s.n2;
+  const int tile0 = AX == 1 ? s.ftile0 : s.gtile0, ntile = AX == 1 ? s.nftile : s.ngtile;
+  const int n1 = AX == 1 ? s.n1 : s.n1 * s.n2, n2 = AX == 1 ? s.n2 : s.n3;
   const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + kSmB2 - 1) / kSmB2;
-  const int lt = t - s.ftile0;
+  const int lt = t - tile0;
   const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
   const int o2 = t2 * kSmB2;
   const int rows = min(kSmB2, n2 - o2);
@@ -1103,7 +1108,8 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
   const int j = threadIdx.x;
   const int g1 = t1 * kSmStrip + j;
   const bool colok = g1 < n1;
-  const int nb1 = NB1 > 0 ? NB1 : q.nb1, h1 = nb1 - 1;
+  const int nb1 = NB1 > 0 ? NB1 : (AX == 1 ? q.nb1 : q.nb2), h1 = nb1 - 1;
+  const float wt = AX == 1 ? q.wt1 : q.wt2;
   const float st = (OUT == SM_OUT_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
   const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
   // staging slot: [6][kSmStrip] = input, then 5 output operands
@@ -1192,12 +1198,12 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
       if (step >= 2 * h1) {
         int c = slot - h1;
         if (c < 0) c += RING;
-        float acc = __fmul_rn(tri_tap(0, nb1, q.wt1), sring[c * kSmStrip + j]);
+        float acc = __fmul_rn(tri_tap(0, nb1, wt), sring[c * kSmStrip + j]);
         int lo = c, hi = c;
         for (int k = 1; k <= h1; k++) {
           lo = lo == 0 ? RING - 1 : lo - 1;
           hi = hi == RING - 1 ? 0 : hi + 1;
-          acc = __fmaf_rn(tri_tap(k, nb1, q.wt1),
+          acc = __fmaf_rn(tri_tap(k, nb1, wt),
                           __fadd_rn(sring[lo * kSmStrip + j], sring[hi * kSmStrip + j]), acc);
         }
         out_op(step - 2 * h1, acc);
@@ -1209,57 +1215,14 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
   if (OUT == SM_OUT_CG1) {
     dvec<1> acc = {{co.a0.value()}};
     dvec<1> tot;
-    if (tiles_sum_last<1>(acc, b.partials, t, s.ftile0, s.nftile, &S->cnt[2], tot) &&
+    if (tiles_sum_last<1>(acc, b.partials, t, tile0, ntile, &S->cnt[2], tot) &&
         threadIdx.x == 0)
       cg1_finish(S, tot.v[0], q.iter);
   } else if (OUT == SM_OUT_CG2) {
     dvec<3> acc = {{co.a0.value(), co.a1.value(), co.a2.value()}};
     dvec<3> tot;
-    if (tiles_sum_last<3>(acc, b.partials, t, s.ftile0, s.nftile, &S->cnt[3], tot) &&
+    if (tiles_sum_last<3>(acc, b.partials, t, tile0, ntile, &S->cnt[3], tot) &&
         threadIdx.x == 0)
-      cg2_finish(S, tot, q.iter);
-  }
-}
-
-// Smoothing along axis 2 (cubes), elementwise tiles, with the CG output
-// operation.
-template <int OUT>
-__global__ void k_smooth3(DipArrays a, DipBatch b, SmParams q) {
-  const int t = blockIdx.x;
-  const TileRange tr = tile_range(b, t);
-  const SecDesc& s = b.secs[tr.sec];
-  DipScalars* S = b.S + tr.sec;
-  if (!sm_selected(q.sel, s) || S->cg_done) return;
-  const int n3 = s.n3, h2 = q.nb2 - 1;
-  const long n12 = (long)s.n1 * s.n2;
-  const float st = (OUT == SM_OUT_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
-  const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
-  const float* src = q.in + s.off;
-  CgOut co;
-  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
-    const int i3 = (int)(j / n12);
-    const long rem = j - (long)i3 * n12;
-    float acc = __fmul_rn(tri_tap(0, q.nb2, q.wt2), src[j]);
-    for (int k = 1; k <= h2; k++) {
-      const float lo = src[rem + n12 * mirror_idx(i3 - k, n3)];
-      const float hi = src[rem + n12 * mirror_idx(i3 + k, n3)];
-      acc = __fmaf_rn(tri_tap(k, q.nb2, q.wt2), __fadd_rn(lo, hi), acc);
-    }
-    const long i = s.off + j;
-    if (OUT == SM_OUT_CG1)
-      co.cg1(a, i, acc, st, q.iter);
-    else
-      co.cg2(a, i, acc, q.gpc[i], al, q.iter);
-  }
-  if (OUT == SM_OUT_CG1) {
-    dvec<1> acc = {{co.a0.value()}};
-    dvec<1> tot;
-    if (sec_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0)
-      cg1_finish(S, tot.v[0], q.iter);
-  } else {
-    dvec<3> acc = {{co.a0.value(), co.a1.value(), co.a2.value()}};
-    dvec<3> tot;
-    if (sec_sum_last<3>(acc, b, t, s, &S->cnt[3], tot) && threadIdx.x == 0)
       cg2_finish(S, tot, q.iter);
   }
 }
@@ -1272,6 +1235,7 @@ struct DipLayout {
   int ntiles;
   int nftiles;  // column-strip tiles (mixed mode)
   int nctiles;  // row-segment tiles (mixed mode)
+  int ngtiles;  // axis-2 strip tiles of cubes (mixed mode)
   long scr_total;
   long nlines[3];
   bool any3d, any2d;
@@ -1293,6 +1257,10 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
     s.ftile0 = L.nftiles;
     s.nftile = ((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
     L.nftiles += s.nftile;
+    s.gtile0 = L.ngtiles;
+    s.ngtile = s.n3 > 1 ? ((s.n1 * s.n2 + kSmStrip - 1) / kSmStrip) * ((s.n3 + kSmB2 - 1) / kSmB2)
+                        : 0;
+    L.ngtiles += s.ngtile;
     s.ctile0 = L.nctiles;
     s.nctile = conv0_tiles(s.n1, (long)s.n2 * s.n3, std::max(rect[0], 1) - 1);
     L.nctiles += s.nctile;
@@ -1349,7 +1317,8 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.secs = cv.take<SecDesc>(nsec);
   w.tile_sec = cv.take<int>(L.ntiles);
   w.S = cv.take<DipScalars>(nsec);
-  w.partials = cv.take<double>((size_t)std::max(L.ntiles, mixed ? L.nftiles : 0) * 3);
+  w.partials = cv.take<double>(
+      (size_t)std::max(L.ntiles, mixed ? std::max(L.nftiles, L.ngtiles) : 0) * 3);
   *total = cv.size();
   return w;
 }
@@ -1417,11 +1386,11 @@ SmKernel conv0_kernel(int nb) {
   if (nb == 5) return k_conv0<IN, 5>;
   return k_conv0<IN, 0>;
 }
-template <int OUT>
+template <int OUT, int AX = 1>
 SmKernel conv1_kernel(int nb) {
-  if (nb == 10) return k_conv1<OUT, 10>;
-  if (nb == 5) return k_conv1<OUT, 5>;
-  return k_conv1<OUT, 0>;
+  if (nb == 10) return k_conv1<OUT, 10, AX>;
+  if (nb == 5) return k_conv1<OUT, 5, AX>;
+  return k_conv1<OUT, 0, AX>;
 }
 
 // Mixed mode of dip3: FP32 filter taps, the fused smoothing passes of the
@@ -1439,7 +1408,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   q.wt2 = (float)(1.0 / ((double)q.nb2 * q.nb2));
   const bool ax2 = q.nb2 > 1 && L.any3d;
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
-  const unsigned gc = (unsigned)L.nctiles;
+  const unsigned gc = (unsigned)L.nctiles, gg = (unsigned)L.ngtiles;
   q.c0map = a.c0map;
   q.c0buf = conv0_buffer(q.nb0 - 1);
   const size_t smem0 = sizeof(float) * q.c0buf, smem0cg = 5 * smem0;
@@ -1454,6 +1423,14 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   cudaFuncSetAttribute(c0_arr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
   for (SmKernel k : {c1_cg1, c1_cg2, c1_arr})
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  // axis 2 of cubes: the axis-1 kernel on the (n1 n2) x n3 view
+  const bool ring2 = !(q.nb2 == 10 || q.nb2 == 5);
+  const size_t smem2 = sizeof(float) * (kSmStages * 6 * kSmStrip +
+                                        (ring2 ? (2 * q.nb2 - 1) * kSmStrip : 0));
+  const SmKernel c2_cg1 = conv1_kernel<SM_OUT_CG1, 2>(q.nb2),
+                 c2_cg2 = conv1_kernel<SM_OUT_CG2, 2>(q.nb2);
+  for (SmKernel k : {c2_cg1, c2_cg2})
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
   float* X[2] = {a.dp, a.x2};
   float* Rv[2] = {a.r, a.r2};
   PWD_KERNEL(PWD_FAM_OTHER, st,
@@ -1493,8 +1470,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
         q.out = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
         q.in = a.t2;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   k_smooth3<SM_OUT_CG1><<<gt, kTileThreads, 0, st>>>(a, b, q));
+        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg1<<<gg, kSmStrip, smem2, st>>>(a, b, q)));
         q.in = a.gp;
         q.out = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
@@ -1503,8 +1479,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
         q.in = a.t2;
         q.gpc = a.gp;
-        PWD_KERNEL(PWD_FAM_CG, st,
-                   k_smooth3<SM_OUT_CG2><<<gt, kTileThreads, 0, st>>>(a, b, q));
+        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg2<<<gg, kSmStrip, smem2, st>>>(a, b, q)));
       }
     }
     DipArrays af = a;  // x and r after the last iteration
