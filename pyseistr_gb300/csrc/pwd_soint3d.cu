@@ -246,6 +246,9 @@ __device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, long 
 // The same without drift: every "+" row (m - st - is) precedes every "-"
 // row (m + is), because a valid row has st > 2 NW nj, so the scatter order
 // is the "+" terms with iw descending, then the "-" terms with iw ascending.
+// All rows' validity, residual and tap are loaded first (indices clamped
+// into the patch), then the valid terms are added in that order: the same
+// additions as a loop that tests each row before loading it.
 template <int NW>
 __device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ y, long m,
                                                       long st, int nj,
@@ -253,16 +256,26 @@ __device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ 
                                                       const uint8_t* __restrict__ v, long n,
                                                       float acc) {
   constexpr int NA = 2 * NW + 1;
+  float yv[2 * NA], fv[2 * NA];
+  bool ok[2 * NA];
 #pragma unroll
-  for (int iw = NA - 1; iw >= 0; iw--) {
-    const long i = m - st - (long)(iw - NW) * nj;
-    if (i >= 0 && i < n && v[i]) acc = __fadd_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
+  for (int k = 0; k < 2 * NA; k++) {
+    // k < NA: "+" term iw = NA-1-k at row m - st - is; else "-" term iw = k-NA at m + is
+    const int iw = k < NA ? NA - 1 - k : k - NA;
+    const long is = (long)(iw - NW) * nj;
+    const long i = k < NA ? m - st - is : m + is;
+    const bool in = i >= 0 && i < n;
+    const long ic = in ? i : m;
+    ok[k] = in && v[ic];
+    yv[k] = y[ic];
+    fv[k] = f[iw * n + ic];
   }
 #pragma unroll
-  for (int iw = 0; iw < NA; iw++) {
-    const long i = m + (long)(iw - NW) * nj;
-    if (i >= 0 && i < n && v[i]) acc = __fsub_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
-  }
+  for (int k = 0; k < NA; k++)
+    if (ok[k]) acc = __fadd_rn(acc, __fmul_rn(yv[k], fv[k]));
+#pragma unroll
+  for (int k = NA; k < 2 * NA; k++)
+    if (ok[k]) acc = __fsub_rn(acc, __fmul_rn(yv[k], fv[k]));
   return acc;
 }
 
