@@ -174,16 +174,26 @@ __global__ void k_ap3_fwd(const float* __restrict__ xxb, float* __restrict__ yyb
       float* y = yy + (part == 0 ? 0 : g.n);
       float acc = add ? y[i] : 0.f;
       const uint8_t ok = (part == 0 ? A.v1 : A.v2)[s.off + i];
-      if (ok) {
-        const long st = part == 0 ? g.nx : (long)g.nx * g.ny;
-        const int nj = part == 0 ? g.nj1 : g.nj2;
-        const int id = (part == 0 ? A.id1 : A.id2)[s.off + i];
-        const float* f = (part == 0 ? A.f1 : A.f2) + NA * s.off;
+      const long st = part == 0 ? g.nx : (long)g.nx * g.ny;
+      const int nj = part == 0 ? g.nj1 : g.nj2;
+      // the shifts are all 0 without drift
+      const int id = g.drift ? (part == 0 ? A.id1 : A.id2)[s.off + i] : 0;
+      const float* f = (part == 0 ? A.f1 : A.f2) + NA * s.off;
+      // operands loaded before the row's validity is known (indices clamped
+      // into the patch; a valid row's are in range), added only if valid
+      float xa[NA], xb[NA], fv[NA];
 #pragma unroll
-        for (int iw = 0; iw < NA; iw++) {
-          int is = (iw - NW) * nj;
-          acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(xx[i + st + is], xx[i - is - id]), f[iw * g.n + i]));
-        }
+      for (int iw = 0; iw < NA; iw++) {
+        const long is = (long)(iw - NW) * nj;
+        const long ia = i + st + is, ib = i - is - id;
+        xa[iw] = xx[ia < 0 ? 0 : (ia >= g.n ? g.n - 1 : ia)];
+        xb[iw] = xx[ib < 0 ? 0 : (ib >= g.n ? g.n - 1 : ib)];
+        fv[iw] = f[iw * g.n + i];
+      }
+      if (ok) {
+#pragma unroll
+        for (int iw = 0; iw < NA; iw++)
+          acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(xa[iw], xb[iw]), fv[iw]));
       }
       y[i] = acc;
     }
