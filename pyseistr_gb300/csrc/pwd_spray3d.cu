@@ -5,8 +5,11 @@
 // update_init/get_update (:980-1056).  Each source trace's spray is a tree
 // over the offset grid visited by increasing distance, every cell predicted
 // from one or two already-predicted neighbours (predict1_step /
-// predict2_step); one GPU thread runs one source's tree.  The visit table
-// depends only on (r1, r2) and is built on the host and passed by value.
+// predict2_step).  A cell's neighbours are strictly closer to the source, so
+// the cells of one distance (a level) are independent: a group of lanes runs
+// one source's tree, one cell of the current level per lane, the levels in
+// order with a warp barrier between them.  The visit table and its levels
+// depend only on (r1, r2) and are built on the host and passed by value.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -22,8 +25,10 @@ constexpr int kMaxCells = (2 * kMaxR + 1) * (2 * kMaxR + 1);
 
 struct Visit3 {
   int np, np2, np3, ns2, ns3;
+  int nlev, maxlev;             // levels of equal distance, largest level
   short jp[kMaxCells];
   unsigned char fl[kMaxCells];  // bits 0-1 update, bit 2 up2, bit 3 up3
+  short lev0[kMaxCells + 1];    // first visit index of each level
 };
 
 // update_init + get_update, evaluated once per cell.
@@ -65,7 +70,23 @@ Visit3 make_visit(int ns2, int ns3) {
     v.jp[i] = (short)j;
     v.fl[i] = (unsigned char)(update | (up1 ? 4 : 0) | (up2 ? 8 : 0));
   }
+  // levels: runs of equal distance in the visit order (a neighbour used by
+  // get_update is strictly closer, so it lies in an earlier level)
+  v.nlev = 0;
+  v.maxlev = 0;
+  for (int i = 0; i < v.np; i++)
+    if (i == 0 || t0[visit[i]] != t0[visit[i - 1]]) v.lev0[v.nlev++] = (short)i;
+  v.lev0[v.nlev] = (short)v.np;
+  for (int l = 0; l < v.nlev; l++) v.maxlev = std::max(v.maxlev, v.lev0[l + 1] - v.lev0[l]);
   return v;
+}
+
+// Lanes per source: the largest level rounded up to a power of two, at
+// least 4 (levels hold at most 16 cells for radii up to kMaxR).
+int spray3_lanes(const Visit3& v) {
+  int l = 4;
+  while (l < v.maxlev) l *= 2;
+  return l;
 }
 
 struct Spray3 {
@@ -73,66 +94,80 @@ struct Spray3 {
   float eps, eps2;
 };
 
-// One source trace's spray tree (csomean3d :1466-1520).
+// One source trace's spray tree (csomean3d :1466-1520) on lps lanes: lane
+// k of the group predicts cell k of each level.  Every lane of a warp runs
+// every level (lanes without a source or a cell only meet the barriers), so
+// a cell's neighbours, predicted by other lanes of the group in earlier
+// levels, are complete and visible when it reads them.
 template <int NW>
-__global__ void k_spray3_tree(const float* __restrict__ din, const float* __restrict__ p1,
-                              const float* __restrict__ p2, float* __restrict__ u, Spray3 s,
-                              Visit3 v, ApCoef c, PredictScratch sc) {
+__global__ void __launch_bounds__(128) k_spray3_tree(const float* __restrict__ din,
+                                                     const float* __restrict__ p1,
+                                                     const float* __restrict__ p2,
+                                                     float* __restrict__ u, Spray3 s, Visit3 v,
+                                                     ApCoef c, PredictScratch sc, int lps) {
   const long n23 = (long)s.n2 * s.n3;
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= n23) return;
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long i = gt / lps;
+  const int lane = (int)(gt - i * lps);
+  const bool src_ok = i < n23;
   const int n1 = s.n1, np = v.np, np2 = v.np2;
-  PredictScratch my = sc;
-  my.o += i;
-  my.d += i;
-  my.y += i;
+  PredictScratch my = sc;  // one scratch column per lane of the grid
+  my.o += gt;
+  my.d += gt;
+  my.y += gt;
   auto U = [&](long tr, int slot) { return u + (tr * np + slot) * (long)n1; };
-  {
+  if (src_ok) {
     float* cen = U(i, v.ns3 * np2 + v.ns2);
-    for (int j = 0; j < n1; j++) cen[j] = din[i * n1 + j];
+    for (int j = lane; j < n1; j += lps) cen[j] = din[i * n1 + j];
   }
-  const int i2 = (int)(i % s.n2), i3 = (int)(i / s.n2);
-  for (int ip = 0; ip < np; ip++) {
-    const int jp = v.jp[ip];
-    const int fl = v.fl[ip];
-    const int update = fl & 3;
-    const bool up2 = (fl & 4) != 0, up3 = (fl & 8) != 0;
-    if (update == 0) continue;
-    int k2 = jp % np2, k3 = jp / np2;
-    int j2 = i2 + k2 - v.ns2, j3 = i3 + k3 - v.ns3;
-    if (j2 < 0 || j2 >= s.n2 || j3 < 0 || j3 >= s.n3) continue;
-    const long j = j2 + (long)j3 * s.n2;
-    float* trace = U(j, jp);
-    long t2 = 0, t3 = 0;
-    int s2 = 0, s3 = 0;
-    const float *q2 = nullptr, *q3 = nullptr;
-    if (update & 1) {
-      if (up2) {
-        if (j2 == 0) continue;
-        t2 = j - 1; q2 = p1 + t2 * n1; s2 = jp - 1;
-      } else {
-        if (j2 == s.n2 - 1) continue;
-        t2 = j + 1; q2 = p1 + j * n1; s2 = jp + 1;
+  __syncwarp();
+  const int i2 = src_ok ? (int)(i % s.n2) : 0, i3 = src_ok ? (int)(i / s.n2) : 0;
+  for (int lv = 0; lv < v.nlev; lv++) {
+    const int ip = v.lev0[lv] + lane;
+    if (src_ok && ip < v.lev0[lv + 1]) {
+      const int jp = v.jp[ip];
+      const int fl = v.fl[ip];
+      const int update = fl & 3;
+      const bool up2 = (fl & 4) != 0, up3 = (fl & 8) != 0;
+      const int k2 = jp % np2, k3 = jp / np2;
+      const int j2 = i2 + k2 - v.ns2, j3 = i3 + k3 - v.ns3;
+      bool go = update != 0 && j2 >= 0 && j2 < s.n2 && j3 >= 0 && j3 < s.n3;
+      const long j = j2 + (long)j3 * s.n2;
+      long t2 = 0, t3 = 0;
+      int s2 = 0, s3 = 0;
+      const float *q2 = nullptr, *q3 = nullptr;
+      if (go && (update & 1)) {
+        if (up2) {
+          if (j2 == 0) go = false;
+          t2 = j - 1; q2 = p1 + t2 * n1; s2 = jp - 1;
+        } else {
+          if (j2 == s.n2 - 1) go = false;
+          t2 = j + 1; q2 = p1 + j * n1; s2 = jp + 1;
+        }
+      }
+      if (go && (update & 2)) {
+        if (up3) {
+          if (j3 == 0) go = false;
+          t3 = j - s.n2; q3 = p2 + t3 * n1; s3 = jp - np2;
+        } else {
+          if (j3 == s.n3 - 1) go = false;
+          t3 = j + s.n2; q3 = p2 + j * n1; s3 = jp + np2;
+        }
+      }
+      if (go) {
+        float* trace = U(j, jp);
+        if (update == 1)
+          predict_fwd<NW, false>(n1, s.eps, s.eps2, c, U(t2, s2), q2, up2, nullptr, nullptr,
+                                 false, trace, my);
+        else if (update == 2)
+          predict_fwd<NW, false>(n1, s.eps, s.eps2, c, U(t3, s3), q3, up3, nullptr, nullptr,
+                                 false, trace, my);
+        else
+          predict_fwd<NW, true>(n1, s.eps, s.eps2, c, U(t2, s2), q2, up2, U(t3, s3), q3, up3,
+                                trace, my);
       }
     }
-    if (update & 2) {
-      if (up3) {
-        if (j3 == 0) continue;
-        t3 = j - s.n2; q3 = p2 + t3 * n1; s3 = jp - np2;
-      } else {
-        if (j3 == s.n3 - 1) continue;
-        t3 = j + s.n2; q3 = p2 + j * n1; s3 = jp + np2;
-      }
-    }
-    if (update == 1)
-      predict_fwd<NW, false>(n1, s.eps, s.eps2, c, U(t2, s2), q2, up2, nullptr, nullptr, false,
-                             trace, my);
-    else if (update == 2)
-      predict_fwd<NW, false>(n1, s.eps, s.eps2, c, U(t3, s3), q3, up3, nullptr, nullptr, false,
-                             trace, my);
-    else
-      predict_fwd<NW, true>(n1, s.eps, s.eps2, c, U(t2, s2), q2, up2, U(t3, s3), q3, up3, trace,
-                            my);
+    __syncwarp();
   }
 }
 
@@ -141,19 +176,23 @@ struct Spray3Work {
   PredictScratch sc;
 };
 
+// Threads of the tree launch: LPS lanes per source, blocks of 128.
+long spray3_threads(long n23, int lanes) { return (n23 * lanes + 127) / 128 * 128; }
+
 Spray3Work carve_spray3(void* ws, int n1, int n2, int n3, int r1, int r2, int order,
                         bool need_svmf, size_t* total) {
   const long n23 = (long)n2 * n3;
   const int np = (2 * r1 + 1) * (2 * r2 + 1), nb = 2 * order;
+  const long nthr = spray3_threads(n23, spray3_lanes(make_visit(r1, r2)));
   Carver cv(ws);
   Spray3Work w;
   w.u = cv.take<float>(n23 * np * n1);
   w.v2 = need_svmf ? cv.take<float>(n23 * np * n1) : nullptr;
   w.avg = need_svmf ? cv.take<float>(n23) : nullptr;
-  w.sc.o = cv.take<float>((long)nb * n1 * n23);
-  w.sc.d = cv.take<float>((long)n1 * n23);
-  w.sc.y = cv.take<float>((long)n1 * n23);
-  w.sc.ss = n23;
+  w.sc.o = cv.take<float>((long)nb * n1 * nthr);
+  w.sc.d = cv.take<float>((long)n1 * nthr);
+  w.sc.y = cv.take<float>((long)n1 * nthr);
+  w.sc.ss = nthr;
   *total = cv.size();
   return w;
 }
@@ -174,15 +213,17 @@ int spray3(const float* d, const float* p1, const float* p2, const Spray3Work& w
   s.eps = 0.01f * 0.01f;  // csomean3d/csomf3d force eps=0.01 (:1402, :1586)
   s.eps2 = s.eps;
   const Visit3 v = make_visit(r1, r2);
-  const int b = 64;
-  const unsigned g = (unsigned)((n23 + b - 1) / b);
+  const int lanes = spray3_lanes(v);  // 4, 8 or 16: lane groups never straddle warps
+  const unsigned g = (unsigned)(spray3_threads(n23, lanes) / 128);
+  int rc = PWD_OK;
   switch (order) {
-    case 1: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<1><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(1), w.sc)); break;
-    case 2: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<2><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(2), w.sc)); break;
-    case 3: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<3><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(3), w.sc)); break;
-    case 4: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<4><<<g, b, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(4), w.sc)); break;
-    default: return PWD_ENOTSUP;
+    case 1: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<1><<<g, 128, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(1), w.sc, lanes)); break;
+    case 2: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<2><<<g, 128, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(2), w.sc, lanes)); break;
+    case 3: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<3><<<g, 128, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(3), w.sc, lanes)); break;
+    case 4: PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray3_tree<4><<<g, 128, 0, st>>>(d, p1, p2, w.u, s, v, make_apcoef(4), w.sc, lanes)); break;
+    default: rc = PWD_ENOTSUP;
   }
+  if (rc != PWD_OK) return rc;
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
