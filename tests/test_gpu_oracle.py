@@ -60,6 +60,21 @@ def test_somf3d_r4(ps, O):
     assert np.array_equal(ps.somf3dc(c, pi, px, 4, 4, 0.01, 2), O.somf3d(c, pi, px, 4, 4, 2))
 
 
+@pytest.mark.parametrize("r1,r2", [(5, 5), (6, 2), (3, 0)])
+def test_somean3d_somf3d_radii_lane_groups(ps, O, r1, r2):
+    """The 3-D spray runs each distance level of a source's tree on a group
+    of 4, 8 or 16 lanes, set by the largest level: radius (5, 5) has a
+    level of 12 cells (16 lanes), (6, 2) 8 lanes, (3, 0) 4 lanes."""
+    import workloads
+
+    c = workloads.plain3d()[:40, :14, :13].copy()
+    pi, px = O.dip3d(c, 2, 4, 2, (3, 3, 3))
+    assert np.array_equal(ps.somean3dc(c, pi, px, r1, r2, 0.01, 2),
+                          O.somean3d(c, pi, px, r1, r2, 2))
+    assert np.array_equal(ps.somf3dc(c, pi, px, r1, r2, 0.01, 2),
+                          O.somf3d(c, pi, px, r1, r2, 2))
+
+
 def test_median_selection_bit_exact_on_reference_spray(O):
     """The GPU median of sprayed panels equals the reference's quickselect
     when both are given the same (oracle-sprayed) values, including exact
