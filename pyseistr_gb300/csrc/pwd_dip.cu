@@ -696,10 +696,10 @@ __global__ void k_zero_slopes(float* __restrict__ p, DipBatch b) {
   }
 }
 
-__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsec) return;
-  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int ntiles, int* tile_sec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  tile_sec[t] = find_section(nsec, (long)t, [&](int k) { return (long)secs[k].tile0; });
 }
 
 __global__ void k_put_single(SecDesc* dst, SecDesc v) { *dst = v; }
@@ -1518,7 +1518,7 @@ int dip_enqueue(const float* data, const float* mask, float* out, const DipLayou
                 const DipWork& w, int nsec, int niter, int liter, int order, const int rect[3],
                 cudaStream_t st, bool mixed = false) {
   PWD_KERNEL(PWD_FAM_OTHER, st,
-             k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
+             k_tile_map<<<(unsigned)((L.ntiles + 255) / 256), 256, 0, st>>>(w.secs, nsec, L.ntiles, w.tile_sec));
   if (cudaMemsetAsync(w.S, 0, sizeof(DipScalars) * nsec, st) != cudaSuccess) return PWD_ECUDA;
   DipBatch b{w.secs, w.tile_sec, nsec, L.ntiles, w.S, w.partials};
   DipArrays a = w.a;

@@ -315,9 +315,10 @@ struct PredictFactor {
 };
 
 // Taps and both factors of one slope trace pp (the band and LDL' steps of
-// predict_fwd with one filter, for the two orientations side by side).
+// predict_fwd with one filter, for the two orientations side by side, the
+// taps of each column evaluated once for both).
 template <int NW>
-__device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
+__device__ void predict_factor_pair(int n1, float eps, float eps2, const ApCoef& c,
                                const float* __restrict__ pp, const PredictFactor& F) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
   const RegConst rc = reg_const(eps, eps2);
@@ -389,6 +390,69 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
 #pragma unroll
       for (int q = 0; q < NB; q++) O[0][q] = ok[q];
     }
+  }
+}
+
+// One factor of slope trace pp (the band and LDL' steps of predict_fwd with
+// one filter): side 0 the unreversed filter (forw = false, into F.f0, also
+// storing the taps), side 1 the reversed one (F.f1).  The two sides are
+// independent and run on two threads.
+template <int NW>
+__device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
+                               const float* __restrict__ pp, const PredictFactor& F, int side) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
+  const RegConst rc = reg_const(eps, eps2);
+  FilterWin<NW> w;
+  float O[NB][NB], D[NB];
+#pragma unroll
+  for (int cc = 0; cc < NA; cc++)
+#pragma unroll
+    for (int j = 0; j < NA; j++) w.a[cc][j] = 0.f;
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    D[m] = 0.f;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[m][q] = 0.f;
+  }
+  float* f = side ? F.f1 : F.f0;
+  auto column = [&](int cn, float* col) {
+    float t[NA];
+    passfilter<NW>(c, pp[cn], t);
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+      if (side == 0) F.taps[((long)j * n1 + cn) * F.ss] = t[j];
+      col[j] = side ? t[NA - 1 - j] : t[j];
+    }
+  };
+#pragma unroll
+  for (int cc = 0; cc < NW; cc++)
+    if (cc < n1) column(cc, w.a[NW + 1 + cc]);
+  for (int i = 0; i < n1; i++) {
+    const int cn = i + NW;
+    shift_win<NW>(w);
+    if (cn < n1) {
+      column(cn, w.a[2 * NW]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < NA; j++) w.a[2 * NW][j] = 0.f;
+    }
+    float diag, offd[NB];
+    reg_row<NB>(i, n1, rc, diag, offd);
+    band_add<NW>(w, i, n1, diag, offd);
+    float dk, ok[NB];
+    ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);
+#pragma unroll
+    for (int m = 0; m < NB; m++) f[((long)m * n1 + i) * F.ss] = ok[m];
+    f[((long)NB * n1 + i) * F.ss] = dk;
+#pragma unroll
+    for (int m = NB - 1; m > 0; m--) {
+      D[m] = D[m - 1];
+#pragma unroll
+      for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
+    }
+    D[0] = dk;
+#pragma unroll
+    for (int q = 0; q < NB; q++) O[0][q] = ok[q];
   }
 }
 

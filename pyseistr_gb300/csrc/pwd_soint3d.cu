@@ -470,10 +470,10 @@ __global__ void k_rr0(SoArrays A, SoBatch b) {
   if (so_sum_last<1>(acc, b, t, s, &S->cnt[2], tot) && threadIdx.x == 0) S->rr0 = tot.v[0];
 }
 
-__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsec) return;
-  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int ntiles, int* tile_sec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  tile_sec[t] = find_section(nsec, (long)t, [&](int k) { return (long)secs[k].tile0; });
 }
 
 struct SoLayout {
@@ -598,8 +598,8 @@ int soint3_run(const SoArrays& A, const SoBatch& b, int niter, cudaStream_t st) 
   const unsigned gt = (unsigned)b.ntiles;
   const int bs = kTileThreads;
   PWD_KERNEL(PWD_FAM_OTHER, st,
-             k_tile_map<<<(b.nsec + 127) / 128, 128, 0, st>>>(b.secs, b.nsec,
-                                                              const_cast<int*>(b.tile_sec)));
+             k_tile_map<<<(unsigned)((b.ntiles + 255) / 256), 256, 0, st>>>(
+                 b.secs, b.nsec, b.ntiles, const_cast<int*>(b.tile_sec)));
   if (cudaMemsetAsync(b.S, 0, sizeof(SolveScalars) * b.nsec, st) != cudaSuccess) return PWD_ECUDA;
   PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_coef<NW><<<gt, bs, 0, st>>>(A, b, make_apcoef(NW)));
   if (b.drift) PWD_KERNEL(PWD_FAM_SOINT, st, k_max_shift<<<gt, bs, 0, st>>>(A, b));

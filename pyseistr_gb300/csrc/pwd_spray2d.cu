@@ -96,17 +96,26 @@ __device__ __forceinline__ const SecDesc& padded_section(const SprayB& b, long g
   return s;
 }
 
-// Taps and factors of every trace of the batch: thread per padded trace.
-template <int NW>
+// Taps and factors of every trace of the batch.  SPLIT: thread per (padded
+// trace, filter orientation), each warp 32 consecutive traces of one
+// orientation (batches of few traces, where a thread per trace would leave
+// SMs idle); otherwise thread per padded trace with both orientations
+// sharing the taps.
+template <int NW, bool SPLIT>
 __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, SprayB b, ApCoef c) {
-  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int side = SPLIT ? (int)((t >> 5) & 1) : 0;
+  const long g = SPLIT ? (t >> 6) * 32 + (t & 31) : t;
   if (g >= b.ntp) return;
   long q;
   const SecDesc& s = padded_section(b, g, q);
   if (q >= (long)s.n2 * s.n3) return;
   const FactorLayout f = factor_layout<NW>(bf, s);
   PredictFactor F{f.taps + q, f.f0 + q, f.f1 + q, f.ntp};
-  predict_factor<NW>(s.n1, b.eps, b.eps2, c, dip + s.off + q * s.n1, F);
+  if (SPLIT)
+    predict_factor<NW>(s.n1, b.eps, b.eps2, c, dip + s.off + q * s.n1, F, side);
+  else
+    predict_factor_pair<NW>(s.n1, b.eps, b.eps2, c, dip + s.off + q * s.n1, F);
 }
 
 // Forward spray with the stored factors.  Chains are numbered so that each
@@ -289,10 +298,10 @@ __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restr
   }
 }
 
-__global__ void k_tile_map(const SecDesc* secs, int nsec, int* tile_sec) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsec) return;
-  for (int t = 0; t < secs[s].ntile; t++) tile_sec[secs[s].tile0 + t] = s;
+__global__ void k_tile_map(const SecDesc* secs, int nsec, int ntiles, int* tile_sec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  tile_sec[t] = find_section(nsec, (long)t, [&](int k) { return (long)secs[k].tile0; });
 }
 
 __global__ void k_put_single(SecDesc* dst, SecDesc v) { *dst = v; }
@@ -395,7 +404,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, L.ntp, ns, 2 * ns + 1, eps * eps, eps * eps};
   const int bs = 64;
   PWD_KERNEL(PWD_FAM_OTHER, st,
-             k_tile_map<<<(nsec + 127) / 128, 128, 0, st>>>(w.secs, nsec, w.tile_sec));
+             k_tile_map<<<(unsigned)((L.ntiles + 255) / 256), 256, 0, st>>>(w.secs, nsec, L.ntiles, w.tile_sec));
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_fill<<<(unsigned)((L.n1max + 255) / 256), 256, 0, st>>>(w.ones, 1.0f, L.n1max));
   // slots whose source lies outside the section stay 0 (pwspray_lop :995)
@@ -404,10 +413,24 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   if (w.bf.u1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
     return PWD_ECUDA;
   const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
-  const unsigned gfa = (unsigned)((L.ntp + bs - 1) / bs);
   const unsigned gap = (unsigned)((2 * L.ntp + bs - 1) / bs);
   const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
-  PWD_KERNEL(PWD_FAM_SPRAY, st, k_spray2_factor<NW><<<gfa, bs, 0, st>>>(dip, w.bf, b, c));
+  // a thread per filter orientation when even then the factor launch fills
+  // less than one wave (a thread per trace then leaves SMs idle); otherwise
+  // a thread per trace, its two factors sharing the taps
+  int dev = 0, sms = 1, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spray2_factor<NW, true>, bs, 0);
+  if (2 * L.ntp <= (long)sms * per * bs) {
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               (k_spray2_factor<NW, true><<<(unsigned)((2 * L.ntp + bs - 1) / bs), bs, 0, st>>>(
+                   dip, w.bf, b, c)));
+  } else {
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               (k_spray2_factor<NW, false><<<(unsigned)((L.ntp + bs - 1) / bs), bs, 0, st>>>(
+                   dip, w.bf, b, c)));
+  }
   if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
