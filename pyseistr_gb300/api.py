@@ -22,6 +22,18 @@ import torch
 from . import device as D
 
 
+_COPY_STREAMS = {}
+
+
+def _copy_stream():
+    """A side stream of the current device for device-to-host copies that
+    overlap later kernels."""
+    dev = torch.cuda.current_device()
+    if dev not in _COPY_STREAMS:
+        _COPY_STREAMS[dev] = torch.cuda.Stream(device=dev)
+    return _COPY_STREAMS[dev]
+
+
 def _dev():
     if not torch.cuda.is_available():
         raise RuntimeError("pyseistr_gb300 needs a CUDA GPU; no CPU fallback exists")
@@ -229,14 +241,21 @@ def dip_somean2d_packed(data, shapes, niter=5, liter=10, order=2, rect=[10, 10, 
         raise TypeError("data must be a flat float32 tensor")
     d = data if data.is_cuda else data.to(_dev(), non_blocking=True)
     p = D.dip_batch(d, shapes, niter, liter, order, rect, mixed=mixed)
-    f = D.sofilter2d_batch(d, p, shapes, ns, order, eps,
-                           filter=D.FILTER_MEDIAN if median else D.FILTER_MEAN)
     if out is None:
         out = (torch.empty(p.shape, dtype=torch.float32, pin_memory=True),
-               torch.empty(f.shape, dtype=torch.float32, pin_memory=True))
-    out[0].copy_(p, non_blocking=True)
+               torch.empty(d.shape, dtype=torch.float32, pin_memory=True))
+    # the slopes go down on a side stream while the filter runs
+    cur = torch.cuda.current_stream()
+    side = _copy_stream()
+    side.wait_stream(cur)
+    with torch.cuda.stream(side):
+        out[0].copy_(p, non_blocking=True)
+    p.record_stream(side)
+    f = D.sofilter2d_batch(d, p, shapes, ns, order, eps,
+                           filter=D.FILTER_MEDIAN if median else D.FILTER_MEAN)
     out[1].copy_(f, non_blocking=True)
-    torch.cuda.current_stream().synchronize()
+    cur.synchronize()
+    side.synchronize()
     return out
 
 
