@@ -271,6 +271,50 @@ def api_step(wl, mixed=False, host=None):
 # Algorithmic bytes per sample of each kernel family, averaged over the
 # family's launches of one step (what the launches must read and write at
 # minimum; every launch covers every section of the batch).
+def fp32_peak_tflops():
+    """FP32 FMA peak of this GPU, measured with the library's probe kernel
+    (pwd_fp32_fma_probe: 8 independent FMA chains per thread, 8 blocks of
+    256 threads per SM), best of 5 launches timed with CUDA events."""
+    import ctypes
+
+    import torch
+    from pyseistr_gb300 import _lib
+
+    lib = _lib.load()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = 8 * sms, 256, 16384
+    out = torch.empty(blocks * threads, dtype=torch.float32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best = None
+    for _ in range(6):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _lib.check(lib.pwd_fp32_fma_probe(ctypes.c_void_p(out.data_ptr()), blocks, threads,
+                                          iters, st), "fp32 probe")
+        b.record()
+        b.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        best = t if best is None else min(best, t)
+    return 16.0 * iters * blocks * threads / best / 1e12
+
+
+def spray_flops_per_sample(wl):
+    """Algorithmic FP32 work of the spray and its filter per input sample
+    (the pinned model: 2-D mean 148 ns + 220, 2-D median 74 ns + 220, 3-D
+    (np - 1) x 47 + 880 per filter), for the workloads that spray."""
+    f = wl.filt
+    if wl.name == "batch2d":
+        return 148 * f["ns"] + 220
+    if wl.name == "das2d":
+        return 74 * f["ns"] + 220
+    if wl.name == "plain2d":
+        return (148 * f["ns"] + 220) + (74 * f["ns"] + 220)
+    if wl.name == "plain3d":
+        npc = (2 * f["r1"] + 1) * (2 * f["r2"] + 1)
+        return 2 * ((npc - 1) * 47 + 880)
+    return 0
+
+
 def family_bytes(wl, launches, mixed=False):
     """Average algorithmic bytes per launch of each family for one step."""
     n = wl.samples()
@@ -710,6 +754,15 @@ def main():
     }
     if plain is not None:
         line["plain_fp32"] = plain
+    if rank == 0 and fam_ms.get("spray", 0.0) > 0 and spray_flops_per_sample(wl):
+        # the spray is bound by FP32 issue and latency, not by HBM: its
+        # algorithmic flops per second against the measured FMA peak
+        fpk = fp32_peak_tflops()
+        ach = spray_flops_per_sample(wl) * wl.samples() / (fam_ms["spray"] / 1e3) / 1e12
+        line["spray_fp32"] = {"bound": "fp32-issue", "achieved": ach, "peak": fpk,
+                              "unit": "TFLOP/s", "frac": ach / fpk,
+                              "flops_per_sample": spray_flops_per_sample(wl),
+                              "peak_source": "measured: pwd_fp32_fma_probe"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         kind = (None if wl.name in ("plain3d", "patches3d") else _ref_modules()) or "port"
         sample, desc = cpu_sample(wl, args.cpu_budget)

@@ -263,6 +263,11 @@ void pwd_profile_start(void);
  * the summed kernel time in ms and the number of launches (arrays of
  * `nfam` entries).  Returns the number of launches recorded. */
 int pwd_profile_stop(double *ms, int *launches, int nfam);
+/* FP32 FMA throughput probe (no reference counterpart): `blocks` x
+ * `threads` threads each run 8 independent FMA chains of `iters` steps
+ * (16 flops per step) and write one float to out[thread]; time it with
+ * CUDA events to measure the FP32 CUDA-core peak. */
+int pwd_fp32_fma_probe(float *out, int blocks, int threads, int iters, pwd_stream_t stream);
 
 #ifdef __cplusplus
 }

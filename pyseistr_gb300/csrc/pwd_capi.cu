@@ -109,3 +109,30 @@ extern "C" int pwd_profile_stop(double* ms, int* launches, int nfam) {
   p.recs.clear();
   return n;
 }
+
+// FP32 FMA throughput probe: every thread runs 8 independent FMA chains for
+// `iters` steps (16 flops a step) and folds them into out[thread], so the
+// timed launch measures the CUDA-core FP32 peak that the latency-bound
+// spray kernels are compared with.
+namespace {
+__global__ void k_fma_probe(float* out, int iters, float x, float y) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = (float)(threadIdx.x + k);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = __fmaf_rn(a[k], x, y);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s = __fadd_rn(s, a[k]);
+  out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" int pwd_fp32_fma_probe(float* out, int blocks, int threads, int iters,
+                                  pwd_stream_t stream) {
+  if (!out || blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return PWD_EINVAL;
+  k_fma_probe<<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters, 0.999999f, 1e-7f);
+  return pwd::cuda_status(cudaGetLastError());
+}
