@@ -254,6 +254,24 @@ enum {
   PWD_FAM_OTHER = 6,
   PWD_NFAM = 7
 };
+/* ---- Patching (pyseistr/patch.py mode 1) --------------------------------
+ * An n1 x n2 x n3 column-major array (n3 = l3 = s3 = 1 for patch2d) cut into
+ * l1 x l2 x l3 windows at strides s1, s2, s3, each axis zero-padded at its
+ * end to n + s - mod(n - l, s) when mod(n - l, s) != 0; patch id runs over
+ * the first axis's window starts outermost; x = [npatch][l1 l2 l3], each
+ * patch column-major (the packed-section layout of the batched entries).
+ * Replace patch2d (patch.py:2), patch3d (:86), patch2d_inv (:208) and
+ * patch3d_inv (:307).  The inverse adds the patches covering each sample in
+ * FP64 in patch order, divides by their count (NaN where none covers it)
+ * and rounds to float.  Device pointers; no workspace. */
+/* Number of patches, 0 for invalid sizes or more than 2^31 - 1 patch
+ * elements. */
+size_t pwd_patch_count(int n1, int n2, int n3, int l1, int l2, int l3, int s1, int s2, int s3);
+int pwd_patch(const float *a, float *x, int n1, int n2, int n3, int l1, int l2, int l3, int s1,
+              int s2, int s3, pwd_stream_t stream);
+int pwd_patch_inv(const float *x, float *a, int n1, int n2, int n3, int l1, int l2, int l3,
+                  int s1, int s2, int s3, pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

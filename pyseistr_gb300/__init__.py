@@ -14,6 +14,8 @@ sm_103a kernels of libpwd_gb300.so:
     dip_somean2d_batch,            call per section); the packed forms take
     dip_somean2d_packed,           flat (pinned) host tensors
     dip_soint3d_packed
+    patch2d, patch3d,              windows of a section / cube and their
+    patch2d_inv, patch3d_inv       overlap-add inverse (pyseistr/patch.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -30,6 +32,10 @@ from .api import (  # noqa: F401
     dip_soint3d_packed,
     dip3dc,
     dipc,
+    patch2d,
+    patch2d_inv,
+    patch3d,
+    patch3d_inv,
     soint3dc,
     somean2dc,
     somean2dc_batch,

@@ -321,3 +321,69 @@ def dip_somean2d_batch(sections, niter=5, liter=10, order=2, rect=[10, 10, 1], n
     else:
         f = D.sofilter2d_batch(d, p, shapes, ns, order, eps, filter=D.FILTER_MEAN)
     return _unpack(p, shapes), _unpack(f, shapes)
+
+
+def _mode1(mode):
+    if mode != 1:
+        raise ValueError("patching mode 1 is the only mode the reference defines")
+
+
+def _patches_to_dev(X, npatch, m):
+    """The patch matrix (rows = patches) as a flat CUDA tensor, row-major."""
+    if isinstance(X, torch.Tensor):
+        t = X.to(device=_dev(), dtype=torch.float32).reshape(-1).contiguous()
+        return t, True
+    arr = np.ascontiguousarray(np.asarray(X, dtype=np.float32).reshape(npatch, m))
+    return torch.from_numpy(arr.reshape(-1)).pin_memory().to(_dev(), non_blocking=True), False
+
+
+def _patch_fwd(A, ls, ss):
+    shape = tuple(A.shape)
+    a, as_t = _to_dev_flat(A)
+    x = D.patch(a, shape, ls, ss)
+    return x if as_t else x.cpu().numpy()
+
+
+def _patch_inv(X, shape, ls, ss):
+    npatch = D.patch_count(shape, ls, ss)
+    if npatch == 0:
+        raise ValueError("invalid patch sizes")
+    m = int(np.prod(ls))
+    x, as_t = _patches_to_dev(X, npatch, m)
+    out = D.patch_inv(x, shape, ls, ss)
+    return _from_dev_flat(out, shape, as_t)
+
+
+def patch2d(A, l1=8, l2=8, s1=4, s2=4, mode=1):
+    """patch2d (patch.py:2): the l1 x l2 windows of a 2-D array at strides
+    s1, s2 (the array zero-padded at its ends so that the last window ends
+    on it) as the rows of a [npatch, l1*l2] float32 array, each window
+    flattened column-major; rows are ordered with the first axis's window
+    starts outermost.  A CUDA tensor in gives a CUDA tensor out."""
+    _mode1(mode)
+    return _patch_fwd(A, (l1, l2), (s1, s2))
+
+
+def patch3d(A, l1=4, l2=4, l3=4, s1=2, s2=2, s3=2, mode=1):
+    """patch3d (patch.py:86): as patch2d for a 3-D array; the result has the
+    reference's trailing axis of length 1, [npatch, l1*l2*l3, 1]."""
+    _mode1(mode)
+    x = _patch_fwd(A, (l1, l2, l3), (s1, s2, s3))
+    return x.unsqueeze(-1) if isinstance(x, torch.Tensor) else x[:, :, None]
+
+
+def patch2d_inv(X, n1, n2, l1=8, l2=8, s1=4, s2=4, mode=1):
+    """patch2d_inv (patch.py:208): overlap-add of the patches into an n1 x n2
+    float32 array, each sample divided by the number of windows covering it
+    (NaN where none does)."""
+    _mode1(mode)
+    return _patch_inv(X, (n1, n2), (l1, l2), (s1, s2))
+
+
+def patch3d_inv(X, n1, n2, n3, l1=4, l2=4, l3=4, s1=2, s2=2, s3=2, mode=1):
+    """patch3d_inv (patch.py:307): as patch2d_inv for 3-D, from [npatch, L]
+    or the [npatch, L, 1] that patch3d returns.  Every pattern of padded
+    axes is handled (the reference's leaves two of them unassigned and
+    raises)."""
+    _mode1(mode)
+    return _patch_inv(X, (n1, n2, n3), (l1, l2, l3), (s1, s2, s3))

@@ -284,3 +284,46 @@ def sofilter2d_batch(data, dip_, shapes, ns, order=2, eps=0.01, filter=FILTER_ME
                                       order, filter, nmf, option, float(eps), _ptr(ws), ws.numel(),
                                       _stream()), "sofilter2d_batch")
     return out
+
+
+def _patch_dims(n, l, s):
+    n, l, s = (list(v) + [1] * (3 - len(v)) for v in (n, l, s))
+    return n, l, s
+
+
+def patch_count(n, l, s):
+    """Number of windows of patch2d / patch3d (0 for invalid sizes)."""
+    n, l, s = _patch_dims(n, l, s)
+    return int(_lib.load().pwd_patch_count(*n, *l, *s))
+
+
+def patch(a, n, l, s, out=None):
+    """Windows of the column-major array `a` (flat CUDA float32, n = (n1, n2[,
+    n3])) as a [npatch, prod(l)] tensor, each row a window flattened
+    column-major (pwd_patch)."""
+    L = _lib.load()
+    nn, ll, ss = _patch_dims(n, l, s)
+    npatch = int(L.pwd_patch_count(*nn, *ll, *ss))
+    if npatch == 0:
+        raise ValueError("invalid patch sizes")
+    a = _as_flat(a, nn[0] * nn[1] * nn[2], "a")
+    m = ll[0] * ll[1] * ll[2]
+    if out is None:
+        out = torch.empty((npatch, m), dtype=torch.float32, device=a.device)
+    _lib.check(L.pwd_patch(_ptr(a), _ptr(out), *nn, *ll, *ss, _stream()), "patch")
+    return out
+
+
+def patch_inv(x, n, l, s, out=None):
+    """Overlap-add of the windows x [npatch, prod(l)] back into a flat
+    column-major array of shape n (pwd_patch_inv)."""
+    L = _lib.load()
+    nn, ll, ss = _patch_dims(n, l, s)
+    npatch = int(L.pwd_patch_count(*nn, *ll, *ss))
+    if npatch == 0:
+        raise ValueError("invalid patch sizes")
+    x = _as_flat(x, npatch * ll[0] * ll[1] * ll[2], "x")
+    if out is None:
+        out = torch.empty(nn[0] * nn[1] * nn[2], dtype=torch.float32, device=x.device)
+    _lib.check(L.pwd_patch_inv(_ptr(x), _ptr(out), *nn, *ll, *ss, _stream()), "patch_inv")
+    return out
