@@ -578,13 +578,151 @@ def run_reference(args):
     return 0
 
 
+PATCH = {"l": (64, 64), "s": (32, 32)}
+
+
+def measured_hbm_peak():
+    """(GB/s, source): the measured copy bandwidth, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def run_patch(args):
+    """patch2d + patch2d_inv of the 2000 x 5000 DAS-like record in 64 x 64
+    windows at stride 32 (the patch / DAS batching workflow's producer and
+    consumer).  A step is one forward and one inverse pass over the record."""
+    rank, world, local = dist_info()
+    d = W.das2d(seed=args.seed + rank)
+    n1, n2 = d.shape
+    n = n1 * n2
+    ls, ss = PATCH["l"], PATCH["s"]
+    metric = "patched and reassembled samples/sec (patch2d + patch2d_inv)"
+    config = {"workload": f"patch2d: {n1} x {n2} DAS-like record, windows {ls} at strides {ss}",
+              "samples_per_step": n, "l2": "inputs larger than L2 (129 MB patch matrix)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle import patch_oracle as P
+
+        sub = d[:500, :1250]
+        tt, m = 0.0, 0
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            P.patch_inv(P.patch(sub, ls, ss), sub.shape, ls, ss)
+            if k >= args.warmup:
+                tt += time.perf_counter() - t0
+                m += sub.size
+        value = m / tt
+        desc = "500 x 1250 corner of the record, numpy restatement (oracle/patch_oracle.py)"
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": value, "unit": "samples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+            "config": dict(config, sample=desc),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": 1, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return 0
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import pyseistr_gb300 as ps
+    from pyseistr_gb300 import _lib
+    from pyseistr_gb300 import device as D
+
+    _lib.load()
+    dev = torch.device("cuda", local)
+    a = torch.from_numpy(np.ascontiguousarray(d.reshape(-1, order="F"))).to(dev)
+    npatch = D.patch_count((n1, n2), ls, ss)
+    x = torch.empty((npatch, ls[0] * ls[1]), dtype=torch.float32, device=dev)
+    back = torch.empty_like(a)
+
+    def step():
+        D.patch(a, (n1, n2), ls, ss, out=x)
+        D.patch_inv(x, (n1, n2), ls, ss, out=back)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            step()
+        ev1.record()
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev) if world > 1 else ev0.elapsed_time(ev1)
+    ms_step = ms / args.steps
+    # per-kernel times: each direction moves 4 n + 4 npatch L algorithmic bytes
+    per = {}
+    for name, fn in (("k_patch", lambda: D.patch(a, (n1, n2), ls, ss, out=x)),
+                     ("k_patch_inv", lambda: D.patch_inv(x, (n1, n2), ls, ss, out=back))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        per[name] = e0.elapsed_time(e1) / args.steps
+    dom = max(per, key=per.get)
+    nbytes = 4 * n + 4 * npatch * ls[0] * ls[1]
+    achieved = nbytes / (per[dom] / 1e3) / 1e9
+    peak, peak_src = measured_hbm_peak()
+    # end to end through the public API on host arrays
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        xh = ps.patch2d(d, *ls, *ss)
+        bh = ps.patch2d_inv(xh, n1, n2, *ls, *ss)
+    e2e = world * n / ((time.perf_counter() - t0) / args.steps)
+    assert np.array_equal(bh, d)
+    line = {
+        "metric": metric, "value": world * n / (ms_step / 1e3), "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+        "config": dict(config, parallelism=f"replicas x{world}"),
+        "e2e": {"value": e2e, "unit": "samples/s", "h2d_bytes_per_step": 4 * n + 4 * x.numel(),
+                "d2h_bytes_per_step": 4 * x.numel() + 4 * n},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel_ms": per,
+                     "bytes_per_launch": nbytes},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import patch_oracle as P
+
+        sub = d[:500, :1250]
+        t0 = time.perf_counter()
+        P.patch_inv(P.patch(sub, ls, ss), sub.shape, ls, ss)
+        line["cpu_baseline"] = {"value": sub.size / (time.perf_counter() - t0),
+                                "unit": "samples/s", "cores": 1, "kind": "port",
+                                "sample": "500 x 1250 corner, oracle/patch_oracle.py"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch2d")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["patch2d"], default="batch2d")
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
                     help="sections of the batch2d workload, patches of patches3d (at most 64); "
@@ -600,6 +738,8 @@ def main():
                     help="seconds of single-core CPU work for the cpu_baseline sample")
     args = ap.parse_args()
 
+    if args.workload == "patch2d":
+        return run_patch(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -664,12 +804,7 @@ def main():
     fam_n = {f: v // args.steps for f, v in prof.launches.items()}
     dom = max(fam_ms, key=lambda f: fam_ms[f])
     bpl = family_bytes(wl, fam_n, mixed)
-    peak, peak_src = HBM_FALLBACK_GBS, "fallback"
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-            peak, peak_src = float(json.load(fh)["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        pass
+    peak, peak_src = measured_hbm_peak()
     avg_launch_s = fam_ms[dom] / 1e3 / max(1, fam_n[dom])
     achieved = bpl.get(dom, 0.0) / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
     traffic = None
