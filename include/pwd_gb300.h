@@ -264,8 +264,10 @@ enum {
  * patch3d_inv (:307).  The inverse adds the patches covering each sample in
  * FP64 in patch order, divides by their count (NaN where none covers it)
  * and rounds to float.  Device pointers; no workspace. */
-/* Number of patches, 0 for invalid sizes or more than 2^31 - 1 patch
- * elements. */
+/* Number of patches, 0 for invalid sizes, for more than 2^31 - 1 patch
+ * elements, or for an axis with no window (a window longer than the axis
+ * when the stride divides the excess: the reference's loops then make no
+ * patch at all). */
 size_t pwd_patch_count(int n1, int n2, int n3, int l1, int l2, int l3, int s1, int s2, int s3);
 int pwd_patch(const float *a, float *x, int n1, int n2, int n3, int l1, int l2, int l3, int s1,
               int s2, int s3, pwd_stream_t stream);

@@ -47,7 +47,7 @@ def test_patch_matches_reference(ps, case):
 
 @pytest.mark.parametrize("shape,l,s", [((13, 10, 9), (4, 4, 4), (2, 2, 2)),
                                        ((12, 11, 9), (4, 4, 4), (2, 2, 2)),
-                                       ((3, 40, 7), (5, 8, 2), (2, 6, 3)),
+                                       ((3, 40, 7), (4, 8, 2), (2, 6, 3)),
                                        ((101, 1, 1), (16, 1, 1), (5, 1, 1))])
 def test_patch3d_vs_oracle(ps, shape, l, s):
     from oracle import patch_oracle as P
@@ -99,3 +99,7 @@ def test_invalid_sizes(ps):
         ps.patch2d(np.zeros((8, 8), np.float32), 0, 4, 2, 2)
     with pytest.raises(ValueError):
         ps.patch2d(np.zeros((8, 8), np.float32), mode=2)
+    # a window longer than an axis whose excess the stride divides: the
+    # reference's window loop is empty (no patches); refused here
+    with pytest.raises(ValueError):
+        ps.patch3d(np.zeros((3, 40, 7), np.float32), 5, 8, 2, 2, 6, 3)
