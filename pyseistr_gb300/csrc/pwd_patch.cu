@@ -127,7 +127,12 @@ __global__ void k_patch_inv(const float* __restrict__ x, float* __restrict__ a, 
     cover(i1, g.l[0], g.np[0], g.ds[0], lo1, hi1);
     cover(i2, g.l[1], g.np[1], g.ds[1], lo2, hi2);
     cover(i3, g.l[2], g.np[2], g.ds[2], lo3, hi3);
-    double sum = 0.0, cnt = 0.0;
+    // GB300's FP64 rate is small: the count is an integer, the first term
+    // enters without an addition (0.0 + v is v, except that a zero becomes
+    // +0), and a power-of-two count divides by its exact reciprocal (the
+    // same double as the division)
+    double sum = 0.0;
+    unsigned cnt = 0;
     for (unsigned p1 = lo1; p1 <= hi1; p1++)
       for (unsigned p2 = lo2; p2 <= hi2; p2++)
         for (unsigned p3 = lo3; p3 <= hi3; p3++) {
@@ -135,10 +140,18 @@ __global__ void k_patch_inv(const float* __restrict__ x, float* __restrict__ a, 
           const unsigned k = (i1 - p1 * g.s[0]) +
                              (unsigned)g.l[0] * ((i2 - p2 * g.s[1]) +
                                                  (unsigned)g.l[1] * (i3 - p3 * g.s[2]));
-          sum = __dadd_rn(sum, (double)x[(size_t)id * g.L + k]);
-          cnt = __dadd_rn(cnt, 1.0);
+          const double v = (double)x[(size_t)id * g.L + k];
+          sum = cnt == 0 ? (v == 0.0 ? 0.0 : v) : __dadd_rn(sum, v);
+          cnt++;
         }
-    a[e] = __double2float_rn(__ddiv_rn(sum, cnt));
+    double q;
+    if (cnt == 0)
+      q = __ddiv_rn(0.0, 0.0);  // no window covers the sample: NaN as 0/0
+    else if ((cnt & (cnt - 1)) == 0)
+      q = __dmul_rn(sum, 1.0 / (double)cnt);
+    else
+      q = __ddiv_rn(sum, (double)cnt);
+    a[e] = __double2float_rn(q);
   }
 }
 
