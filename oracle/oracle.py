@@ -58,6 +58,7 @@ def lib():
         L.orc_pwspray2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
         L.orc_pwspray3d_f32.argtypes = [_P, _P, _P, _P] + [_I] * 6
         L.orc_spray_median_f32.argtypes = [_P, _P, _I, _I, _L, _I, _I]
+        L.orc_bandpass_f32.argtypes = [_P, _P, _I, _L, _F, _F, _F, _I, _I, _I]
         _lib = L
     return _lib
 
@@ -210,3 +211,17 @@ def spray_median(u, nmf, option=1):
     out = np.empty((ntr, n1), dtype=np.float32)
     _check(lib().orc_spray_median_f32(_ptr(u), _ptr(out), n1, npp, ntr, nmf, option), "median")
     return out
+
+
+def bandpass(din, dt, flo=0.0, fhi=0.5, nplo=6, nphi=6, phase=0):
+    """cbp (pyseistr/src/bp_cfuns.c:524-645): Butterworth band-pass of every
+    trace of a column-major (n1, n2[, n3]) float32 array; same shape out."""
+    a = np.asarray(din, dtype=np.float32)
+    n1 = a.shape[0]
+    ntr = a.size // n1
+    x = _flat(a, np.float32)
+    out = np.empty_like(x)
+    _check(lib().orc_bandpass_f32(_ptr(x), _ptr(out), n1, ntr, dt, flo, fhi, nplo, nphi,
+                                  phase), "bandpass")
+    return out.reshape(a.shape, order="F")
+

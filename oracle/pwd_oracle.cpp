@@ -1376,6 +1376,121 @@ struct DefaultFpEnv {
 };
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Band-pass (bp_cfuns.c:422-507 sf_butter_init / sf_butter_apply, :524-645
+// cbp): Butterworth low-cut and high-cut filters of cascaded first- and
+// second-order sections, run along each trace, and again from the trace's
+// end for zero phase.  Coefficients follow the C expressions' types: a
+// float mixed with a double constant is evaluated in double and stored as
+// float; the per-sample recurrences are float, left to right.
+// ---------------------------------------------------------------------------
+namespace orc {
+
+struct Butter {
+  bool low = false;
+  int nn = 0;
+  std::vector<float> c0, c2;  // per section: gain and last feedback tap
+  float mid = 0.f;             // middle feedback tap of the second-order sections
+};
+
+inline Butter butter_init(bool low, float cutoff, int nn) {
+  const double pi = 3.14159265358979323846264338328;
+  Butter b;
+  b.low = low;
+  b.nn = nn;
+  b.c0.assign((nn + 1) / 2, 0.f);
+  b.c2.assign((nn + 1) / 2, 0.f);
+  const float arg = (float)(2. * pi * (double)cutoff);
+  const float sw = sinf(arg), cw = cosf(arg);
+  if (nn % 2) {  // the first-order section is the last row
+    float f;
+    if (low) {
+      f = (float)((1. + (double)cw) / (double)sw);
+      b.c0[nn / 2] = (float)(1. / (1. + (double)f));
+      b.c2[nn / 2] = (float)(1. - (double)f);
+    } else {
+      f = (float)((double)sw / (1. + (double)cw));
+      b.c0[nn / 2] = (float)(1. / ((double)f + 1.));
+      b.c2[nn / 2] = (float)((double)f - 1.);
+    }
+  }
+  const float half = (float)(0.5 * (double)arg);
+  float g = low ? sinf(half) : cosf(half);
+  g = g * g;
+  for (int j = 0; j < nn / 2; j++) {
+    const float ang = (float)(pi * (double)(2 * j + 1) / (double)(2 * nn));
+    const float ss = sinf(ang) * sw;
+    b.c0[j] = (float)((double)g / (1. + (double)ss));
+    b.c2[j] = (float)((1. - (double)ss) / (double)g);
+  }
+  b.mid = (float)(-2. * (double)cw / (double)g);
+  return b;
+}
+
+// The filter along x[0..nx) (back = false) or from x[nx-1] down (back =
+// true: the reference's reverse, apply, reverse).
+inline void butter_run(const Butter& b, int nx, float* x, bool back) {
+  auto at = [&](int k) -> float& { return x[back ? nx - 1 - k : k]; };
+  const int nn = b.nn;
+  if (nn % 2) {
+    const float c0 = b.c0[nn / 2], c2 = b.c2[nn / 2];
+    float x0 = 0.f, x1, y1 = 0.f;
+    for (int k = 0; k < nx; k++) {
+      x1 = x0;
+      x0 = at(k);
+      const float s = b.low ? x0 + x1 : x0 - x1;
+      y1 = (s - c2 * y1) * c0;
+      at(k) = y1;
+    }
+  }
+  for (int j = 0; j < nn / 2; j++) {
+    const float c0 = b.c0[j], c2 = b.c2[j], c1 = b.mid;
+    float x0 = 0.f, x1 = 0.f, x2, y1 = 0.f, y2 = 0.f;
+    for (int k = 0; k < nx; k++) {
+      x2 = x1;
+      x1 = x0;
+      x0 = at(k);
+      const float tx = 2.f * x1;
+      const float s = b.low ? (x0 + tx) + x2 : (x0 - tx) + x2;
+      const float y0 = ((s - c1 * y1) - c2 * y2) * c0;
+      y2 = y1;
+      y1 = y0;
+      at(k) = y0;
+    }
+  }
+}
+
+inline int bandpass(const float* in, float* out, int n1, long ntr, float d1, float flo,
+                    float fhi, int nplo, int nphi, int phase) {
+  if (n1 < 1 || ntr < 1) return ORC_EINVAL;
+  const float eps = 0.0001f;
+  if (!(flo < 0.f)) flo = flo * d1;  // a negative flo is kept as given
+  if (!(fhi < 0.f)) fhi = fhi * d1;
+  if (nplo < 1) nplo = 1;
+  if (nplo > 1 && !phase) nplo /= 2;
+  if (nphi < 1) nphi = 1;
+  if (nphi > 1 && !phase) nphi /= 2;
+  const bool lo = flo > eps, hi = (double)fhi < 0.5 - (double)eps;
+  Butter blo, bhi;
+  if (lo) blo = butter_init(false, flo, nplo);
+  if (hi) bhi = butter_init(true, fhi, nphi);
+  for (long t = 0; t < ntr; t++) {
+    float* x = out + t * n1;
+    if (x != in + t * n1) std::memcpy(x, in + t * n1, sizeof(float) * n1);
+    if (lo) {
+      butter_run(blo, n1, x, false);
+      if (!phase) butter_run(blo, n1, x, true);
+    }
+    if (hi) {
+      butter_run(bhi, n1, x, false);
+      if (!phase) butter_run(bhi, n1, x, true);
+    }
+  }
+  return 0;
+}
+
+}  // namespace orc
+
 extern "C" {
 
 int orc_dip_f32(const float* u, const float* mask, float* p, int n1, int n2, int n3, int niter,
@@ -1476,6 +1591,12 @@ int orc_soint3d_f64(const double* din, const double* mask, const double* pp, con
   DefaultFpEnv fpenv;
   return orc::soint3d<double>(din, mask, pp, qq, out, n1, n2, n3, nw, nj1, nj2, niter, drift,
                               seed, hasmask, var);
+}
+
+int orc_bandpass_f32(const float* in, float* out, int n1, long ntr, float d1, float flo,
+                     float fhi, int nplo, int nphi, int phase) {
+  DefaultFpEnv fpenv;
+  return orc::bandpass(in, out, n1, ntr, d1, flo, fhi, nplo, nphi, phase);
 }
 
 }  // extern "C"
