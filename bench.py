@@ -598,7 +598,7 @@ def run_patch(args):
     d = W.das2d(seed=args.seed + rank)
     n1, n2 = d.shape
     n = n1 * n2
-    nrec = PATCH["records"]
+    nrec = args.records or PATCH["records"]
     ls, ss = PATCH["l"], PATCH["s"]
     metric = "patched and reassembled samples/sec (patch2d + patch2d_inv)"
     config = {"workload": f"patch2d: {nrec} DAS-like records of {n1} x {n2} per step, windows "
@@ -731,13 +731,160 @@ def run_patch(args):
     return 0
 
 
+# the DAS demo's filter (demos/test_pyseistr_das.py:39): 2 kHz sampling,
+# high cut at 200 Hz, 6 poles (3 per direction), zero phase
+BANDPASS = {"dt": 0.0005, "flo": 0.0, "fhi": 200.0, "nplo": 6, "nphi": 6, "phase": 0,
+            "records": 16}
+
+
+def cpu_bandpass(d, bp, threads):
+    """Seconds the oracle's C band-pass takes over the traces of `d`, split
+    into `threads` column blocks run on as many host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    args = (bp["dt"], bp["flo"], bp["fhi"], bp["nplo"], bp["nphi"], bp["phase"])
+    edges = np.linspace(0, d.shape[1], threads + 1).astype(int)
+    blocks = [np.asfortranarray(d[:, a:b]) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+    with ThreadPoolExecutor(len(blocks)) as pool:
+        t0 = time.perf_counter()
+        list(pool.map(lambda blk: O.bandpass(blk, *args), blocks))
+        return time.perf_counter() - t0
+
+
+def run_bandpass(args):
+    """bandpassc of 2000 x 5000 DAS-like records with the DAS demo's filter
+    (the step before the slope estimation in the DAS chain).  A step is 16
+    records, each in its own buffer (640 MB of input, more than L2)."""
+    rank, world, local = dist_info()
+    d = W.das2d(seed=args.seed + rank)
+    n1, n2 = d.shape
+    n = n1 * n2
+    bp = BANDPASS
+    nrec = args.records or bp["records"]
+    bpa = (bp["dt"], bp["flo"], bp["fhi"], bp["nplo"], bp["nphi"], bp["phase"])
+    metric = "band-passed samples/sec (bandpassc, Butterworth, zero phase)"
+    config = {"workload": f"bandpass2d: {nrec} DAS-like records of {n1} x {n2} per step, "
+                          f"dt {bp['dt']} s, high cut {bp['fhi']} Hz, {bp['nphi']} poles, "
+                          "zero phase",
+              "samples_per_step": nrec * n,
+              "l2": "inputs larger than L2 (16 distinct 40 MB records per step)"}
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        tt, m = 0.0, 0
+        for k in range(args.warmup + args.steps):
+            t = cpu_bandpass(d, bp, threads)
+            if k >= args.warmup:
+                tt += t
+                m += n
+        value = m / tt
+        desc = (f"one {n1} x {n2} record per step, oracle C restatement "
+                f"(oracle/pwd_oracle.cpp) over {threads} threads")
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": value, "unit": "samples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+            "config": dict(config, sample=desc),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads,
+                             "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return 0
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import pyseistr_gb300 as ps
+    from pyseistr_gb300 import _lib
+    from pyseistr_gb300 import device as D
+
+    _lib.load()
+    dev = torch.device("cuda", local)
+    a1 = torch.from_numpy(np.ascontiguousarray(d.reshape(-1, order="F"))).to(dev)
+    recs = [a1.clone() for _ in range(nrec)]
+    outs = [torch.empty_like(a1) for _ in range(nrec)]
+    shape = (n1, n2, 1)
+
+    def step():
+        for r in range(nrec):
+            D.bandpass(recs[r], shape, *bpa, out=outs[r])
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 0.6:
+            step()
+            torch.cuda.synchronize()
+        l0 = _lib.launch_count()
+        ev0.record()
+        for _ in range(args.steps):
+            step()
+        ev1.record()
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev) if world > 1 else ev0.elapsed_time(ev1)
+    ms_step = ms / args.steps
+    # one k_bandpass launch per record: the average over the timed steps
+    per_launch_ms = ms_step / nrec
+    nbytes = 8 * n  # each sample read once and written once
+    achieved = nbytes / (per_launch_ms / 1e3) / 1e9
+    peak, peak_src = measured_hbm_peak()
+    # end to end through the public API on a host array
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dh = ps.bandpassc(d, *bpa, verb=0)
+    e2e = world * n / ((time.perf_counter() - t0) / args.steps)
+    line = {
+        "metric": metric, "value": world * nrec * n / (ms_step / 1e3), "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+        "config": dict(config, parallelism=f"replicas x{world}"),
+        "e2e": {"value": e2e, "unit": "samples/s", "h2d_bytes_per_step": 4 * n,
+                "d2h_bytes_per_step": 4 * n},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "kernel": "k_bandpass", "achieved": achieved,
+                     "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel_ms": per_launch_ms,
+                     "bytes_per_launch": nbytes,
+                     "sweeps": 2 if bp["fhi"] > 0 and not bp["phase"] else 1},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        assert np.array_equal(dh, O.bandpass(d, *bpa))
+        t, reps = 0.0, 0
+        while t < 2.0:  # a bounded sample: whole records for about 2 s of wall time
+            t += cpu_bandpass(d, bp, threads)
+            reps += 1
+        line["cpu_baseline"] = {"value": reps * n / t, "unit": "samples/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"{reps} passes over one {n1} x {n2} record, "
+                                          "oracle/pwd_oracle.cpp"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["patch2d"], default="batch2d")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["patch2d", "bandpass2d"], default="batch2d")
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
                     help="sections of the batch2d workload, patches of patches3d (at most 64); "
@@ -748,6 +895,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the slope estimation kernel by kernel instead of replaying "
                          "its captured CUDA graph")
+    ap.add_argument("--records", type=int, default=0,
+                    help="records per step of the patch2d and bandpass2d workloads (default "
+                         "16); smaller counts for profiler captures")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of single-core CPU work for the cpu_baseline sample")
@@ -755,6 +905,8 @@ def main():
 
     if args.workload == "patch2d":
         return run_patch(args)
+    if args.workload == "bandpass2d":
+        return run_bandpass(args)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -274,6 +274,19 @@ int pwd_patch(const float *a, float *x, int n1, int n2, int n3, int l1, int l2, 
 int pwd_patch_inv(const float *x, float *a, int n1, int n2, int n3, int l1, int l2, int l3,
                   int s1, int s2, int s3, pwd_stream_t stream);
 
+/* ---- Band-pass (pyseistr/bp.py bandpassc, src/bp_cfuns.c cbp) ------------
+ * Replaces cbp (bp_cfuns.c:524, argument tuple "Oiiifffiiii" less the verb
+ * flag): Butterworth low-cut (flo) and high-cut (fhi) filters along each of
+ * the n2*n3 column-major traces of length n1; flo, fhi in Hz with d1 the
+ * sampling interval (a negative cut-off is taken as already in cycles per
+ * sample); flo <= 1e-4 cycles per sample skips the low cut and fhi >=
+ * 0.5 - 1e-4 the high cut; nplo, nphi poles (at least 1, halved when
+ * phase = 0); phase 0 runs each filter forward then backward (zero phase),
+ * 1 forward only.  Results are bit-identical to cbp's.  `out` may equal
+ * `in`.  Device pointers; no workspace. */
+int pwd_bandpass(const float *in, float *out, int n1, int n2, int n3, float d1, float flo,
+                 float fhi, int nplo, int nphi, int phase, pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

@@ -16,10 +16,14 @@ sm_103a kernels of libpwd_gb300.so:
     dip_soint3d_packed
     patch2d, patch3d,              windows of a section / cube and their
     patch2d_inv, patch3d_inv       overlap-add inverse (pyseistr/patch.py)
+    bandpassc, cbp                 Butterworth band-pass along each trace
+                                   (pyseistr/bp.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
 from .api import (  # noqa: F401
+    bandpassc,
+    cbp,
     csoint3d,
     csomean2d,
     csomean3d,

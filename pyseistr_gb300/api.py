@@ -387,3 +387,75 @@ def patch3d_inv(X, n1, n2, n3, l1=4, l2=4, l3=4, s1=2, s2=2, s3=2, mode=1):
     raises)."""
     _mode1(mode)
     return _patch_inv(X, (n1, n2, n3), (l1, l2, l3), (s1, s2, s3))
+
+
+# --------------------------------------------------------------------------
+# band-pass (bp.py / bp_cfuns.c)
+# --------------------------------------------------------------------------
+def _bp_messages(n123, dt, flo, fhi, nplo, nphi, phase, verb):
+    """cbp's console output (bp_cfuns.c:544-580): the range warnings always,
+    the parameter lines when verb."""
+    f32 = np.float32
+    if verb:
+        print("nplo=%d,n123=%d" % (nplo, n123))
+    flo, fhi = f32(flo), f32(fhi)
+    if flo < 0:
+        print("Negative flo", end="")
+    else:
+        flo = f32(flo * f32(dt))
+    if fhi < 0:
+        print("Negative flo", end="")
+    else:
+        fhi = f32(fhi * f32(dt))
+        if flo > fhi:
+            print("Need flo < fhi")
+        if 0.5 < fhi:
+            print("Need fhi < Nyquist")
+    if verb:
+        nlo = max(int(nplo), 1)
+        nhi = max(int(nphi), 1)
+        nlo = nlo // 2 if nlo > 1 and not phase else nlo
+        nhi = nhi // 2 if nhi > 1 and not phase else nhi
+        print("flo=%g fhi=%g nplo=%d nphi=%d" % (float(flo), float(fhi), nlo, nhi))
+
+
+def cbp(din, n1, n2, n3, dt, flo, fhi, nplo, nphi, phase, verb):
+    """cbp "Oiiifffiiii" (bp_cfuns.c:524): Butterworth band-pass of the n2*n3
+    traces of length n1 in the flat column-major din; returns the flat
+    float32 result (a CUDA tensor for a tensor in)."""
+    t, as_t = _to_dev_flat(din)
+    n = n1 * n2 * n3
+    if t.numel() != n:
+        raise ValueError(f"cbp: din has {t.numel()} values, expected {n}")
+    _bp_messages(n, dt, flo, fhi, nplo, nphi, phase, verb)
+    out = D.bandpass(t, (n1, n2, n3), dt, flo, fhi, nplo, nphi, phase)
+    return out if as_t else out.cpu().numpy()
+
+
+def bandpassc(din, dt, flo=0, fhi=0.5, nplo=6, nphi=6, phase=0, verb=1):
+    """bandpassc (bp.py:128): Butterworth band-pass along the first axis.
+    flo, fhi in Hz (dt in s); a cut-off of 0 (low) or at or above Nyquist
+    (high) is not applied; nplo, nphi poles (halved for zero phase); phase
+    0 = zero phase (each filter forward, then backward), 1 = minimum phase.
+    1-D, 2-D or 3-D float32 in, same shape out, squeezed when the third
+    axis has length 1; a CUDA tensor in gives a CUDA tensor out."""
+    shape = tuple(din.shape)
+    if len(shape) == 1:
+        shape = (shape[0], 1, 1)
+    elif len(shape) == 2:
+        shape = (shape[0], shape[1], 1)
+    elif len(shape) != 3:
+        raise ValueError("bandpassc: din must have 1, 2 or 3 axes")
+    if shape[0] == 1 and shape[1] > 1 and shape[2] == 1:
+        # the reference flattens a row vector and then fails to unpack its shape
+        raise ValueError("bandpassc: a 1 x n row vector is not accepted (the reference raises)")
+    n1, n2, n3 = shape
+    if n1 * n2 * n3 == 0:
+        raise ValueError("bandpassc: empty input")
+    t, as_t = _to_dev_flat(din)
+    _bp_messages(n1 * n2 * n3, dt, flo, fhi, nplo, nphi, phase, verb)
+    out = D.bandpass(t, shape, dt, flo, fhi, nplo, nphi, phase)
+    dout = _from_dev_flat(out, shape, as_t)
+    if n3 == 1:
+        dout = dout.squeeze() if as_t else np.squeeze(dout)
+    return dout

@@ -327,3 +327,18 @@ def patch_inv(x, n, l, s, out=None):
         out = torch.empty(nn[0] * nn[1] * nn[2], dtype=torch.float32, device=x.device)
     _lib.check(L.pwd_patch_inv(_ptr(x), _ptr(out), *nn, *ll, *ss, _stream()), "patch_inv")
     return out
+
+
+def bandpass(d, n, dt, flo, fhi, nplo, nphi, phase, out=None):
+    """Butterworth band-pass of every trace of the flat column-major CUDA
+    float32 array `d` of shape n = (n1, n2, n3) (pwd_bandpass); `out` may be
+    `d` itself."""
+    L = _lib.load()
+    n1, n2, n3 = (int(v) for v in n)
+    d = _as_flat(d, n1 * n2 * n3, "d")
+    if out is None:
+        out = torch.empty_like(d)
+    _lib.check(L.pwd_bandpass(_ptr(d), _ptr(out), n1, n2, n3, float(dt), float(flo),
+                              float(fhi), int(nplo), int(nphi), int(phase), _stream()),
+               "bandpass")
+    return out
