@@ -62,7 +62,8 @@ def test_bandpass_vs_oracle(ps, shape, args):
     a = np.random.default_rng(3).standard_normal(shape).astype(np.float32)
     got = ps.bandpassc(a, *args, verb=0)
     want = O.bandpass(a, *args)
-    assert np.array_equal(got, np.squeeze(want) if len(shape) < 3 else want)
+    # a negative high cut makes an unstable filter: overflow and NaN alike
+    assert np.array_equal(got, np.squeeze(want) if len(shape) < 3 else want, equal_nan=True)
 
 
 def test_bandpass_das_record_on_device(ps):
