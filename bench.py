@@ -769,7 +769,8 @@ def run_bandpass(args):
                           f"dt {bp['dt']} s, high cut {bp['fhi']} Hz, {bp['nphi']} poles, "
                           "zero phase",
               "samples_per_step": nrec * n,
-              "l2": "inputs larger than L2 (16 distinct 40 MB records per step)"}
+              "l2": "inputs larger than L2 (16 distinct 40 MB records per step)",
+              "e2e_input": "one column-major float32 host record per call"}
     threads = os.cpu_count() or 1
     if args.impl == "reference":
         if rank != 0:
@@ -839,10 +840,12 @@ def run_bandpass(args):
     nbytes = 8 * n  # each sample read once and written once
     achieved = nbytes / (per_launch_ms / 1e3) / 1e9
     peak, peak_src = measured_hbm_peak()
-    # end to end through the public API on a host array
+    # end to end through the public API on a host array, column-major as the
+    # DAS demo reads its record (np.fromfile(...).reshape(..., order="F"))
+    df = np.asfortranarray(d)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        dh = ps.bandpassc(d, *bpa, verb=0)
+        dh = ps.bandpassc(df, *bpa, verb=0)
     e2e = world * n / ((time.perf_counter() - t0) / args.steps)
     line = {
         "metric": metric, "value": world * nrec * n / (ms_step / 1e3), "unit": "samples/s",

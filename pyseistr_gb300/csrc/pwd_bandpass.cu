@@ -10,17 +10,22 @@
 // its order, with no contraction: outputs are bit-identical to it.
 //
 // The recurrences are serial along a trace, so the parallelism is the trace
-// count: one thread per trace, a warp per 32 traces.  A warp walks its
-// traces in chunks of 32 samples: a 32 x 32 chunk comes in coalesced (lane =
-// sample) by cp.async into a shared-memory ring a few chunks ahead, each
-// thread runs its trace's samples through all sections of the pass (fusing
-// the sections of one direction changes nothing: section k at sample i
-// needs only section k-1 at samples <= i), and the chunk goes back out
-// coalesced.  A backward pass walks the chunks, and the samples in each, in
-// reverse.  Passes after the first read the output array back, which for a
-// record of tens of MB is still in L2.
+// count: one thread per trace, a warp per 32 traces, and with a few
+// thousand traces one warp per SM; the time is the instructions each
+// thread issues per sample, so data movement is kept to a few instructions
+// per 4 samples.  A warp walks its traces in chunks of 32 samples: a 32 x 32
+// chunk comes in coalesced by cp.async into a shared-memory ring a few
+// chunks ahead (16-byte copies, 8 lanes per trace, when traces start on
+// 16-byte boundaries; else 4-byte copies, lane = sample), each thread runs
+// its trace's samples through all sections of the pass reading and writing
+// 4 samples per shared-memory access (fusing the sections of one direction
+// changes nothing: section k at sample i needs only section k-1 at samples
+// <= i), and the chunk goes back out coalesced.  A backward pass walks the
+// chunks, and the samples in each, in reverse.  Passes after the first read
+// the output array back, which for a record of tens of MB is still in L2.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdint.h>
 #include <string.h>
 
 #include <algorithm>
@@ -46,10 +51,19 @@ struct BpPlan {
   BpPass p[kBpPass];
 };
 
-typedef float BpRing[kBpStages][32][33];
+// rows of 36 floats: 16-byte aligned, and a quarter-warp's 16-byte accesses
+// to 8 rows (row stride 36 = 4 mod 32 banks) or to 8 consecutive quads of one
+// row fall in distinct banks
+constexpr int kBpPitch = 36;
+typedef float BpRing[kBpStages][32][kBpPitch];
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
 
 // One pass of a cascade over the warp's 32 traces.
-template <bool LOW, bool FIRST, int NS2>
+template <bool VEC, bool LOW, bool FIRST, int NS2>
 __device__ void bp_pass(const float* src, float* dst, long n1, long t0, long ntr,
                         const BpPass& P, BpRing& ring) {
   const int lane = threadIdx.x & 31;
@@ -96,13 +110,23 @@ __device__ void bp_pass(const float* src, float* dst, long n1, long t0, long ntr
   };
 
   const long ntw = ntr - t0 < 32 ? ntr - t0 : 32;  // traces of this warp
+  // VEC: lane -> trace lane / 8 + 4 m (m < 8), samples 4 (lane % 8) .. + 3
+  const int vq = 4 * (lane & 7), vj = lane >> 3;
   auto load = [&](int q) {
     if (q < nch) {
-      const long i = (long)(back ? nch - 1 - q : q) * 32 + lane;
-      if (i < n1) {
-        const float* s = src + t0 * n1 + i;
+      const long c0 = (long)(back ? nch - 1 - q : q) * 32;
+      float(*buf)[kBpPitch] = ring[q % kBpStages];
+      if (VEC) {
+        if (c0 + vq < n1) {
+          const float* s = src + (t0 + vj) * n1 + c0 + vq;
+#pragma unroll
+          for (int m = 0; m < 8; m++)
+            if (vj + 4 * m < ntw) cp_async16(&buf[vj + 4 * m][vq], s + 4 * m * n1);
+        }
+      } else if (c0 + lane < n1) {
+        const float* s = src + t0 * n1 + c0 + lane;
 #pragma unroll 8
-        for (int j = 0; j < ntw; j++) cp_async4(&ring[q % kBpStages][j][lane], s + j * n1);
+        for (int j = 0; j < ntw; j++) cp_async4(&buf[j][lane], s + j * n1);
       }
     }
     cp_async_commit();
@@ -118,12 +142,27 @@ __device__ void bp_pass(const float* src, float* dst, long n1, long t0, long ntr
     const int c = back ? nch - 1 - q : q;
     const long len = n1 - (long)c * 32 < 32 ? n1 - (long)c * 32 : 32;
     if (len == 32) {
+      float4* r4 = reinterpret_cast<float4*>(row);
       if (back) {
 #pragma unroll
-        for (int i = 31; i >= 0; i--) row[i] = step(row[i]);
+        for (int g = 7; g >= 0; g--) {
+          float4 v = r4[g];
+          v.w = step(v.w);
+          v.z = step(v.z);
+          v.y = step(v.y);
+          v.x = step(v.x);
+          r4[g] = v;
+        }
       } else {
 #pragma unroll
-        for (int i = 0; i < 32; i++) row[i] = step(row[i]);
+        for (int g = 0; g < 8; g++) {
+          float4 v = r4[g];
+          v.x = step(v.x);
+          v.y = step(v.y);
+          v.z = step(v.z);
+          v.w = step(v.w);
+          r4[g] = v;
+        }
       }
     } else if (back) {
       for (int i = (int)len - 1; i >= 0; i--) row[i] = step(row[i]);
@@ -131,11 +170,21 @@ __device__ void bp_pass(const float* src, float* dst, long n1, long t0, long ntr
       for (int i = 0; i < (int)len; i++) row[i] = step(row[i]);
     }
     __syncwarp();
-    const long i = (long)c * 32 + lane;
-    if (i < n1) {
-      float* d = dst + t0 * n1 + i;
+    float(*buf)[kBpPitch] = ring[q % kBpStages];
+    const long c0 = (long)c * 32;
+    if (VEC) {
+      if (c0 + vq < n1) {
+        float* d = dst + (t0 + vj) * n1 + c0 + vq;
+#pragma unroll
+        for (int m = 0; m < 8; m++)
+          if (vj + 4 * m < ntw)
+            *reinterpret_cast<float4*>(d + 4 * m * n1) =
+                *reinterpret_cast<const float4*>(&buf[vj + 4 * m][vq]);
+      }
+    } else if (c0 + lane < n1) {
+      float* d = dst + t0 * n1 + c0 + lane;
 #pragma unroll 8
-      for (int j = 0; j < ntw; j++) d[j * n1] = ring[q % kBpStages][j][lane];
+      for (int j = 0; j < ntw; j++) d[j * n1] = buf[j][lane];
     }
     __syncwarp();
   }
@@ -144,6 +193,7 @@ __device__ void bp_pass(const float* src, float* dst, long n1, long t0, long ntr
 // One warp per 32 traces, the plan's passes in order; the first reads `in`
 // (which may be `out`), the others read `out` back.  Each lane reads back
 // only the samples it stored itself.
+template <bool VEC>
 __global__ void __launch_bounds__(32) k_bandpass(const float* in, float* out, long n1, long ntr,
                                                  BpPlan plan) {
   __shared__ __align__(16) BpRing ring;
@@ -155,7 +205,7 @@ __global__ void __launch_bounds__(32) k_bandpass(const float* in, float* out, lo
     switch (code) {
 #define BP_CASE(L, F, N)                                         \
   case (L ? 8 : 0) + (F ? 4 : 0) + N:                            \
-    bp_pass<L, F, N>(src, out, n1, t0, ntr, P, ring);            \
+    bp_pass<VEC, L, F, N>(src, out, n1, t0, ntr, P, ring);       \
     break;
       BP_CASE(false, false, 1) BP_CASE(false, false, 2) BP_CASE(false, false, 3)
       BP_CASE(false, true, 0) BP_CASE(false, true, 1) BP_CASE(false, true, 2)
@@ -281,13 +331,20 @@ extern "C" int pwd_bandpass(const float* in, float* out, int n1, int n2, int n3,
                                        cudaMemcpyDeviceToDevice, st));
   }
   const unsigned grid = (unsigned)((ntr + 31) / 32);
+  // 16-byte copies when every trace starts on a 16-byte boundary
+  const bool vec = n1 % 4 == 0 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0;
   for (size_t p0 = 0; p0 < passes.size(); p0 += kBpPass) {
     BpPlan plan;
     memset(&plan, 0, sizeof plan);
     plan.npass = (int)std::min(passes.size() - p0, (size_t)kBpPass);
     for (int k = 0; k < plan.npass; k++) plan.p[k] = passes[p0 + k];
-    PWD_KERNEL(PWD_FAM_OTHER, st,
-               k_bandpass<<<grid, 32, 0, st>>>(p0 == 0 ? in : out, out, (long)n1, ntr, plan));
+    const float* src = p0 == 0 ? in : out;
+    if (vec)
+      PWD_KERNEL(PWD_FAM_OTHER, st,
+                 k_bandpass<true><<<grid, 32, 0, st>>>(src, out, (long)n1, ntr, plan));
+    else
+      PWD_KERNEL(PWD_FAM_OTHER, st,
+                 k_bandpass<false><<<grid, 32, 0, st>>>(src, out, (long)n1, ntr, plan));
     const int rc = cuda_status(cudaGetLastError());
     if (rc != PWD_OK) return rc;
   }
