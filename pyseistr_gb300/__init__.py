@@ -7,8 +7,10 @@ sm_103a kernels of libpwd_gb300.so:
     somean2dc, somf2dc             2-D structure-oriented mean / median
     somean3dc, somf3dc             3-D structure-oriented mean / median
     soint3dc                       3-D structure-oriented interpolation
+    soint2dc                       2-D structure-oriented interpolation
     dipc, csomean2d, csomf2d,      the reference's low-level positional
-    csomean3d, csomf3d, csoint3d   entries
+    csomean3d, csomf3d, csoint3d,  entries
+    csoint2d
     dip2dc_batch, somean2dc_batch, many sections of uneven size in one
     somf2dc_batch,                 launch sequence (same results as one
     dip_somean2d_batch,            call per section); the packed forms take
@@ -24,6 +26,7 @@ sm_103a kernels of libpwd_gb300.so:
 from .api import (  # noqa: F401
     bandpassc,
     cbp,
+    csoint2d,
     csoint3d,
     csomean2d,
     csomean3d,
@@ -40,6 +43,7 @@ from .api import (  # noqa: F401
     patch2d_inv,
     patch3d,
     patch3d_inv,
+    soint2dc,
     soint3dc,
     somean2dc,
     somean2dc_batch,

@@ -119,6 +119,31 @@ def csoint3d(din, mask, dipi, dipx, n1, n2, n3, nw, nj1, nj2, niter, drift, seed
     return out if as_t else out.cpu().numpy()
 
 
+def csoint2d(din, mask, dip1, dip2, n1, n2, nw, nj1, nj2, niter, drift, hasmask, twoplane, prec,
+             verb):
+    """csoint2d "OOOOiiiiiiiiiii" (soint2d_cfuns.c:2260).  Its default branch
+    (twoplane 0, prec 0: allpass21_lop inside ps_solver with the known mask
+    and x0) is csoint3d's operator and solver with n3 = 1 (the crossline
+    rows are empty), computed here by pwd_soint3d; the two-plane branch
+    without preconditioning returns din unchanged, as the reference's (its
+    solver call is commented out).  The preconditioned branches (prec 1:
+    predict_lop / predict2_lop in ps_solver_prec) are not built."""
+    if prec:
+        raise NotImplementedError("csoint2d: prec=1 (plane-wave construction "
+                                  "preconditioning) is not implemented")
+    n = n1 * n2
+    d, as_t = _to_dev_flat(din)
+    if d.numel() != n:
+        raise ValueError(f"csoint2d: din has {d.numel()} values, expected {n}")
+    if twoplane:
+        out = d.clone()
+    else:
+        m, _ = _to_dev_flat(mask)
+        p, _ = _to_dev_flat(dip1)
+        out = D.soint3d(d, m, p, p, n1, n2, 1, nw, nj1, nj2, niter, drift, 202223, hasmask, 0.0)
+    return out if as_t else out.cpu().numpy()
+
+
 # --------------------------------------------------------------------------
 # high-level entries
 # --------------------------------------------------------------------------
@@ -209,6 +234,31 @@ def soint3dc(din, mask, dipi, dipx, order=1, niter=100, njs=[1, 1], drift=0, see
     out = D.soint3d(d, m, pi, px, n1, n2, n3, order, njs[0], njs[1], niter, drift, seed, hasmask,
                     var)
     return _from_dev_flat(out, (n1, n2, n3), as_t)
+
+
+def soint2dc(din, mask, dip, order=1, niter=100, njs=[1, 1], drift=0, hasmask=1, twoplane=0,
+             prec=0, verb=1):
+    """2-D structure-oriented interpolation (soint2d.py:92): fills the
+    samples the mask marks unknown (mask 0, or din 0 when hasmask is 0) by
+    conjugate gradients on the plane-wave-destruction residual along the
+    slope field dip [n1, n2] (the first plane of a [n1, n2, 2] dip when
+    twoplane).  order = PWD accuracy order, njs = antialiasing steps, drift
+    = shift the filter by the rounded slope."""
+    n1, n2 = din.shape[:2]
+    dip1 = dip if twoplane == 0 else dip[:, :, 0]
+    d, as_t = _to_dev_flat(din)
+    if twoplane:
+        if prec:
+            raise NotImplementedError("soint2dc: prec=1 is not implemented")
+        return _from_dev_flat(d.clone(), (n1, n2), as_t)
+    if prec:
+        raise NotImplementedError("soint2dc: prec=1 (plane-wave construction "
+                                  "preconditioning) is not implemented")
+    m, _ = _to_dev_flat(mask)
+    p, _ = _to_dev_flat(dip1)
+    out = D.soint3d(d, m, p, p, n1, n2, 1, order, njs[0], njs[1], niter, drift, 202223, hasmask,
+                    0.0)
+    return _from_dev_flat(out, (n1, n2), as_t)
 
 
 # --------------------------------------------------------------------------
