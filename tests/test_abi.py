@@ -72,3 +72,28 @@ def test_calls_reject_bad_arguments_before_touching_the_gpu():
     assert lib.pwd_somf2d(fake, fake, fake, 50, 10, 1, 2, 5, 1, 2, 0.01, fake, 16, None) == _lib.PWD_EWORKSPACE
     assert lib.pwd_somf3d(fake, fake, fake, fake, 50, 10, 10, 2, 2, 200, 1, 2, 0.01, fake, 1 << 30, None) == _lib.PWD_ENOTSUP
     assert lib.pwd_soint3d(fake, None, fake, fake, fake, 8, 8, 8, 2, 1, 1, 5, 0, 1, 1, 0.0, fake, 1 << 30, None) == _lib.PWD_EINVAL
+
+
+def test_patch_and_bandpass_entries_check_arguments_on_the_host():
+    """pwd_patch_count is host arithmetic; invalid sizes and null pointers
+    come back as PWD_EINVAL before any launch."""
+    from oracle import patch_oracle as P
+
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+    for n, l, s in [((37, 29, 1), (8, 8, 1), (4, 4, 1)), ((13, 11, 9), (4, 4, 4), (2, 2, 2)),
+                    ((5, 30, 1), (8, 6, 1), (4, 3, 1)), ((2000, 5000, 1), (64, 64, 1), (32, 32, 1))]:
+        want = 1
+        for a in range(3):
+            want *= len(P.starts(n[a], l[a], s[a]))
+        assert lib.pwd_patch_count(*n, *l, *s) == want
+    assert lib.pwd_patch_count(8, 8, 1, 0, 4, 1, 2, 2, 1) == 0  # zero window
+    assert lib.pwd_patch_count(3, 40, 7, 5, 8, 2, 2, 6, 3) == 0  # an axis with no window
+    assert lib.pwd_patch(None, fake, 8, 8, 1, 4, 4, 1, 2, 2, 1, None) == _lib.PWD_EINVAL
+    assert lib.pwd_patch(fake, fake, 8, 8, 1, 4, 4, 1, 0, 2, 1, None) == _lib.PWD_EINVAL
+    assert lib.pwd_patch_inv(fake, None, 8, 8, 1, 4, 4, 1, 2, 2, 1, None) == _lib.PWD_EINVAL
+    assert lib.pwd_bandpass(None, fake, 100, 3, 1, 0.004, 0.0, 20.0, 6, 6, 0, None) == _lib.PWD_EINVAL
+    assert lib.pwd_bandpass(fake, fake, 0, 3, 1, 0.004, 0.0, 20.0, 6, 6, 0, None) == _lib.PWD_EINVAL
+    assert lib.pwd_bandpass(fake, fake, 100, 3, 0, 0.004, 0.0, 20.0, 6, 6, 0, None) == _lib.PWD_EINVAL
+    # in place with no cut at all: nothing to do, no CUDA call
+    assert lib.pwd_bandpass(fake, fake, 100, 3, 1, 0.004, 0.0, 125.0, 6, 6, 0, None) == _lib.PWD_OK
