@@ -58,6 +58,8 @@ def lib():
         L.orc_pwspray2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
         L.orc_pwspray3d_f32.argtypes = [_P, _P, _P, _P] + [_I] * 6
         L.orc_spray_median_f32.argtypes = [_P, _P, _I, _I, _L, _I, _I]
+        L.orc_sint2d_f32.argtypes = [_P, _P, _P, _P, _I, _I, _I, _I, _I, _F]
+        L.orc_sint3d_f32.argtypes = [_P, _P, _P, _P, _P] + [_I] * 8 + [_F]
         L.orc_bandpass_f32.argtypes = [_P, _P, _I, _L, _F, _F, _F, _I, _I, _I]
         _lib = L
     return _lib
@@ -225,3 +227,28 @@ def bandpass(din, dt, flo=0.0, fhi=0.5, nplo=6, nphi=6, phase=0):
                                   phase), "bandpass")
     return out.reshape(a.shape, order="F")
 
+
+
+def sint2d(din, mask, dip, niter=100, eps=0.01, ns=1, order=1):
+    """csint2d (pyseistr/src/soint2d_cfuns.c:2421-2523): sparse-data
+    interpolation of an (n1, n2) section, known samples where mask != 0."""
+    a = np.asarray(din, dtype=np.float32)
+    n1, n2 = a.shape
+    d, m, p = _flat(a, np.float32), _flat(mask, np.float32), _flat(dip, np.float32)
+    out = np.empty_like(d)
+    _check(lib().orc_sint2d_f32(_ptr(d), _ptr(p), _ptr(m), _ptr(out), n1, n2, niter, ns, order,
+                                eps), "sint2d")
+    return out.reshape(n1, n2, order="F")
+
+
+def sint3d(din, mask, dipi, dipx, niter=100, eps=0.01, ns1=1, ns2=1, order1=1, order2=1):
+    """csint3d (pyseistr/src/soint3d_cfuns.c:2510-2612): sparse-data
+    interpolation of an (n1, n2, n3) cube, known samples where mask != 0."""
+    a = np.asarray(din, dtype=np.float32)
+    n1, n2, n3 = a.shape
+    d, m = _flat(a, np.float32), _flat(mask, np.float32)
+    p, q = _flat(dipi, np.float32), _flat(dipx, np.float32)
+    out = np.empty_like(d)
+    _check(lib().orc_sint3d_f32(_ptr(d), _ptr(p), _ptr(q), _ptr(m), _ptr(out), n1, n2, n3, niter,
+                                ns1, ns2, order1, order2, eps), "sint3d")
+    return out.reshape(n1, n2, n3, order="F")

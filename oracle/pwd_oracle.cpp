@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 namespace orc {
@@ -915,6 +916,243 @@ static int somean2d(const R* din, const R* dip, R* dout, int n1, int n2, int n3,
   return ORC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Sparse-data interpolation, csint2d soint2d_cfuns.c:2421-2523: shaping-
+// regularised CG (ps_conjgrad :888-1012 with prec = NULL and a given initial
+// model) whose operator is the known-sample mask (ps_mask_lop :145-157) and
+// whose shaping is the normalised plane-wave smoothing (pwsmooth_* :2160-
+// 2240, the operator csomean2d applies, on pwspray :2038-2150).
+// ---------------------------------------------------------------------------
+template <class R>
+struct PwSmooth2 {
+  int n1 = 0, n2 = 0, ns = 0, ns2 = 0;
+  long n12 = 0;
+  Predict<R> pr;
+  std::vector<R> u, w, w1, t;
+  const R* pp = nullptr;
+  void init(int nr, int m1, int m2, int order, R eps) {
+    n1 = m1;
+    n2 = m2;
+    ns = nr;
+    ns2 = 2 * ns + 1;
+    n12 = (long)n1 * n2;
+    pr.init(n1, eps * eps, order, false);
+    u.assign(n12 * ns2, 0);
+    w.resize(ns2);
+    for (int is = 0; is < ns2; is++) w[is] = (R)(ns + 1 - std::abs(is - ns));
+    w1.assign(n12, 0);
+    t.assign(n12, 0);
+  }
+  // pwsmooth_lop: smooth (+)= S trace, or trace (+)= S' smooth
+  void lop(bool adj, bool add, R* trace, R* smooth) {
+    if (!add) {
+      R* z = adj ? trace : smooth;
+      for (long i = 0; i < n12; i++) z[i] = 0;
+    }
+    if (adj) {
+      for (int i2 = 0; i2 < n2; i2++)
+        for (int i1 = 0; i1 < n1; i1++) {
+          const R ws = w1[(long)i2 * n1 + i1];
+          for (int is = 0; is < ns2; is++)
+            u[((long)i2 * ns2 + is) * n1 + i1] = smooth[(long)i2 * n1 + i1] * w[is] * ws;
+        }
+      pwspray2(pr, true, n1, n2, ns, pp, trace, u.data());
+    } else {
+      pwspray2(pr, false, n1, n2, ns, pp, trace, u.data());
+      for (int i2 = 0; i2 < n2; i2++)
+        for (int i1 = 0; i1 < n1; i1++) {
+          const R ws = w1[(long)i2 * n1 + i1];
+          for (int is = 0; is < ns2; is++)
+            smooth[(long)i2 * n1 + i1] += u[((long)i2 * ns2 + is) * n1 + i1] * w[is] * ws;
+        }
+    }
+  }
+  // pwsmooth_set: the slope and the normalisation 1 / S 1
+  void set(const R* dip) {
+    pp = dip;
+    for (long i = 0; i < n12; i++) w1[i] = 1;
+    lop(false, false, w1.data(), t.data());
+    for (long i = 0; i < n12; i++) w1[i] = (t[i] != (R)0) ? (R)(1.0 / t[i]) : (R)0;
+  }
+};
+
+// ps_conjgrad with oper = the mask of `known`, shape = S, a given initial
+// model p (hasp0) and x, dat the same array (csint2d passes mm for both).
+template <class R, class Shape>
+static void conjgrad_masked(Shape& S, const std::vector<char>& known, long n, R eps1, R tol,
+                            R* p, R* x, int niter) {
+  const R eps = eps1 * eps1;
+  std::vector<R> r(n), sp(n), gp(n), sx(n), gx(n), sr(n), gr(n);
+  for (long i = 0; i < n; i++) r[i] = -x[i];  // r = -dat before x is overwritten
+  S.lop(false, false, p, x);                   // x = S p
+  for (long i = 0; i < n; i++)
+    if (known[i]) r[i] += x[i];                // r += M x
+  double gn, gnp = 0., alpha, beta, g0 = 0., dg = 0., r0;
+  r0 = dsdot(n, r.data(), r.data());
+  if (r0 == 0.) return;
+  for (int iter = 0; iter < niter; iter++) {
+    for (long i = 0; i < n; i++) gp[i] = eps * p[i];
+    for (long i = 0; i < n; i++) gx[i] = -eps * x[i];
+    for (long i = 0; i < n; i++)
+      if (known[i]) gx[i] += r[i];              // gx += M' r
+    S.lop(true, true, gp.data(), gx.data());    // gp += S' gx
+    S.lop(false, false, gp.data(), gx.data());  // gx = S gp
+    for (long i = 0; i < n; i++) gr[i] = 0;
+    for (long i = 0; i < n; i++)
+      if (known[i]) gr[i] += gx[i];             // gr = M gx
+    gn = dsdot(n, gp.data(), gp.data());
+    if (iter == 0) {
+      g0 = gn;
+      sp = gp;
+      sx = gx;
+      sr = gr;
+    } else {
+      alpha = gn / gnp;
+      dg = gn / g0;
+      if (alpha < (double)tol || dg < (double)tol) break;
+      const R a = (R)alpha;
+      saxpy(n, a, sp.data(), gp.data());
+      std::swap(sp, gp);
+      saxpy(n, a, sx.data(), gx.data());
+      std::swap(sx, gx);
+      saxpy(n, a, sr.data(), gr.data());
+      std::swap(sr, gr);
+    }
+    beta = dsdot(n, sr.data(), sr.data()) +
+           (double)eps * (dsdot(n, sp.data(), sp.data()) - dsdot(n, sx.data(), sx.data()));
+    alpha = -gn / beta;
+    const R a = (R)alpha;
+    saxpy(n, a, sp.data(), p);
+    saxpy(n, a, sx.data(), x);
+    saxpy(n, a, sr.data(), r.data());
+    gnp = gn;
+  }
+}
+
+template <class R>
+static int sint2d(const R* din, const R* dip, const R* mask, R* dout, int n1, int n2, int niter,
+                  int ns, int order, R eps) {
+  if (n1 < 4 || n2 < 1 || ns < 0 || order < 1 || order > 8 || niter < 0) return ORC_EINVAL;
+  const long n12 = (long)n1 * n2;
+  PwSmooth2<R> S;
+  S.init(ns, n1, n2, order, eps);
+  std::vector<R> xx(din, din + n12);
+  for (long i = 0; i < n12; i++) dout[i] = din[i];
+  std::vector<char> known(n12);
+  R lam = 0;
+  for (long i = 0; i < n12; i++) {
+    known[i] = mask[i] != (R)0;
+    if (known[i]) lam += (R)1.;
+  }
+  lam = std::sqrt(lam / (R)n12);
+  const R tol = (R)(10 * std::numeric_limits<float>::epsilon());
+  S.set(dip);
+  conjgrad_masked(S, known, n12, lam, tol, xx.data(), dout, niter);
+  return ORC_OK;
+}
+
+// csint3d soint3d_cfuns.c:2510-2612: the same CG with the 3-D smoothing
+// pwsmooth3_lop (:2157-2300): the 2-D smoothing along the inline slope on
+// every (n1, n2) slice, then along the crossline slope on every (n1, n3)
+// section (the cube transposed to [n2][n3][n1]); the adjoint in reverse,
+// adding into the model.
+template <class R>
+struct PwSmooth3 {
+  int n1 = 0, n2 = 0, n3 = 0, ns1 = 0, ns2 = 0, order1 = 0, order2 = 0;
+  R eps = 0;
+  const R* pi = nullptr;
+  std::vector<R> xd, itmp, itmp2, xtmp;  // xd: crossline slope as [n2][n3][n1]
+  PwSmooth2<R> S;
+  void init(int r1, int r2, int m1, int m2, int m3, int o1, int o2, R e, const R* dipi,
+            const R* dipx) {
+    n1 = m1;
+    n2 = m2;
+    n3 = m3;
+    ns1 = r1;
+    ns2 = r2;
+    order1 = o1;
+    order2 = o2;
+    eps = e;
+    pi = dipi;
+    const long n = (long)n1 * n2 * n3;
+    xd.resize(n);
+    itmp.assign(n, 0);
+    itmp2.assign(n, 0);
+    xtmp.assign(n, 0);
+    for (int i3 = 0; i3 < n3; i3++)
+      for (int i2 = 0; i2 < n2; i2++)
+        for (int i1 = 0; i1 < n1; i1++)
+          xd[i1 + (long)n1 * (i3 + (long)n3 * i2)] = dipx[i1 + (long)n1 * (i2 + (long)n2 * i3)];
+  }
+  long ixc(int i1, int i2, int i3) const { return i1 + (long)n1 * (i2 + (long)n2 * i3); }
+  long ixt(int i1, int i2, int i3) const { return i1 + (long)n1 * (i3 + (long)n3 * i2); }
+  void lop(bool adj, bool add, R* trace, R* smooth) {
+    const long n = (long)n1 * n2 * n3, n12 = (long)n1 * n2, n13 = (long)n1 * n3;
+    if (!add) {
+      R* z = adj ? trace : smooth;
+      for (long i = 0; i < n; i++) z[i] = 0;
+    }
+    if (adj) {
+      for (int i3 = 0; i3 < n3; i3++)
+        for (int i2 = 0; i2 < n2; i2++)
+          for (int i1 = 0; i1 < n1; i1++) xtmp[ixt(i1, i2, i3)] = smooth[ixc(i1, i2, i3)];
+      S.init(ns2, n1, n3, order2, eps);
+      for (int i2 = 0; i2 < n2; i2++) {
+        S.set(xd.data() + i2 * n13);
+        S.lop(true, false, itmp2.data() + i2 * n13, xtmp.data() + i2 * n13);
+      }
+      for (int i3 = 0; i3 < n3; i3++)
+        for (int i2 = 0; i2 < n2; i2++)
+          for (int i1 = 0; i1 < n1; i1++) itmp[ixc(i1, i2, i3)] = itmp2[ixt(i1, i2, i3)];
+      S.init(ns1, n1, n2, order1, eps);
+      for (int i3 = 0; i3 < n3; i3++) {
+        S.set(pi + i3 * n12);
+        S.lop(true, true, trace + i3 * n12, itmp.data() + i3 * n12);
+      }
+    } else {
+      S.init(ns1, n1, n2, order1, eps);
+      for (int i3 = 0; i3 < n3; i3++) {
+        S.set(pi + i3 * n12);
+        S.lop(false, false, trace + i3 * n12, itmp.data() + i3 * n12);
+      }
+      for (int i3 = 0; i3 < n3; i3++)
+        for (int i2 = 0; i2 < n2; i2++)
+          for (int i1 = 0; i1 < n1; i1++) itmp2[ixt(i1, i2, i3)] = itmp[ixc(i1, i2, i3)];
+      S.init(ns2, n1, n3, order2, eps);
+      for (int i2 = 0; i2 < n2; i2++) {
+        S.set(xd.data() + i2 * n13);
+        S.lop(false, false, itmp2.data() + i2 * n13, xtmp.data() + i2 * n13);
+      }
+      for (int i3 = 0; i3 < n3; i3++)
+        for (int i2 = 0; i2 < n2; i2++)
+          for (int i1 = 0; i1 < n1; i1++) smooth[ixc(i1, i2, i3)] += xtmp[ixt(i1, i2, i3)];
+    }
+  }
+};
+
+template <class R>
+static int sint3d(const R* din, const R* dipi, const R* dipx, const R* mask, R* dout, int n1,
+                  int n2, int n3, int niter, int ns1, int ns2, int order1, int order2, R eps) {
+  if (n1 < 4 || n2 < 1 || n3 < 1 || ns1 < 0 || ns2 < 0 || order1 < 1 || order1 > 8 ||
+      order2 < 1 || order2 > 8 || niter < 0)
+    return ORC_EINVAL;
+  const long n = (long)n1 * n2 * n3;
+  std::vector<R> xx(din, din + n);
+  for (long i = 0; i < n; i++) dout[i] = din[i];
+  std::vector<char> known(n);
+  R lam = 0;
+  for (long i = 0; i < n; i++) {
+    known[i] = mask[i] != (R)0;
+    if (known[i]) lam += (R)1.;
+  }
+  lam = std::sqrt(lam / (R)n);
+  PwSmooth3<R> S;
+  S.init(ns1, ns2, n1, n2, n3, order1, order2, eps, dipi, dipx);
+  const R tol = (R)(10 * std::numeric_limits<float>::epsilon());
+  conjgrad_masked(S, known, n, lam, tol, xx.data(), dout, niter);
+  return ORC_OK;
+}
+
 // sf_quantile sof_cfuns.c:1137-1163 (Hoare-style selection, a is changed)
 template <class R>
 static R quantile(int q, int n, R* a) {
@@ -1520,6 +1758,17 @@ int orc_somean2d_f32(const float* d, const float* p, float* out, int n1, int n2,
                      int order, float eps, int adj) {
   DefaultFpEnv fpenv;
   return orc::somean2d<float>(d, p, out, n1, n2, n3, ns, order, eps, adj);
+}
+int orc_sint2d_f32(const float* d, const float* p, const float* m, float* out, int n1, int n2,
+                   int niter, int ns, int order, float eps) {
+  DefaultFpEnv fpenv;
+  return orc::sint2d<float>(d, p, m, out, n1, n2, niter, ns, order, eps);
+}
+int orc_sint3d_f32(const float* d, const float* pi, const float* px, const float* m, float* out,
+                   int n1, int n2, int n3, int niter, int ns1, int ns2, int order1, int order2,
+                   float eps) {
+  DefaultFpEnv fpenv;
+  return orc::sint3d<float>(d, pi, px, m, out, n1, n2, n3, niter, ns1, ns2, order1, order2, eps);
 }
 int orc_somean2d_f64(const double* d, const double* p, double* out, int n1, int n2, int n3,
                      int ns, int order, double eps, int adj) {
