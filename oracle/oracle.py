@@ -60,6 +60,7 @@ def lib():
         L.orc_spray_median_f32.argtypes = [_P, _P, _I, _I, _L, _I, _I]
         L.orc_sint2d_f32.argtypes = [_P, _P, _P, _P, _I, _I, _I, _I, _I, _F]
         L.orc_sint3d_f32.argtypes = [_P, _P, _P, _P, _P] + [_I] * 8 + [_F]
+        L.orc_paint2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
         L.orc_bandpass_f32.argtypes = [_P, _P, _I, _L, _F, _F, _F, _I, _I, _I]
         _lib = L
     return _lib
@@ -252,3 +253,17 @@ def sint3d(din, mask, dipi, dipx, niter=100, eps=0.01, ns1=1, ns2=1, order1=1, o
     _check(lib().orc_sint3d_f32(_ptr(d), _ptr(p), _ptr(q), _ptr(m), _ptr(out), n1, n2, n3, niter,
                                 ns1, ns2, order1, order2, eps), "sint3d")
     return out.reshape(n1, n2, n3, order="F")
+
+
+def paint2d(dip, seed, order=1, i0=0, eps=0.01):
+    """cpaint2d (pyseistr/src/paint_cfuns.c:1861-1940): plane-wave painting
+    of the seed trace from trace i0 along the slope dip (n1, n2)."""
+    p = np.asarray(dip, dtype=np.float32)
+    n1, n2 = p.shape
+    t = _flat(seed, np.float32)
+    if t.size != n1:
+        raise ValueError(f"paint2d: the seed trace has {t.size} samples, expected {n1}")
+    out = np.empty(n1 * n2, dtype=np.float32)
+    _check(lib().orc_paint2d_f32(_ptr(_flat(p, np.float32)), _ptr(t), _ptr(out), n1, n2, order,
+                                 i0, eps), "paint2d")
+    return out.reshape(n1, n2, order="F")

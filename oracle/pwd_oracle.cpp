@@ -1153,6 +1153,31 @@ static int sint3d(const R* din, const R* dipi, const R* dipx, const R* mask, R* 
   return ORC_OK;
 }
 
+// Plane-wave painting, cpaint2d paint_cfuns.c:1861-1940 (called by pwpaintc
+// and rgt, rgt.py:4-87): the seed trace placed at trace i0 and carried
+// trace by trace to both ends by the PWD prediction step (predict_step
+// :1247-1274), leftwards along the slope of the trace it leaves, rightwards
+// along the slope of the trace before the one it reaches.
+template <class R>
+static int paint2d(const R* dip, const R* seed, R* out, int n1, int n2, int order, int i0,
+                   R eps) {
+  if (n1 < 4 || n2 < 1 || order < 1 || order > 8 || i0 < 0 || i0 >= n2) return ORC_EINVAL;
+  Predict<R> pr;
+  pr.init(n1, eps * eps, order, false);
+  std::vector<R> tr(seed, seed + n1);
+  for (int i1 = 0; i1 < n1; i1++) out[(long)i0 * n1 + i1] = tr[i1];
+  for (int i2 = i0 - 1; i2 >= 0; i2--) {
+    pr.step(false, false, tr.data(), dip + (long)i2 * n1);
+    for (int i1 = 0; i1 < n1; i1++) out[(long)i2 * n1 + i1] = tr[i1];
+  }
+  for (int i1 = 0; i1 < n1; i1++) tr[i1] = out[(long)i0 * n1 + i1];
+  for (int i2 = i0 + 1; i2 < n2; i2++) {
+    pr.step(false, true, tr.data(), dip + (long)(i2 - 1) * n1);
+    for (int i1 = 0; i1 < n1; i1++) out[(long)i2 * n1 + i1] = tr[i1];
+  }
+  return ORC_OK;
+}
+
 // sf_quantile sof_cfuns.c:1137-1163 (Hoare-style selection, a is changed)
 template <class R>
 static R quantile(int q, int n, R* a) {
@@ -1769,6 +1794,11 @@ int orc_sint3d_f32(const float* d, const float* pi, const float* px, const float
                    float eps) {
   DefaultFpEnv fpenv;
   return orc::sint3d<float>(d, pi, px, m, out, n1, n2, n3, niter, ns1, ns2, order1, order2, eps);
+}
+int orc_paint2d_f32(const float* dip, const float* seed, float* out, int n1, int n2, int order,
+                    int i0, float eps) {
+  DefaultFpEnv fpenv;
+  return orc::paint2d<float>(dip, seed, out, n1, n2, order, i0, eps);
 }
 int orc_somean2d_f64(const double* d, const double* p, double* out, int n1, int n2, int n3,
                      int ns, int order, double eps, int adj) {
