@@ -61,6 +61,7 @@ def lib():
         L.orc_sint2d_f32.argtypes = [_P, _P, _P, _P, _I, _I, _I, _I, _I, _F]
         L.orc_sint3d_f32.argtypes = [_P, _P, _P, _P, _P] + [_I] * 8 + [_F]
         L.orc_paint2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
+        L.orc_coh_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F, _I, _P, _P]
         L.orc_bandpass_f32.argtypes = [_P, _P, _I, _L, _F, _F, _F, _I, _I, _I]
         _lib = L
     return _lib
@@ -267,3 +268,23 @@ def paint2d(dip, seed, order=1, i0=0, eps=0.01):
     _check(lib().orc_paint2d_f32(_ptr(_flat(p, np.float32)), _ptr(t), _ptr(out), n1, n2, order,
                                  i0, eps), "paint2d")
     return out.reshape(n1, n2, order="F")
+
+
+class Coherence:
+    """cohc_fb (pyseistr/src/coh_cfuns.c:415-545): forward (forw 1: model
+    [nt, nv] -> data [nt, nh]) and adjoint coherence (forw -1: data ->
+    model) Radon operators.  Keeps the parabolic type's hmax across calls,
+    as the reference's file-scope static does within one process."""
+
+    def __init__(self):
+        self.hmax = np.zeros(1, dtype=np.float32)
+
+    def __call__(self, din, v, h, typ, nt, dt, forw):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        h = np.ascontiguousarray(h, dtype=np.float32)
+        nv, nh = v.size, h.size
+        x = _flat(din, np.float32)
+        out = np.empty(nt * (nh if forw == 1 else nv), dtype=np.float32)
+        _check(lib().orc_coh_f32(_ptr(x), _ptr(v), _ptr(h), typ, nt, nv, nh, dt, forw, _ptr(out),
+                                 _ptr(self.hmax)), "coh")
+        return out.reshape(nt, -1, order="F")

@@ -1178,6 +1178,81 @@ static int paint2d(const R* dip, const R* seed, R* out, int n1, int n2, int orde
   return ORC_OK;
 }
 
+// Radon coherence, cohc_fb coh_cfuns.c:415-545 with coh_init2 :158-179 and
+// coh :181-225 (called by cohc, das.py:92).  Forward (forw 1): data[ih][it]
+// += model[iv][itau] along t(itau, ih, iv) (linear itau dt + h v, parabolic
+// itau dt + h^2 v / hmax^2, hyperbolic sqrt(tau^2 + (h/v)^2)); adjoint
+// (forw -1): the stack num and the energy den of the data along the same
+// curves and model = num^2 / (nh den + 1e-16).  Sample index floor(t/dt) + 1
+// is used as the reference uses it: up to nt, which is the next trace's
+// first sample (flat indexing).  On the last trace that is one past the
+// data array, which the reference writes (forward; its output never shows
+// it, dropped here) or reads (adjoint; an undefined value, so the model
+// samples whose stack includes it are NaN here).  The parabolic type's hmax
+// is the reference's file-scope static (never reset, set to the signed
+// offset of the largest magnitude): the caller passes and keeps it.
+static int coh_radon(const float* in, const float* v, const float* h, int typ, int nt, int nv,
+                     int nh, float dt, int forw, float* out, float* hmax) {
+  if (nt < 1 || nv < 1 || nh < 1 || (forw != 1 && forw != -1)) return ORC_EINVAL;
+  if (typ != 1 && typ != 2 && typ != 3) typ = 1;
+  if (typ == 2)
+    for (int i = 0; i < nh; i++)
+      if (*hmax < std::fabs((double)h[i])) *hmax = h[i];
+  const long ndata = (long)nt * nh, nmod = (long)nt * nv;
+  // the sample indices first, so that a refused call writes nothing
+  std::vector<int> its((size_t)nt * nh * nv);
+  for (int itau = 0; itau < nt; itau++)
+    for (int ih = 0; ih < nh; ih++)
+      for (int iv = 0; iv < nv; iv++) {
+        float t = 0.f;
+        if (typ == 1) t = (float)itau * dt + h[ih] * v[iv];
+        if (typ == 2) t = (float)itau * dt + h[ih] * h[ih] * v[iv] / *hmax / *hmax;
+        if (typ == 3) {
+          const float tau = (float)itau * dt, hv = h[ih] / v[iv];
+          t = std::sqrt(tau * tau + hv * hv);
+        }
+        const float fl = std::floor(t / dt) + 1;
+        if (!(std::fabs(fl) < 2.0e9f)) return ORC_EINVAL;
+        its[((size_t)itau * nh + ih) * nv + iv] = (int)fl;
+      }
+  if (forw == 1) {
+    for (long i = 0; i < ndata; i++) out[i] = 0.f;
+    for (int itau = 0; itau < nt; itau++)
+      for (int ih = 0; ih < nh; ih++)
+        for (int iv = 0; iv < nv; iv++) {
+          const int it = its[((size_t)itau * nh + ih) * nv + iv];
+          const long id = (long)ih * nt + it;
+          if (it <= nt && it + 1 > 0 && id < ndata) out[id] += in[(long)iv * nt + itau];
+        }
+    return ORC_OK;
+  }
+  std::vector<float> num(nmod, 0.f), den(nmod, 0.f);
+  std::vector<char> undefined(nmod, 0);
+  for (int itau = 0; itau < nt; itau++)
+    for (int ih = 0; ih < nh; ih++)
+      for (int iv = 0; iv < nv; iv++) {
+        const int it = its[((size_t)itau * nh + ih) * nv + iv];
+        if (it <= nt && it + 1 > 0) {
+          const long id = (long)ih * nt + it, m = (long)iv * nt + itau;
+          if (id >= ndata) {
+            undefined[m] = 1;
+            continue;
+          }
+          const float y = in[id];
+          num[m] = num[m] + y;
+          den[m] = den[m] + y * y;
+        }
+      }
+  for (int itau = 0; itau < nt; itau++)
+    for (int iv = 0; iv < nv; iv++) {
+      const long m = (long)iv * nt + itau;
+      out[m] = undefined[m] ? std::numeric_limits<float>::quiet_NaN()
+                            : (float)((double)(num[m] * num[m]) /
+                                      ((double)((float)nh * den[m]) + 0.0000000000000001));
+    }
+  return ORC_OK;
+}
+
 // sf_quantile sof_cfuns.c:1137-1163 (Hoare-style selection, a is changed)
 template <class R>
 static R quantile(int q, int n, R* a) {
@@ -1799,6 +1874,11 @@ int orc_paint2d_f32(const float* dip, const float* seed, float* out, int n1, int
                     int i0, float eps) {
   DefaultFpEnv fpenv;
   return orc::paint2d<float>(dip, seed, out, n1, n2, order, i0, eps);
+}
+int orc_coh_f32(const float* in, const float* v, const float* h, int typ, int nt, int nv, int nh,
+                float dt, int forw, float* out, float* hmax) {
+  DefaultFpEnv fpenv;
+  return orc::coh_radon(in, v, h, typ, nt, nv, nh, dt, forw, out, hmax);
 }
 int orc_somean2d_f64(const double* d, const double* p, double* out, int n1, int n2, int n3,
                      int ns, int order, double eps, int adj) {
