@@ -287,6 +287,29 @@ int pwd_patch_inv(const float *x, float *a, int n1, int n2, int n3, int l1, int 
 int pwd_bandpass(const float *in, float *out, int n1, int n2, int n3, float d1, float flo,
                  float fhi, int nplo, int nphi, int phase, pwd_stream_t stream);
 
+/* ---- Radon coherence (pyseistr/das.py cohc, src/coh_cfuns.c cohc_fb) ----
+ * Replaces cohc_fb (coh_cfuns.c:415, argument tuple "OOOiiiifii" less the
+ * verb flag) with coh_init2 (:158) and coh (:181).  Model [nv][nt], data
+ * [nh][nt], column-major; v[nv] curve parameters, h[nh] offsets; typ 1
+ * linear (t = itau dt + h v), 2 parabolic (itau dt + h^2 v / hmax / hmax),
+ * 3 hyperbolic (sqrt(tau^2 + (h / v)^2)), any other value linear; sample
+ * floor(t / dt) + 1 for 0 <= it <= nt, as flat indices into the data (it = nt
+ * is the next trace's first sample).  forw = 1: `in` is the model, `out` the
+ * data (the terms added in the reference's order; the past-the-end sample
+ * of the last trace dropped).  forw = -1: `in` is the data, `out` the model
+ * num^2 / (nh den + 1e-16) of the stack num and energy den along each
+ * curve.  Where a curve reaches past the end of the data (sample nt of the
+ * last trace) the reference reads whatever follows its array (undefined:
+ * NaN or garbage); that sample reads as 0 here.  Results are bit-identical
+ * to cohc_fb's on every other sample.  `hmax` is the parabolic normaliser that the reference keeps
+ * in a file-scope static across calls (updated from h by coh_init2); the
+ * caller keeps and passes it.  Curves whose sample index is NaN or at least
+ * 2e9 in magnitude add nothing (the reference converts them to int with an
+ * undefined result; the Python layer refuses them).  Device pointers; no
+ * workspace; `out` must not overlap `in`. */
+int pwd_coherence(const float *in, const float *v, const float *h, int typ, int nt, int nv,
+                  int nh, float dt, int forw, float hmax, float *out, pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

@@ -20,12 +20,17 @@ sm_103a kernels of libpwd_gb300.so:
     patch2d_inv, patch3d_inv       overlap-add inverse (pyseistr/patch.py)
     bandpassc, cbp                 Butterworth band-pass along each trace
                                    (pyseistr/bp.py)
+    cohc, cohc_fb                  time-domain Radon coherence along
+                                   linear, parabolic or hyperbolic curves
+                                   (pyseistr/das.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
 from .api import (  # noqa: F401
     bandpassc,
     cbp,
+    cohc,
+    cohc_fb,
     csoint2d,
     csoint3d,
     csomean2d,

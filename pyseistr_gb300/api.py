@@ -509,3 +509,114 @@ def bandpassc(din, dt, flo=0, fhi=0.5, nplo=6, nphi=6, phase=0, verb=1):
     if n3 == 1:
         dout = dout.squeeze() if as_t else np.squeeze(dout)
     return dout
+
+
+# --------------------------------------------------------------------------
+# Radon coherence (das.py cohc / coh_cfuns.c cohc_fb)
+# --------------------------------------------------------------------------
+class _CohState:
+    """The parabolic normaliser hmax, which the reference keeps in a
+    file-scope static of coh_cfuns.c for the life of the process: it starts
+    at 0 and coh_init2 (coh_cfuns.c:158-179) updates it from every parabolic
+    call's offsets (to the signed offset h[i] whenever hmax < |h[i]|)."""
+
+    def __init__(self):
+        self.hmax = np.float32(0.0)
+
+    def update(self, h):
+        hm = float(self.hmax)
+        for x in h.tolist():
+            if hm < abs(x):
+                hm = x
+        self.hmax = np.float32(hm)
+
+
+coh_state = _CohState()
+
+
+def _coh_indices_usable(v, h, typ, nt, dt, hmax):
+    """Whether every curve's sample index floor(t / dt) + 1 is a finite value
+    below 2e9 in magnitude, evaluated in float32 as the kernels do.  The
+    index is monotone along each curve (in itau), so its two ends decide."""
+    f32 = np.float32
+    dt = f32(dt)
+    hh, vv = h[:, None], v[None, :]
+    with np.errstate(all="ignore"):
+        for itau in (0, nt - 1):
+            if typ == 2:
+                t = f32(itau) * dt + hh * hh * vv / hmax / hmax
+            elif typ == 3:
+                tau = f32(itau) * dt
+                hv = hh / vv
+                t = np.sqrt(tau * tau + hv * hv)
+            else:
+                t = f32(itau) * dt + hh * vv
+            fl = np.floor(t / dt) + f32(1)
+            if not (np.abs(fl) < f32(2.0e9)).all():
+                return False
+    return True
+
+
+def _host_f32(a, name):
+    if isinstance(a, torch.Tensor):
+        a = a.detach().cpu().numpy()
+    a = np.asarray(a, dtype=np.float32).reshape(-1)
+    return np.ascontiguousarray(a)
+
+
+def cohc_fb(din, v, h, typ, nt, nv, nh, dt, forw, verb):
+    """cohc_fb "OOOiiiifii" (coh_cfuns.c:415): forw = 1 maps the flat model
+    [nv][nt] to the flat data [nh][nt], forw = -1 the data to the coherence
+    model num^2 / (nh den + 1e-16); typ 1 linear, 2 parabolic, 3 hyperbolic
+    (others linear).  Returns a flat float32 array (a CUDA tensor for a
+    tensor in).  A curve reaching past the end of the data (sample nt of the
+    last trace), where the reference reads whatever follows its array, reads
+    0 there.  Raises ValueError for forw other
+    than 1 or -1, for fewer values than the sizes name (the reference reads
+    past its arrays), and for curves with no usable sample index (NaN, or
+    2e9 samples or more; the reference's int conversion is undefined)."""
+    typ, nt, nv, nh, forw = int(typ), int(nt), int(nv), int(nh), int(forw)
+    if verb:
+        print("typ=%d,nt0=%d,nv0=%d,nh0=%d,dt0=%g,forw=%d,verb=%d"
+              % (typ, nt, nv, nh, float(np.float32(dt)), forw, verb))
+    if forw not in (1, -1):
+        raise ValueError(f"cohc_fb: forw must be 1 or -1, got {forw}")
+    if nt < 1 or nv < 1 or nh < 1:
+        raise ValueError("cohc_fb: nt, nv and nh must be positive")
+    vh, hh = _host_f32(v, "v"), _host_f32(h, "h")
+    if vh.size < nv or hh.size < nh:
+        raise ValueError(f"cohc_fb: {vh.size} velocities and {hh.size} offsets, expected "
+                         f"{nv} and {nh}")
+    vh, hh = vh[:nv].copy(), hh[:nh].copy()
+    if typ not in (1, 2, 3):
+        typ = 1
+    if typ == 2:
+        coh_state.update(hh)
+    if not _coh_indices_usable(vh, hh, typ, nt, dt, coh_state.hmax):
+        raise ValueError("cohc_fb: curve sample indices not finite or beyond 2e9 samples")
+    t, as_t = _to_dev_flat(din)
+    need = nt * (nv if forw == 1 else nh)
+    if t.numel() < need:
+        raise ValueError(f"cohc_fb: din has {t.numel()} values, expected {need}")
+    t = t[:need].contiguous()
+    dev = t.device
+    vt = torch.from_numpy(vh).to(dev)
+    ht = torch.from_numpy(hh).to(dev)
+    out = D.coherence(t, vt, ht, typ, nt, dt, forw, coh_state.hmax)
+    return out if as_t else out.cpu().numpy()
+
+
+def cohc(din, par, operator=-1, verb=0):
+    """cohc (das.py:92): time-domain Radon coherence.  par holds 'h'
+    (offsets), 'v' (curve parameters), 'nt', 'dt' and 'typ'; operator 1 is
+    the forward map of an (nt, nv) model to (nt, nh) data, -1 (the default)
+    the coherence of (nt, nh) data as an (nt, nv) model; a CUDA tensor in
+    gives a CUDA tensor out."""
+    h, v = _host_f32(par["h"], "h"), _host_f32(par["v"], "v")
+    nt, dt, typ = int(par["nt"]), par["dt"], par["typ"]
+    nh, nv = h.size, v.size
+    dout = cohc_fb(din, v, h, typ, nt, nv, nh, dt, operator, verb)
+    ncol = nh if operator == 1 else nv
+    if isinstance(dout, torch.Tensor):
+        return dout.view(ncol, nt).t()
+    return dout.reshape(nt, ncol, order="F")

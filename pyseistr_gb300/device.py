@@ -342,3 +342,20 @@ def bandpass(d, n, dt, flo, fhi, nplo, nphi, phase, out=None):
                               float(fhi), int(nplo), int(nphi), int(phase), _stream()),
                "bandpass")
     return out
+
+
+def coherence(x, v, h, typ, nt, dt, forw, hmax, out=None):
+    """Radon coherence (pwd_coherence) of the flat column-major CUDA float32
+    array `x`: forw = 1 maps the model [nv][nt] to the data [nh][nt], forw =
+    -1 the data to the coherence model; v, h CUDA float32 vectors; hmax the
+    parabolic normaliser kept by the caller."""
+    L = _lib.load()
+    nt, nv, nh = int(nt), int(v.numel()), int(h.numel())
+    x = _as_flat(x, nt * (nv if forw == 1 else nh), "x")
+    v = _as_flat(v, nv, "v")
+    h = _as_flat(h, nh, "h")
+    if out is None:
+        out = torch.empty(nt * (nh if forw == 1 else nv), dtype=torch.float32, device=x.device)
+    _lib.check(L.pwd_coherence(_ptr(x), _ptr(v), _ptr(h), int(typ), nt, nv, nh, float(dt),
+                               int(forw), float(hmax), _ptr(out), _stream()), "coherence")
+    return out

@@ -97,3 +97,16 @@ def test_patch_and_bandpass_entries_check_arguments_on_the_host():
     assert lib.pwd_bandpass(fake, fake, 100, 3, 0, 0.004, 0.0, 20.0, 6, 6, 0, None) == _lib.PWD_EINVAL
     # in place with no cut at all: nothing to do, no CUDA call
     assert lib.pwd_bandpass(fake, fake, 100, 3, 1, 0.004, 0.0, 125.0, 6, 6, 0, None) == _lib.PWD_OK
+
+
+def test_coherence_entry_checks_arguments_on_the_host():
+    """Null pointers, empty sizes and an operator other than 1 / -1 come back
+    as PWD_EINVAL before any launch."""
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+    ok = _lib.PWD_EINVAL
+    assert lib.pwd_coherence(None, fake, fake, 1, 10, 2, 2, 0.004, -1, 0.0, fake, None) == ok
+    assert lib.pwd_coherence(fake, fake, fake, 1, 0, 2, 2, 0.004, -1, 0.0, fake, None) == ok
+    assert lib.pwd_coherence(fake, fake, fake, 1, 10, 0, 2, 0.004, 1, 0.0, fake, None) == ok
+    assert lib.pwd_coherence(fake, fake, fake, 1, 10, 2, 0, 0.004, 1, 0.0, fake, None) == ok
+    assert lib.pwd_coherence(fake, fake, fake, 2, 10, 2, 2, 0.004, 0, 0.0, fake, None) == ok
