@@ -310,6 +310,23 @@ int pwd_bandpass(const float *in, float *out, int n1, int n2, int n3, float d1, 
 int pwd_coherence(const float *in, const float *v, const float *h, int typ, int nt, int nv,
                   int nh, float dt, int forw, float hmax, float *out, pwd_stream_t stream);
 
+/* ---- Plane-wave painting (pyseistr/rgt.py pwpaintc, rgt; src/paint_cfuns.c
+ * cpaint2d) ---------------------------------------------------------------
+ * Replaces cpaint2d (paint_cfuns.c:1861, argument tuple "OOiiiifi" less the
+ * verb flag): the seed trace seed[n1] placed at trace i0 of out[n2][n1] and
+ * carried to both ends by the PWD prediction step along the slopes
+ * dip[n2][n1] (leftwards along the slope of the trace reached, rightwards
+ * along the slope of the trace before it), with accuracy order 1..4 and
+ * regularisation eps (squared, as predict_init takes it).  Results are
+ * bit-identical to cpaint2d's.  Serial along the traces: one thread per
+ * side of the section.  Device pointers; the workspace holds both threads'
+ * band arrays (pwd_paint2d_workspace_size bytes, 0 for n1 < 4 or an order
+ * outside 1..4); i0 outside [0, n2) is PWD_EINVAL (the reference writes out
+ * of bounds). */
+size_t pwd_paint2d_workspace_size(int n1, int order);
+int pwd_paint2d(const float *dip, const float *seed, float *out, int n1, int n2, int order,
+                int i0, float eps, void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

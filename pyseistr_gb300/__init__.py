@@ -23,6 +23,8 @@ sm_103a kernels of libpwd_gb300.so:
     cohc, cohc_fb                  time-domain Radon coherence along
                                    linear, parabolic or hyperbolic curves
                                    (pyseistr/das.py)
+    pwpaintc, rgt, cpaint2d        plane-wave painting of a seed trace and
+                                   relative geological time (pyseistr/rgt.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -31,6 +33,7 @@ from .api import (  # noqa: F401
     cbp,
     cohc,
     cohc_fb,
+    cpaint2d,
     csoint2d,
     csoint3d,
     csomean2d,
@@ -48,6 +51,8 @@ from .api import (  # noqa: F401
     patch2d_inv,
     patch3d,
     patch3d_inv,
+    pwpaintc,
+    rgt,
     soint2dc,
     soint3dc,
     somean2dc,

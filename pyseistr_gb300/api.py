@@ -620,3 +620,52 @@ def cohc(din, par, operator=-1, verb=0):
     if isinstance(dout, torch.Tensor):
         return dout.view(ncol, nt).t()
     return dout.reshape(nt, ncol, order="F")
+
+
+# --------------------------------------------------------------------------
+# plane-wave painting (rgt.py / paint_cfuns.c cpaint2d)
+# --------------------------------------------------------------------------
+def cpaint2d(dip, trace, n1, n2, order, i0, eps, verb):
+    """cpaint2d "OOiiiifi" (paint_cfuns.c:1861): the flat column-major slopes
+    dip (n1 n2 values) and the seed trace (n1 values) painted from trace i0;
+    returns the flat float32 section (a CUDA tensor for a tensor in).  Prints
+    the reference's parameter line (it prints it whatever verb is).  Raises
+    ValueError where the reference prints "Dimension mismatch" and returns
+    NULL, for a seed of fewer than n1 values and for i0 outside [0, n2)
+    (the reference reads and writes out of bounds there)."""
+    n1, n2, order, i0 = int(n1), int(n2), int(order), int(i0)
+    print("n1=%d,n2=%d,order=%d,i0=%d,eps=%g,verb=%d"
+          % (n1, n2, order, i0, float(np.float32(eps)), int(verb)))
+    p, as_t = _to_dev_flat(dip)
+    if p.numel() != n1 * n2:
+        raise ValueError(f"Dimension mismatch, N_input = {p.numel()}, N_data = {n1 * n2}")
+    t, _ = _to_dev_flat(trace)
+    if t.numel() < n1:
+        raise ValueError(f"cpaint2d: the seed trace has {t.numel()} values, expected {n1}")
+    if not 0 <= i0 < n2:
+        raise ValueError(f"cpaint2d: reference trace i0 = {i0} outside [0, {n2})")
+    if n1 < 4:
+        raise ValueError("cpaint2d: n1 must be at least 4")
+    out = D.paint2d(p, t[:n1].contiguous(), n1, n2, order, i0, eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def pwpaintc(dip, trace, order=1, i0=0, eps=0.01, verb=False):
+    """pwpaintc (rgt.py:51): plane-wave painting of the seed trace along the
+    (n1, n2) slopes dip from trace i0; returns the (n1, n2) painted section
+    (a CUDA tensor for a tensor in)."""
+    n1, n2 = (int(x) for x in dip.shape)
+    dout = cpaint2d(dip, trace, n1, n2, order, i0, eps, verb)
+    if isinstance(dout, torch.Tensor):
+        return _from_dev_flat(dout, (n1, n2), True)
+    return dout.reshape(n1, n2, order="F")
+
+
+def rgt(dip, o1=0, d1=0.004, order=1, i0=0, eps=0.01, verb=False):
+    """rgt (rgt.py:4): relative geological time, the time axis o1 + d1 i1
+    painted along the slopes dip from trace i0."""
+    n1 = int(dip.shape[0])
+    trace = np.linspace(0, d1 * (n1 - 1), n1) + o1
+    if isinstance(dip, torch.Tensor):
+        trace = torch.from_numpy(trace.astype(np.float32)).to(dip.device)
+    return pwpaintc(dip, trace, order=order, i0=i0, eps=eps, verb=verb)

@@ -359,3 +359,19 @@ def coherence(x, v, h, typ, nt, dt, forw, hmax, out=None):
     _lib.check(L.pwd_coherence(_ptr(x), _ptr(v), _ptr(h), int(typ), nt, nv, nh, float(dt),
                                int(forw), float(hmax), _ptr(out), _stream()), "coherence")
     return out
+
+
+def paint2d(dip, seed, n1, n2, order, i0, eps, out=None, workspace=None):
+    """Plane-wave painting (pwd_paint2d) of the seed trace (CUDA float32,
+    n1 samples) from trace i0 along the flat column-major slopes `dip` of an
+    (n1, n2) section; returns the flat painted section."""
+    L = _lib.load()
+    n1, n2, order, i0 = int(n1), int(n2), int(order), int(i0)
+    dip = _as_flat(dip, n1 * n2, "dip")
+    seed = _as_flat(seed, n1, "seed")
+    ws = _workspace(L.pwd_paint2d_workspace_size(n1, order), dip.device, workspace)
+    if out is None:
+        out = torch.empty(n1 * n2, dtype=torch.float32, device=dip.device)
+    _lib.check(L.pwd_paint2d(_ptr(dip), _ptr(seed), _ptr(out), n1, n2, order, i0, float(eps),
+                             _ptr(ws), ws.numel() * ws.element_size(), _stream()), "paint2d")
+    return out

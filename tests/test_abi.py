@@ -110,3 +110,19 @@ def test_coherence_entry_checks_arguments_on_the_host():
     assert lib.pwd_coherence(fake, fake, fake, 1, 10, 0, 2, 0.004, 1, 0.0, fake, None) == ok
     assert lib.pwd_coherence(fake, fake, fake, 1, 10, 2, 0, 0.004, 1, 0.0, fake, None) == ok
     assert lib.pwd_coherence(fake, fake, fake, 2, 10, 2, 2, 0.004, 0, 0.0, fake, None) == ok
+
+
+def test_paint_entry_checks_arguments_on_the_host():
+    """Workspace query and argument checks of pwd_paint2d, before any launch."""
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+    assert lib.pwd_paint2d_workspace_size(3, 2) == 0
+    assert lib.pwd_paint2d_workspace_size(100, 5) == 0
+    need = lib.pwd_paint2d_workspace_size(100, 2)
+    assert need >= 2 * 15 * 100 * 4 and need % 256 == 0
+    assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 10, 0.1, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, -1, 0.1, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_paint2d(fake, fake, fake, 3, 10, 2, 0, 0.1, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 5, 0, 0.1, fake, need, None) == _lib.PWD_ENOTSUP
+    assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, fake, need - 256, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, ctypes.c_void_p(300), need, None) == _lib.PWD_EWORKSPACE

@@ -1,0 +1,94 @@
+"""The host layer of the coherence and painting rows (argument handling,
+flattening, reshapes, the parabolic hmax state) through the GPU tests' own
+checks, on the CPU: the two device wrappers are replaced, for these tests
+only, by the kernels' per-thread code run on the CPU (tests/emu), and the
+host-to-device copy by a CPU tensor.  The library itself has no CPU path."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+
+
+def _build(tmp, name):
+    so = str(tmp / f"lib{name}.so")
+    subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-o", so,
+                    os.path.join(HERE, "emu", f"{name}.cpp")], check=True)
+    return ctypes.CDLL(so)
+
+
+@pytest.fixture(scope="module")
+def emulated(tmp_path_factory):
+    tmp = tmp_path_factory.mktemp("api_emu")
+    coh, paint = _build(tmp, "coh_emu"), _build(tmp, "paint_emu")
+    coh.emu_coherence.argtypes = [P, P, P, I, I, I, I, F, I, F, P]
+    paint.emu_paint2d.argtypes = [P, P, P, I, I, I, I, F]
+    return coh, paint
+
+
+@pytest.fixture
+def ps(emulated, monkeypatch):
+    from pyseistr_gb300 import api
+    from pyseistr_gb300 import device as D
+
+    coh, paint = emulated
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def to_flat(a):
+        if isinstance(a, torch.Tensor):
+            t = a.to(dtype=torch.float32)
+            return t.permute(*reversed(range(t.dim()))).contiguous().view(-1), True
+        arr = np.asarray(a, dtype=np.float32)
+        return torch.from_numpy(np.ascontiguousarray(arr.reshape(-1, order="F"))), False
+
+    def coherence(x, v, h, typ, nt, dt, forw, hmax, out=None):
+        nv, nh = v.numel(), h.numel()
+        assert x.numel() == nt * (nv if forw == 1 else nh) and x.is_contiguous()
+        out = torch.empty(nt * (nh if forw == 1 else nv), dtype=torch.float32)
+        assert coh.emu_coherence(ptr(x), ptr(v), ptr(h), int(typ), int(nt), nv, nh, float(dt),
+                                 int(forw), float(hmax), ptr(out)) == 0
+        return out
+
+    def paint2d(dip, seed, n1, n2, order, i0, eps, out=None, workspace=None):
+        assert dip.numel() == n1 * n2 and seed.numel() == n1 and seed.is_contiguous()
+        out = torch.empty(n1 * n2, dtype=torch.float32)
+        assert paint.emu_paint2d(ptr(dip), ptr(seed), ptr(out), n1, n2, order, i0,
+                                 float(eps)) == 0
+        return out
+
+    monkeypatch.setattr(api, "_to_dev_flat", to_flat)
+    monkeypatch.setattr(D, "coherence", coherence)
+    monkeypatch.setattr(D, "paint2d", paint2d)
+    import pyseistr_gb300
+
+    return pyseistr_gb300
+
+
+def test_coherence_api(ps):
+    import test_gpu_zcoherence as T
+
+    T.test_cohc_fb_matches_reference_in_call_order(ps)
+    for c in T.CASES[1:]:  # the first, a DAS window's shape, is left to the GPU run
+        T.test_cohc_matches_oracle(ps, c)
+    T.test_cohc_refuses_what_the_reference_cannot_compute(ps)
+
+
+def test_painting_api(ps):
+    import test_gpu_zpaint as T
+
+    T.test_pwpaintc_matches_reference(ps)
+    for c in T.CASES:
+        T.test_rgt_matches_oracle(ps, c)
+    T.test_cpaint2d_refuses_bad_arguments(ps)
+    rng = np.random.default_rng(21)
+    dip = rng.standard_normal((80, 30)).astype(np.float32)
+    tr = rng.standard_normal(80).astype(np.float32)
+    a = ps.pwpaintc(dip, tr, order=2, i0=10, eps=0.1)
+    b = ps.pwpaintc(torch.from_numpy(dip), torch.from_numpy(tr), order=2, i0=10, eps=0.1)
+    assert tuple(b.shape) == (80, 30) and np.array_equal(b.numpy(), a)
