@@ -327,6 +327,25 @@ size_t pwd_paint2d_workspace_size(int n1, int order);
 int pwd_paint2d(const float *dip, const float *seed, float *out, int n1, int n2, int order,
                 int i0, float eps, void *workspace, size_t workspace_bytes, pwd_stream_t stream);
 
+/* ---- Sparse-data interpolation (pyseistr/sint.py sint2dc, src/soint2d_cfuns.c
+ * csint2d) ------------------------------------------------------------------
+ * Replaces csint2d (soint2d_cfuns.c:2421, argument tuple "OOOiiiiiif" less
+ * the verb flag): the (n1, n2) section din with known samples where mask
+ * != 0, interpolated by niter shaping-regularised CG iterations whose
+ * shaping is the plane-wave smoothing of csomean2d (spray radius ns,
+ * accuracy order 1..4, regularisation eps) along the slopes dip, started
+ * from din, with lambda = sqrt(known / n) and the reference's stopping
+ * test.  Every float operation is the reference's; the dot products are
+ * FP64 sums in another order, so a scalar can differ in its last double
+ * bits.  The call synchronises `stream` twice per iteration (the CG's
+ * decisions are taken on the host).  Device pointers; workspace of
+ * pwd_sint2d_workspace_size bytes (0 for invalid sizes); out must not
+ * overlap the inputs. */
+size_t pwd_sint2d_workspace_size(int n1, int n2, int ns, int order);
+int pwd_sint2d(const float *din, const float *dip, const float *mask, float *out, int n1, int n2,
+               int niter, int ns, int order, float eps, void *workspace, size_t workspace_bytes,
+               pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

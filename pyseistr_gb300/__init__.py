@@ -25,6 +25,8 @@ sm_103a kernels of libpwd_gb300.so:
                                    (pyseistr/das.py)
     pwpaintc, rgt, cpaint2d        plane-wave painting of a seed trace and
                                    relative geological time (pyseistr/rgt.py)
+    sint2dc, csint2d               sparse-data interpolation along the
+                                   slopes (pyseistr/sint.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -34,6 +36,7 @@ from .api import (  # noqa: F401
     cohc,
     cohc_fb,
     cpaint2d,
+    csint2d,
     csoint2d,
     csoint3d,
     csomean2d,
@@ -53,6 +56,7 @@ from .api import (  # noqa: F401
     patch3d_inv,
     pwpaintc,
     rgt,
+    sint2dc,
     soint2dc,
     soint3dc,
     somean2dc,

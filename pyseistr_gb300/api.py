@@ -669,3 +669,43 @@ def rgt(dip, o1=0, d1=0.004, order=1, i0=0, eps=0.01, verb=False):
     if isinstance(dip, torch.Tensor):
         trace = torch.from_numpy(trace.astype(np.float32)).to(dip.device)
     return pwpaintc(dip, trace, order=order, i0=i0, eps=eps, verb=verb)
+
+
+# --------------------------------------------------------------------------
+# sparse-data interpolation (sint.py / soint2d_cfuns.c csint2d)
+# --------------------------------------------------------------------------
+def csint2d(din, dip, mask, n1, n2, niter, ns, order, verb, eps):
+    """csint2d "OOOiiiiiif" (soint2d_cfuns.c:2421): the flat column-major
+    section din (n1 n2 values, known where mask != 0) interpolated along the
+    slopes dip by niter shaping CG iterations with the plane-wave smoothing
+    of radius ns and accuracy order `order`; returns the flat float32 result
+    (a CUDA tensor for a tensor in).  Prints the reference's parameter line
+    (it prints it whatever verb is).  Raises ValueError where the reference
+    prints "Dimension mismatch" and returns NULL, and for slopes or a mask
+    of fewer than n1 n2 values (the reference reads past them)."""
+    n1, n2, niter, ns, order = int(n1), int(n2), int(niter), int(ns), int(order)
+    print("n1=%d,n2=%d,nw=%d,niter=%d,verb=%d,eps=%g"
+          % (n1, n2, order, niter, int(verb), float(np.float32(eps))))
+    n = n1 * n2
+    d, as_t = _to_dev_flat(din)
+    if d.numel() != n:
+        raise ValueError(f"Dimension mismatch, N_input = {d.numel()}, N_data = {n}")
+    p, _ = _to_dev_flat(dip)
+    m, _ = _to_dev_flat(mask)
+    if p.numel() < n or m.numel() < n:
+        raise ValueError(f"csint2d: slopes and mask need {n} values each")
+    if n1 < 4 or n2 < 1 or ns < 0 or order < 1 or niter < 0:
+        raise ValueError("csint2d: invalid sizes or parameters")
+    out = D.sint2d(d, p[:n].contiguous(), m[:n].contiguous(), n1, n2, niter, ns, order, eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def sint2dc(din, mask, dip, niter=100, eps=0.01, ns=1, order=1, verb=1):
+    """sint2dc (sint.py:61): interpolation of sparse data (e.g. well logs)
+    in an (n1, n2) section along the slopes dip; known samples where mask !=
+    0.  Returns the (n1, n2) section (a CUDA tensor for a tensor in)."""
+    n1, n2 = (int(x) for x in din.shape)
+    dout = csint2d(din, dip, mask, n1, n2, niter, ns, order, verb, eps)
+    if isinstance(dout, torch.Tensor):
+        return _from_dev_flat(dout, (n1, n2), True)
+    return dout.reshape(n1, n2, order="F")

@@ -1,0 +1,224 @@
+// Sparse-data interpolation (csint2d, pyseistr/src/soint2d_cfuns.c:2421-2523,
+// called by sint2dc, sint.py:61): the C entry, its per-sample kernels and
+// the GPU operations of the CG driver in pwd_sint.cuh.
+//
+// Each CG iteration applies the adjoint and the forward plane-wave
+// smoothing (the spray kernels of pwd_spray2d.cu, through smooth2_run) and
+// a handful of per-sample passes; the dot products are FP64 sums (per
+// thread, per block in a fixed tree, then the blocks' partials summed on the
+// host in block order: run-to-run deterministic).  The driver needs the dot
+// products on the host to take the reference's decisions (the step, the
+// conjugate scale and the early stop), so the call synchronises its stream
+// twice per iteration.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "pwd_common.cuh"
+#include "pwd_sint.cuh"
+
+namespace pwd {
+
+size_t smooth2_workspace(int n1, int n2, int ns, int order);
+int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int ns, int order,
+                float eps, int add, void* ws, size_t wsb, cudaStream_t st);
+
+namespace {
+
+constexpr int kSintThreads = 256;
+constexpr int kSintDotBlocks = 512;
+
+enum SintPass { kInit, kResidual, kGrad, kMask, kFirst, kConj, kStep };
+
+__global__ void __launch_bounds__(kSintThreads) k_sint_pass(sint::Vecs v, long n, int pass,
+                                                            float a) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    switch (pass) {
+      case kInit: sint::init_sample(v, i); break;
+      case kResidual: sint::residual_sample(v, i); break;
+      case kGrad: sint::grad_sample(v, i, a); break;
+      case kMask: sint::mask_sample(v, i); break;
+      case kFirst: sint::first_sample(v, i); break;
+      case kConj: sint::conj_sample(v, i, a); break;
+      default: sint::step_sample(v, i, a); break;
+    }
+  }
+}
+
+// FP64 partial sums of x*y: one per block, in a fixed order.
+__global__ void __launch_bounds__(kSintThreads) k_sint_dot(const float* __restrict__ x,
+                                                           const float* __restrict__ y, long n,
+                                                           double* __restrict__ part) {
+  __shared__ double sh[kSintThreads];
+  double t = 0.;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    t += (double)x[i] * (double)y[i];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int h = kSintThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Known samples (mask != 0), one integer per block.
+__global__ void __launch_bounds__(kSintThreads) k_sint_count(const float* __restrict__ mask,
+                                                             long n,
+                                                             unsigned long long* __restrict__ part) {
+  __shared__ unsigned long long sh[kSintThreads];
+  unsigned long long t = 0;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    t += mask[i] != 0.f;
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int h = kSintThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+struct SintLayout {
+  size_t vec_bytes, part_bytes, smooth_bytes, total;
+};
+
+SintLayout sint_layout(int n1, int n2, int ns, int order) {
+  SintLayout l{};
+  const long n = (long)n1 * n2;
+  l.vec_bytes = ((sizeof(float) * (size_t)n + 255) & ~(size_t)255);
+  l.part_bytes = ((sizeof(double) * kSintDotBlocks + 255) & ~(size_t)255);
+  l.smooth_bytes = smooth2_workspace(n1, n2, ns, order);
+  l.total = l.smooth_bytes ? 8 * l.vec_bytes + l.part_bytes + l.smooth_bytes : 0;
+  return l;
+}
+
+struct GpuOps {
+  sint::Vecs v;
+  long n;
+  const float* dip;
+  int n1, n2, ns, order;
+  float eps;  // the smoothing's eps (csint2d's eps argument)
+  void* sws;
+  size_t swsb;
+  double* part;
+  std::vector<double> host;
+  cudaStream_t st;
+  unsigned grid;
+
+  float* vec(int k) const {
+    switch (k) {
+      case sint::kP: return v.p;
+      case sint::kR: return v.r;
+      case sint::kSP: return v.sp;
+      case sint::kGP: return v.gp;
+      case sint::kSX: return v.sx;
+      case sint::kGX: return v.gx;
+      case sint::kSR: return v.sr;
+      case sint::kGR: return v.gr;
+      default: return v.x;
+    }
+  }
+  int pass(int which, float a) {
+    PWD_KERNEL(PWD_FAM_CG, st, (k_sint_pass<<<grid, kSintThreads, 0, st>>>(v, n, which, a)));
+    return cuda_status(cudaGetLastError());
+  }
+  int init() { return pass(kInit, 0.f); }
+  int residual() { return pass(kResidual, 0.f); }
+  int grad(float e) { return pass(kGrad, e); }
+  int mask() { return pass(kMask, 0.f); }
+  int first() { return pass(kFirst, 0.f); }
+  int conj(float a) { return pass(kConj, a); }
+  int step(float a) { return pass(kStep, a); }
+  int smooth(int in, int out) {
+    return smooth2_run(vec(in), dip, vec(out), n1, n2, ns, order, eps, 0, sws, swsb, st);
+  }
+  int smooth_adj_add(int in, int out) {
+    return smooth2_run(vec(in), dip, vec(out), n1, n2, ns, order, eps, 1, sws, swsb, st);
+  }
+  int dot(int a, int b, double* s) {
+    PWD_KERNEL(PWD_FAM_CG, st,
+               (k_sint_dot<<<kSintDotBlocks, kSintThreads, 0, st>>>(vec(a), vec(b), n, part)));
+    int rc = cuda_status(cudaGetLastError());
+    if (rc != PWD_OK) return rc;
+    rc = cuda_status(cudaMemcpyAsync(host.data(), part, sizeof(double) * kSintDotBlocks,
+                                     cudaMemcpyDeviceToHost, st));
+    if (rc != PWD_OK) return rc;
+    rc = cuda_status(cudaStreamSynchronize(st));
+    if (rc != PWD_OK) return rc;
+    double t = 0.;
+    for (int k = 0; k < kSintDotBlocks; k++) t += host[k];
+    *s = t;
+    return PWD_OK;
+  }
+};
+
+}  // namespace
+}  // namespace pwd
+
+extern "C" size_t pwd_sint2d_workspace_size(int n1, int n2, int ns, int order) {
+  if (n1 < 4 || n2 < 1 || ns < 0 || order < 1 || order > PWD_MAX_ORDER) return 0;
+  return pwd::sint_layout(n1, n2, ns, order).total;
+}
+
+extern "C" int pwd_sint2d(const float* din, const float* dip, const float* mask, float* out,
+                          int n1, int n2, int niter, int ns, int order, float eps,
+                          void* workspace, size_t workspace_bytes, pwd_stream_t stream) {
+  if (!din || !dip || !mask || !out || n1 < 4 || n2 < 1 || ns < 0 || order < 1 || niter < 0)
+    return PWD_EINVAL;
+  if ((long)n1 * n2 >= (1L << 31)) return PWD_EINVAL;
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  const pwd::SintLayout l = pwd::sint_layout(n1, n2, ns, order);
+  if (!l.total || !workspace || workspace_bytes < l.total || (uintptr_t)workspace % 256)
+    return PWD_EWORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long n = (long)n1 * n2;
+  char* base = (char*)workspace;
+  pwd::GpuOps ops;
+  ops.n = n;
+  ops.dip = dip;
+  ops.n1 = n1;
+  ops.n2 = n2;
+  ops.ns = ns;
+  ops.order = order;
+  ops.eps = eps;
+  ops.st = st;
+  float* f[8];
+  for (int k = 0; k < 8; k++) f[k] = (float*)(base + k * l.vec_bytes);
+  ops.v.din = din;
+  ops.v.mask = mask;
+  ops.v.x = out;
+  ops.v.p = f[0];
+  ops.v.r = f[1];
+  ops.v.sp = f[2];
+  ops.v.gp = f[3];
+  ops.v.sx = f[4];
+  ops.v.gx = f[5];
+  ops.v.sr = f[6];
+  ops.v.gr = f[7];
+  ops.part = (double*)(base + 8 * l.vec_bytes);
+  ops.sws = base + 8 * l.vec_bytes + l.part_bytes;
+  ops.swsb = l.smooth_bytes;
+  ops.host.assign(pwd::kSintDotBlocks, 0.);
+  const long blocks = (n + pwd::kSintThreads - 1) / pwd::kSintThreads;
+  ops.grid = (unsigned)(blocks < 152L * 8 * 16 ? blocks : 152L * 8 * 16);
+  // csint2d's lambda from the number of known samples
+  unsigned long long* cpart = (unsigned long long*)ops.part;
+  PWD_KERNEL(PWD_FAM_CG, st,
+             (pwd::k_sint_count<<<pwd::kSintDotBlocks, pwd::kSintThreads, 0, st>>>(mask, n,
+                                                                                   cpart)));
+  int rc = pwd::cuda_status(cudaGetLastError());
+  if (rc != PWD_OK) return rc;
+  std::vector<unsigned long long> cnt(pwd::kSintDotBlocks, 0);
+  rc = pwd::cuda_status(cudaMemcpyAsync(cnt.data(), cpart,
+                                        sizeof(unsigned long long) * pwd::kSintDotBlocks,
+                                        cudaMemcpyDeviceToHost, st));
+  if (rc == PWD_OK) rc = pwd::cuda_status(cudaStreamSynchronize(st));
+  if (rc != PWD_OK) return rc;
+  unsigned long long known = 0;
+  for (unsigned long long c : cnt) known += c;
+  return pwd::sint::conjgrad(ops, niter, pwd::sint::lambda_of(known, n));
+}

@@ -247,8 +247,10 @@ __global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ 
 
 // Adjoint of the weighted mean (pwsmooth_lop adjoint :1072-1086 with
 // pwspray_lop adjoint :957-989).  Thread per output trace; chain traces in a
-// per-thread buffer.
-template <int NW>
+// per-thread buffer.  ADD: the terms are added into `out` as it stands (the
+// adjoint with add = true, as the sparse-data interpolation's CG applies it,
+// soint2d_cfuns.c:2194-2220) instead of into zeros.
+template <int NW, bool ADD = false>
 __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restrict__ dip,
                                float* __restrict__ out, SprayBufs bf, SprayB b, ApCoef c) {
   long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -281,7 +283,7 @@ __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restr
     predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)(ip - 1) * n1, true, my, my.y);
   }
   for (int i1 = 0; i1 < n1; i1++) {
-    o[i1] = __fadd_rn(0.f, tr[i1]);
+    o[i1] = __fadd_rn(ADD ? o[i1] : 0.f, tr[i1]);
     tr[i1] = 0.f;
   }
   for (int is = b.ns - 1; is >= 0; is--) {
@@ -314,7 +316,7 @@ __global__ void k_fill(float* x, float v, long n) {
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-enum Filter { kMean = 1, kMeanAdj = 2, kMedian = 3 };
+enum Filter { kMean = 1, kMeanAdj = 2, kMedian = 3, kMeanAdjAdd = 4 };
 
 struct SprayLayout {
   int ntiles;
@@ -379,12 +381,13 @@ SprayWork carve2(void* ws, const SprayLayout& L, int nsec, int filter, int optio
                  size_t* total) {
   Carver cv(ws);
   SprayWork w{};
-  const bool mean = filter == kMean || filter == kMeanAdj;
-  w.bf.u = filter == kMeanAdj ? nullptr : cv.take<float>(L.nu);
+  const bool adj = filter == kMeanAdj || filter == kMeanAdjAdd;
+  const bool mean = filter == kMean || adj;
+  w.bf.u = adj ? nullptr : cv.take<float>(L.nu);
   w.bf.u1 = mean ? cv.take<float>(L.nu) : nullptr;
-  w.bf.w1 = filter == kMeanAdj ? cv.take<float>(L.nsamp) : nullptr;
+  w.bf.w1 = adj ? cv.take<float>(L.nsamp) : nullptr;
   w.bf.scr = cv.take<float>(std::max(L.nscr, 1L));
-  w.bf.tbuf = filter == kMeanAdj ? cv.take<float>(L.nsamp) : nullptr;
+  w.bf.tbuf = adj ? cv.take<float>(L.nsamp) : nullptr;
   w.ones = cv.take<float>(L.n1max);
   const bool svmf = filter == kMedian && option != 1;
   w.v2 = svmf ? cv.take<float>(L.nu) : nullptr;
@@ -436,14 +439,18 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
-  } else if (filter == kMeanAdj) {
+  } else if (filter == kMeanAdj || filter == kMeanAdjAdd) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 2><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
     // the adjoint chains reuse the scratch region as their per-chain scratch
-    PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
+    if (filter == kMeanAdj)
+      PWD_KERNEL(PWD_FAM_SPRAY, st,
+                 k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
+    else
+      PWD_KERNEL(PWD_FAM_SPRAY, st,
+                 (k_somean2d_adj<NW, true><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c)));
   } else {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
@@ -526,6 +533,25 @@ int batch_table2(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
 }
 
 }  // namespace
+
+// The 2-D plane-wave smoothing of one section for the sparse-data
+// interpolation (pwd_sint.cu): add = 0 gives out = S in (the weighted spray
+// mean, as pwd_somean2d), add = 1 gives out += S' in, the adjoint adding its
+// terms into out in the reference's order.  `in` and `out` must not overlap.
+size_t smooth2_workspace(int n1, int n2, int ns, int order) {
+  if (check2(n1, n2, 1, ns, order) != PWD_OK) return 0;
+  return std::max(need_single(n1, n2, 1, ns, order, kMean, 1),
+                  need_single(n1, n2, 1, ns, order, kMeanAdjAdd, 1));
+}
+
+int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int ns, int order,
+                float eps, int add, void* ws, size_t wsb, cudaStream_t st) {
+  int rc = check2(n1, n2, 1, ns, order);
+  if (rc != PWD_OK) return rc;
+  return run_single(in, dip, out, n1, n2, 1, ns, order, eps, add ? kMeanAdjAdd : kMean, 1, 0, ws,
+                    wsb, st);
+}
+
 }  // namespace pwd
 
 using namespace pwd;

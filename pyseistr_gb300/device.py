@@ -375,3 +375,24 @@ def paint2d(dip, seed, n1, n2, order, i0, eps, out=None, workspace=None):
     _lib.check(L.pwd_paint2d(_ptr(dip), _ptr(seed), _ptr(out), n1, n2, order, i0, float(eps),
                              _ptr(ws), ws.numel() * ws.element_size(), _stream()), "paint2d")
     return out
+
+
+def sint2d(din, dip, mask, n1, n2, niter, ns, order, eps, out=None, workspace=None):
+    """Sparse-data interpolation (pwd_sint2d) of the flat column-major CUDA
+    float32 section din (known where mask != 0) along the slopes dip;
+    returns the flat interpolated section.  Synchronises the current stream
+    during the call."""
+    L = _lib.load()
+    n1, n2 = int(n1), int(n2)
+    n = n1 * n2
+    din = _as_flat(din, n, "din")
+    dip = _as_flat(dip, n, "dip")
+    mask = _as_flat(mask, n, "mask")
+    ws = _workspace(L.pwd_sint2d_workspace_size(n1, n2, int(ns), int(order)), din.device,
+                    workspace)
+    if out is None:
+        out = torch.empty(n, dtype=torch.float32, device=din.device)
+    _lib.check(L.pwd_sint2d(_ptr(din), _ptr(dip), _ptr(mask), _ptr(out), n1, n2, int(niter),
+                            int(ns), int(order), float(eps), _ptr(ws),
+                            ws.numel() * ws.element_size(), _stream()), "sint2d")
+    return out

@@ -126,3 +126,16 @@ def test_paint_entry_checks_arguments_on_the_host():
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 5, 0, 0.1, fake, need, None) == _lib.PWD_ENOTSUP
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, fake, need - 256, None) == _lib.PWD_EWORKSPACE
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, ctypes.c_void_p(300), need, None) == _lib.PWD_EWORKSPACE
+
+
+def test_sint_entry_checks_arguments_on_the_host():
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+    assert lib.pwd_sint2d_workspace_size(3, 10, 1, 1) == 0
+    assert lib.pwd_sint2d_workspace_size(40, 10, 1, 5) == 0
+    need = lib.pwd_sint2d_workspace_size(40, 10, 2, 2)
+    assert need >= 8 * 40 * 10 * 4 + lib.pwd_somean2d_workspace_size(40, 10, 1, 2, 2)
+    assert lib.pwd_sint2d(None, fake, fake, fake, 40, 10, 5, 1, 1, 0.01, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, -1, 1, 1, 0.01, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, 5, 1, 5, 0.01, fake, need, None) == _lib.PWD_ENOTSUP
+    assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, 5, 2, 2, 0.01, fake, need - 256, None) == _lib.PWD_EWORKSPACE

@@ -1,6 +1,6 @@
-"""The host layer of the coherence and painting rows (argument handling,
-flattening, reshapes, the parabolic hmax state) through the GPU tests' own
-checks, on the CPU: the two device wrappers are replaced, for these tests
+"""The host layer of the coherence, painting and sparse-interpolation rows
+(argument handling, flattening, reshapes, the parabolic hmax state) through
+the GPU tests' own checks, on the CPU: the three device wrappers are replaced, for these tests
 only, by the kernels' per-thread code run on the CPU (tests/emu), and the
 host-to-device copy by a CPU tensor.  The library itself has no CPU path."""
 import ctypes
@@ -26,10 +26,11 @@ def _build(tmp, name):
 @pytest.fixture(scope="module")
 def emulated(tmp_path_factory):
     tmp = tmp_path_factory.mktemp("api_emu")
-    coh, paint = _build(tmp, "coh_emu"), _build(tmp, "paint_emu")
+    coh, paint, sint = _build(tmp, "coh_emu"), _build(tmp, "paint_emu"), _build(tmp, "sint_emu")
     coh.emu_coherence.argtypes = [P, P, P, I, I, I, I, F, I, F, P]
     paint.emu_paint2d.argtypes = [P, P, P, I, I, I, I, F]
-    return coh, paint
+    sint.emu_sint2d.argtypes = [P, P, P, P, I, I, I, I, I, F]
+    return coh, paint, sint
 
 
 @pytest.fixture
@@ -37,7 +38,7 @@ def ps(emulated, monkeypatch):
     from pyseistr_gb300 import api
     from pyseistr_gb300 import device as D
 
-    coh, paint = emulated
+    coh, paint, sint = emulated
     ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
 
     def to_flat(a):
@@ -62,7 +63,17 @@ def ps(emulated, monkeypatch):
                                  float(eps)) == 0
         return out
 
+    def sint2d(din, dip, mask, n1, n2, niter, ns, order, eps, out=None, workspace=None):
+        n = n1 * n2
+        assert din.numel() == n and dip.numel() == n and mask.numel() == n
+        assert dip.is_contiguous() and mask.is_contiguous()
+        out = torch.empty(n, dtype=torch.float32)
+        assert sint.emu_sint2d(ptr(din), ptr(dip), ptr(mask), ptr(out), n1, n2, niter, ns,
+                               order, float(eps)) == 0
+        return out
+
     monkeypatch.setattr(api, "_to_dev_flat", to_flat)
+    monkeypatch.setattr(D, "sint2d", sint2d)
     monkeypatch.setattr(D, "coherence", coherence)
     monkeypatch.setattr(D, "paint2d", paint2d)
     import pyseistr_gb300
@@ -92,3 +103,17 @@ def test_painting_api(ps):
     a = ps.pwpaintc(dip, tr, order=2, i0=10, eps=0.1)
     b = ps.pwpaintc(torch.from_numpy(dip), torch.from_numpy(tr), order=2, i0=10, eps=0.1)
     assert tuple(b.shape) == (80, 30) and np.array_equal(b.numpy(), a)
+
+
+def test_sparse_interpolation_api(ps):
+    import test_gpu_zsint as T
+
+    T.test_sint2dc_matches_reference(ps)
+    for c in T.CASES[1:]:  # the first, a 501 x 100 section, is left to the GPU run
+        T.test_sint2dc_matches_oracle(ps, c)
+    T.test_csint2d_refuses_bad_arguments(ps)
+    d, mask, dip = T._case(80, 24, 0.4, 21)
+    a = ps.sint2dc(d, mask, dip, niter=12, ns=2, order=2)
+    b = ps.sint2dc(torch.from_numpy(d), torch.from_numpy(mask), torch.from_numpy(dip),
+                   niter=12, ns=2, order=2)
+    assert tuple(b.shape) == (80, 24) and np.array_equal(b.numpy(), a)
