@@ -345,6 +345,18 @@ size_t pwd_sint2d_workspace_size(int n1, int n2, int ns, int order);
 int pwd_sint2d(const float *din, const float *dip, const float *mask, float *out, int n1, int n2,
                int niter, int ns, int order, float eps, void *workspace, size_t workspace_bytes,
                pwd_stream_t stream);
+/* Replaces csint3d (soint3d_cfuns.c:2510, tuple "OOOOiiiiiiiiif" less the
+ * verb flag): the same CG on an (n1, n2, n3) cube whose shaping smooths every
+ * (n1, n2) slice along the inline slopes dipi (radius ns1, order order1),
+ * then every (n1, n3) section along the crossline slopes dipx (ns2, order2),
+ * the adjoint in reverse (pwsmooth3_lop, :2157-2300).  Same arithmetic,
+ * synchronisation and workspace rules as pwd_sint2d. */
+size_t pwd_sint3d_workspace_size(int n1, int n2, int n3, int ns1, int ns2, int order1,
+                                 int order2);
+int pwd_sint3d(const float *din, const float *dipi, const float *dipx, const float *mask,
+               float *out, int n1, int n2, int n3, int niter, int ns1, int ns2, int order1,
+               int order2, float eps, void *workspace, size_t workspace_bytes,
+               pwd_stream_t stream);
 
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);

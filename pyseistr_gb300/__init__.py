@@ -25,8 +25,8 @@ sm_103a kernels of libpwd_gb300.so:
                                    (pyseistr/das.py)
     pwpaintc, rgt, cpaint2d        plane-wave painting of a seed trace and
                                    relative geological time (pyseistr/rgt.py)
-    sint2dc, csint2d               sparse-data interpolation along the
-                                   slopes (pyseistr/sint.py)
+    sint2dc, sint3dc,              sparse-data interpolation along the
+    csint2d, csint3d               slopes (pyseistr/sint.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -37,6 +37,7 @@ from .api import (  # noqa: F401
     cohc_fb,
     cpaint2d,
     csint2d,
+    csint3d,
     csoint2d,
     csoint3d,
     csomean2d,
@@ -57,6 +58,7 @@ from .api import (  # noqa: F401
     pwpaintc,
     rgt,
     sint2dc,
+    sint3dc,
     soint2dc,
     soint3dc,
     somean2dc,

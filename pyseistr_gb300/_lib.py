@@ -54,6 +54,8 @@ SIGNATURES = {
     "pwd_paint2d": ([_P, _P, _P, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_sint2d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_sint2d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_sint3d_workspace_size": ([_I] * 7, _S),
+    "pwd_sint3d": ([_P] * 5 + [_I] * 8 + [_F, _P, _S, _P], _I),
     "pwd_soint3d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_soint3d": ([_P, _P, _P, _P, _P] + [_I] * 10 + [_F, _P, _S, _P], _I),
     "pwd_soint3d_batch_workspace_size": ([_P, _I, _I], _S),

@@ -709,3 +709,43 @@ def sint2dc(din, mask, dip, niter=100, eps=0.01, ns=1, order=1, verb=1):
     if isinstance(dout, torch.Tensor):
         return _from_dev_flat(dout, (n1, n2), True)
     return dout.reshape(n1, n2, order="F")
+
+
+def csint3d(din, dipi, dipx, mask, n1, n2, n3, niter, ns1, ns2, order1, order2, verb, eps):
+    """csint3d "OOOOiiiiiiiiif" (soint3d_cfuns.c:2510): the flat cube din
+    (known where mask != 0) interpolated along the inline slopes dipi and
+    the crossline slopes dipx; returns the flat float32 result (a CUDA
+    tensor for a tensor in).  Prints the reference's parameter line (it
+    prints it whatever verb is).  Raises ValueError where the reference
+    prints "Dimension mismatch" and returns NULL, and for slopes or a mask
+    of fewer values than the cube."""
+    n1, n2, n3, niter = int(n1), int(n2), int(n3), int(niter)
+    ns1, ns2, order1, order2 = int(ns1), int(ns2), int(order1), int(order2)
+    print("n1=%d,n2=%d,n3=%d,ns1=%d,ns2=%d,nw1=%d,nw2=%d,niter=%d,verb=%d,eps=%g"
+          % (n1, n2, n3, ns1, ns2, order1, order2, niter, int(verb), float(np.float32(eps))))
+    n = n1 * n2 * n3
+    d, as_t = _to_dev_flat(din)
+    if d.numel() != n:
+        raise ValueError(f"Dimension mismatch, N_input = {d.numel()}, N_data = {n}")
+    pi, _ = _to_dev_flat(dipi)
+    px, _ = _to_dev_flat(dipx)
+    m, _ = _to_dev_flat(mask)
+    if min(pi.numel(), px.numel(), m.numel()) < n:
+        raise ValueError(f"csint3d: slopes and mask need {n} values each")
+    if n1 < 4 or min(n2, n3) < 1 or min(ns1, ns2) < 0 or min(order1, order2) < 1 or niter < 0:
+        raise ValueError("csint3d: invalid sizes or parameters")
+    out = D.sint3d(d, pi[:n].contiguous(), px[:n].contiguous(), m[:n].contiguous(),
+                   (n1, n2, n3), niter, (ns1, ns2), (order1, order2), eps)
+    return out if as_t else out.cpu().numpy()
+
+
+def sint3dc(din, mask, dipi, dipx, niter=100, eps=0.01, ns1=1, ns2=1, order1=1, order2=1,
+            verb=1):
+    """sint3dc (sint.py:97): interpolation of sparse data in an (n1, n2,
+    n3) cube along the inline and crossline slopes; known samples where mask
+    != 0.  Returns the cube (a CUDA tensor for a tensor in)."""
+    n1, n2, n3 = (int(x) for x in din.shape)
+    dout = csint3d(din, dipi, dipx, mask, n1, n2, n3, niter, ns1, ns2, order1, order2, verb, eps)
+    if isinstance(dout, torch.Tensor):
+        return _from_dev_flat(dout, (n1, n2, n3), True)
+    return dout.reshape(n1, n2, n3, order="F")

@@ -1,6 +1,7 @@
 // Sparse-data interpolation (csint2d, pyseistr/src/soint2d_cfuns.c:2421-2523,
-// called by sint2dc, sint.py:61): the C entry, its per-sample kernels and
-// the GPU operations of the CG driver in pwd_sint.cuh.
+// called by sint2dc, sint.py:61; csint3d, soint3d_cfuns.c:2510-2612, called
+// by sint3dc, sint.py:97): the C entries, their per-sample kernels and the
+// GPU operations of the CG driver in pwd_sint.cuh.
 //
 // Each CG iteration applies the adjoint and the forward plane-wave
 // smoothing (the spray kernels of pwd_spray2d.cu, through smooth2_run) and
@@ -19,9 +20,9 @@
 
 namespace pwd {
 
-size_t smooth2_workspace(int n1, int n2, int ns, int order);
-int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int ns, int order,
-                float eps, int add, void* ws, size_t wsb, cudaStream_t st);
+size_t smooth2_workspace(int n1, int n2, int n3, int ns, int order);
+int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int n3, int ns,
+                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st);
 
 namespace {
 
@@ -82,26 +83,51 @@ __global__ void __launch_bounds__(kSintThreads) k_sint_count(const float* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// Cube <-> crossline-major transposes (pwsmooth3_lop's index shuffles).
+__global__ void __launch_bounds__(kSintThreads) k_sint_cross(const float* __restrict__ a,
+                                                             float* __restrict__ b, int n1,
+                                                             int n2, int n3, int to, int sum) {
+  const long n = (long)n1 * n2 * n3, stride = (long)gridDim.x * blockDim.x;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+    if (to)
+      sint::to_crossline_sample(a, b, n1, n2, n3, e);
+    else
+      sint::from_crossline_sample(a, b, n1, n2, n3, e, sum != 0);
+  }
+}
+
 struct SintLayout {
   size_t vec_bytes, part_bytes, smooth_bytes, total;
 };
 
-SintLayout sint_layout(int n1, int n2, int ns, int order) {
+// 8 CG vectors, for csint3d 4 more (itmp, itmp2, xtmp and the transposed
+// crossline slope), the dot partials and the smoothing's workspace.
+SintLayout sint_layout(int n1, int n2, int n3, int ns1, int ns2, int order1, int order2,
+                       bool three) {
   SintLayout l{};
-  const long n = (long)n1 * n2;
+  const long n = (long)n1 * n2 * n3;
   l.vec_bytes = ((sizeof(float) * (size_t)n + 255) & ~(size_t)255);
   l.part_bytes = ((sizeof(double) * kSintDotBlocks + 255) & ~(size_t)255);
-  l.smooth_bytes = smooth2_workspace(n1, n2, ns, order);
-  l.total = l.smooth_bytes ? 8 * l.vec_bytes + l.part_bytes + l.smooth_bytes : 0;
+  l.smooth_bytes = smooth2_workspace(n1, n2, n3, ns1, order1);
+  if (three && l.smooth_bytes) {
+    const size_t c = smooth2_workspace(n1, n3, n2, ns2, order2);
+    l.smooth_bytes = c ? (c > l.smooth_bytes ? c : l.smooth_bytes) : 0;
+  }
+  const int nvec = three ? 12 : 8;
+  l.total = l.smooth_bytes ? nvec * l.vec_bytes + l.part_bytes + l.smooth_bytes : 0;
   return l;
 }
 
 struct GpuOps {
   sint::Vecs v;
   long n;
-  const float* dip;
-  int n1, n2, ns, order;
-  float eps;  // the smoothing's eps (csint2d's eps argument)
+  int n1, n2, n3;
+  bool three;               // csint3d's smoothing (inline, then crossline)
+  const float* dipi;        // inline slopes, cube layout
+  const float* xd;          // crossline slopes, crossline-major layout (3-D)
+  int ns1, ns2, order1, order2;
+  float eps;                // the smoothing's eps (csint2d's / csint3d's eps argument)
+  float *itmp, *itmp2, *xtmp;
   void* sws;
   size_t swsb;
   double* part;
@@ -133,11 +159,27 @@ struct GpuOps {
   int first() { return pass(kFirst, 0.f); }
   int conj(float a) { return pass(kConj, a); }
   int step(float a) { return pass(kStep, a); }
+  // primitives of the 3-D sequence
+  int inline_(int mode, float* in, float* out) {
+    return smooth2_run(in, dipi, out, n1, n2, n3, ns1, order1, eps, mode, sws, swsb, st);
+  }
+  int crossline(int mode, float* in, float* out) {
+    return smooth2_run(in, xd, out, n1, n3, n2, ns2, order2, eps, mode, sws, swsb, st);
+  }
+  int cross(const float* a, float* b, int to, int sum) {
+    PWD_KERNEL(PWD_FAM_CG, st,
+               (k_sint_cross<<<grid, kSintThreads, 0, st>>>(a, b, n1, n2, n3, to, sum)));
+    return cuda_status(cudaGetLastError());
+  }
+  int to_cross(float* c, float* t) { return cross(c, t, 1, 0); }
+  int from_cross(float* t, float* c, bool sum) { return cross(t, c, 0, sum ? 1 : 0); }
   int smooth(int in, int out) {
-    return smooth2_run(vec(in), dip, vec(out), n1, n2, ns, order, eps, 0, sws, swsb, st);
+    if (!three) return inline_(0, vec(in), vec(out));
+    return sint::smooth3_forward(*this, vec(in), vec(out), itmp, itmp2, xtmp);
   }
   int smooth_adj_add(int in, int out) {
-    return smooth2_run(vec(in), dip, vec(out), n1, n2, ns, order, eps, 1, sws, swsb, st);
+    if (!three) return inline_(1, vec(in), vec(out));
+    return sint::smooth3_adjoint_add(*this, vec(in), vec(out), itmp, itmp2, xtmp);
   }
   int dot(int a, int b, double* s) {
     PWD_KERNEL(PWD_FAM_CG, st,
@@ -156,38 +198,39 @@ struct GpuOps {
   }
 };
 
-}  // namespace
-}  // namespace pwd
-
-extern "C" size_t pwd_sint2d_workspace_size(int n1, int n2, int ns, int order) {
-  if (n1 < 4 || n2 < 1 || ns < 0 || order < 1 || order > PWD_MAX_ORDER) return 0;
-  return pwd::sint_layout(n1, n2, ns, order).total;
+bool sint_args_ok(int n1, int n2, int n3, int niter, int ns1, int ns2) {
+  return n1 >= 4 && n2 >= 1 && n3 >= 1 && niter >= 0 && ns1 >= 0 && ns2 >= 0 &&
+         (long)n1 * n2 * n3 < (1L << 31);
 }
 
-extern "C" int pwd_sint2d(const float* din, const float* dip, const float* mask, float* out,
-                          int n1, int n2, int niter, int ns, int order, float eps,
-                          void* workspace, size_t workspace_bytes, pwd_stream_t stream) {
-  if (!din || !dip || !mask || !out || n1 < 4 || n2 < 1 || ns < 0 || order < 1 || niter < 0)
-    return PWD_EINVAL;
-  if ((long)n1 * n2 >= (1L << 31)) return PWD_EINVAL;
-  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
-  const pwd::SintLayout l = pwd::sint_layout(n1, n2, ns, order);
+// Both entries: three = false is csint2d (n3 = 1; ns2, order2 unused),
+// three = true csint3d (for any n3, one included: its crossline pass still
+// rounds).
+int sint_run(const float* din, const float* dipi, const float* dipx, const float* mask,
+             float* out, int n1, int n2, int n3, int niter, int ns1, int ns2, int order1,
+             int order2, float eps, bool three, void* workspace, size_t workspace_bytes,
+             cudaStream_t st) {
+  const SintLayout l = sint_layout(n1, n2, n3, ns1, ns2, order1, order2, three);
   if (!l.total || !workspace || workspace_bytes < l.total || (uintptr_t)workspace % 256)
     return PWD_EWORKSPACE;
-  cudaStream_t st = (cudaStream_t)stream;
-  const long n = (long)n1 * n2;
+  const long n = (long)n1 * n2 * n3;
   char* base = (char*)workspace;
-  pwd::GpuOps ops;
+  GpuOps ops;
   ops.n = n;
-  ops.dip = dip;
   ops.n1 = n1;
   ops.n2 = n2;
-  ops.ns = ns;
-  ops.order = order;
+  ops.n3 = n3;
+  ops.three = three;
+  ops.dipi = dipi;
+  ops.ns1 = ns1;
+  ops.ns2 = ns2;
+  ops.order1 = order1;
+  ops.order2 = order2;
   ops.eps = eps;
   ops.st = st;
-  float* f[8];
-  for (int k = 0; k < 8; k++) f[k] = (float*)(base + k * l.vec_bytes);
+  float* f[12];
+  const int nvec = three ? 12 : 8;
+  for (int k = 0; k < nvec; k++) f[k] = (float*)(base + k * l.vec_bytes);
   ops.v.din = din;
   ops.v.mask = mask;
   ops.v.x = out;
@@ -199,26 +242,70 @@ extern "C" int pwd_sint2d(const float* din, const float* dip, const float* mask,
   ops.v.gx = f[5];
   ops.v.sr = f[6];
   ops.v.gr = f[7];
-  ops.part = (double*)(base + 8 * l.vec_bytes);
-  ops.sws = base + 8 * l.vec_bytes + l.part_bytes;
+  ops.itmp = three ? f[8] : nullptr;
+  ops.itmp2 = three ? f[9] : nullptr;
+  ops.xtmp = three ? f[10] : nullptr;
+  float* xd = three ? f[11] : nullptr;
+  ops.xd = xd;
+  ops.part = (double*)(base + nvec * l.vec_bytes);
+  ops.sws = base + nvec * l.vec_bytes + l.part_bytes;
   ops.swsb = l.smooth_bytes;
-  ops.host.assign(pwd::kSintDotBlocks, 0.);
-  const long blocks = (n + pwd::kSintThreads - 1) / pwd::kSintThreads;
+  ops.host.assign(kSintDotBlocks, 0.);
+  const long blocks = (n + kSintThreads - 1) / kSintThreads;
   ops.grid = (unsigned)(blocks < 152L * 8 * 16 ? blocks : 152L * 8 * 16);
-  // csint2d's lambda from the number of known samples
+  int rc;
+  if (three && (rc = ops.cross(dipx, xd, 1, 0))) return rc;
+  // the lambda from the number of known samples
   unsigned long long* cpart = (unsigned long long*)ops.part;
   PWD_KERNEL(PWD_FAM_CG, st,
-             (pwd::k_sint_count<<<pwd::kSintDotBlocks, pwd::kSintThreads, 0, st>>>(mask, n,
-                                                                                   cpart)));
-  int rc = pwd::cuda_status(cudaGetLastError());
+             (k_sint_count<<<kSintDotBlocks, kSintThreads, 0, st>>>(mask, n, cpart)));
+  rc = cuda_status(cudaGetLastError());
   if (rc != PWD_OK) return rc;
-  std::vector<unsigned long long> cnt(pwd::kSintDotBlocks, 0);
-  rc = pwd::cuda_status(cudaMemcpyAsync(cnt.data(), cpart,
-                                        sizeof(unsigned long long) * pwd::kSintDotBlocks,
-                                        cudaMemcpyDeviceToHost, st));
-  if (rc == PWD_OK) rc = pwd::cuda_status(cudaStreamSynchronize(st));
+  std::vector<unsigned long long> cnt(kSintDotBlocks, 0);
+  rc = cuda_status(cudaMemcpyAsync(cnt.data(), cpart, sizeof(unsigned long long) * kSintDotBlocks,
+                                   cudaMemcpyDeviceToHost, st));
+  if (rc == PWD_OK) rc = cuda_status(cudaStreamSynchronize(st));
   if (rc != PWD_OK) return rc;
   unsigned long long known = 0;
   for (unsigned long long c : cnt) known += c;
-  return pwd::sint::conjgrad(ops, niter, pwd::sint::lambda_of(known, n));
+  return sint::conjgrad(ops, niter, sint::lambda_of(known, n));
+}
+
+}  // namespace
+}  // namespace pwd
+
+extern "C" size_t pwd_sint2d_workspace_size(int n1, int n2, int ns, int order) {
+  if (!pwd::sint_args_ok(n1, n2, 1, 0, ns, 0) || order < 1 || order > PWD_MAX_ORDER) return 0;
+  return pwd::sint_layout(n1, n2, 1, ns, 0, order, 1, false).total;
+}
+
+extern "C" int pwd_sint2d(const float* din, const float* dip, const float* mask, float* out,
+                          int n1, int n2, int niter, int ns, int order, float eps,
+                          void* workspace, size_t workspace_bytes, pwd_stream_t stream) {
+  if (!din || !dip || !mask || !out || !pwd::sint_args_ok(n1, n2, 1, niter, ns, 0) ||
+      order < 1)
+    return PWD_EINVAL;
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  return pwd::sint_run(din, dip, nullptr, mask, out, n1, n2, 1, niter, ns, 0, order, 1, eps,
+                       false, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t pwd_sint3d_workspace_size(int n1, int n2, int n3, int ns1, int ns2, int order1,
+                                            int order2) {
+  if (!pwd::sint_args_ok(n1, n2, n3, 0, ns1, ns2) || order1 < 1 || order2 < 1 ||
+      order1 > PWD_MAX_ORDER || order2 > PWD_MAX_ORDER)
+    return 0;
+  return pwd::sint_layout(n1, n2, n3, ns1, ns2, order1, order2, true).total;
+}
+
+extern "C" int pwd_sint3d(const float* din, const float* dipi, const float* dipx,
+                          const float* mask, float* out, int n1, int n2, int n3, int niter,
+                          int ns1, int ns2, int order1, int order2, float eps, void* workspace,
+                          size_t workspace_bytes, pwd_stream_t stream) {
+  if (!din || !dipi || !dipx || !mask || !out || !pwd::sint_args_ok(n1, n2, n3, niter, ns1, ns2) ||
+      order1 < 1 || order2 < 1)
+    return PWD_EINVAL;
+  if (order1 > PWD_MAX_ORDER || order2 > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  return pwd::sint_run(din, dipi, dipx, mask, out, n1, n2, n3, niter, ns1, ns2, order1, order2,
+                       eps, true, workspace, workspace_bytes, (cudaStream_t)stream);
 }

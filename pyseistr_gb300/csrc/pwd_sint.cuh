@@ -1,9 +1,10 @@
 // Sparse-data interpolation (csint2d, pyseistr/src/soint2d_cfuns.c:2421-2523,
-// called by sint2dc, sint.py:61): the shaping-regularised conjugate
+// called by sint2dc, sint.py:61, and csint3d, soint3d_cfuns.c:2510-2612,
+// called by sint3dc, sint.py:97): the shaping-regularised conjugate
 // gradients of ps_conjgrad (:888-1012, prec = NULL, given initial model)
 // whose operator is the known-sample mask (ps_mask_lop :145-157) and whose
 // shaping is the normalised plane-wave smoothing S of csomean2d (pwsmooth_*,
-// the spray-weighted mean).
+// the spray-weighted mean; in 3-D inline then crossline, below).
 //
 // The driver below is host code shared by the GPU entry (pwd_sint.cu, whose
 // Ops launch the kernels) and by the CPU test harness (whose Ops run the
@@ -87,6 +88,47 @@ PWD_SINT_HD void step_sample(const Vecs& v, long i, float a) {
 inline float lambda_of(unsigned long long known, long n) {
   const float k = known >= 16777216ull ? 16777216.f : (float)known;
   return sqrtf(k / (float)n);
+}
+
+// 3-D smoothing of csint3d (pwsmooth3_lop, soint3d_cfuns.c:2157-2300): the
+// 2-D smoothing along the inline slope on every (n1, n2) slice, then along
+// the crossline slope on every (n1, n3) section of the cube transposed from
+// [n3][n2][n1] (index i1 + n1 (i2 + n2 i3)) to [n2][n3][n1] (index
+// i1 + n1 (i3 + n3 i2)); the adjoint in reverse, adding into the model.
+// Element e of the transposed cube from the cube:
+PWD_SINT_HD void to_crossline_sample(const float* c, float* t, int n1, int n2, int n3, long e) {
+  const long i1 = e % n1, r = e / n1, i3 = r % n3, i2 = r / n3;
+  t[e] = c[i1 + n1 * (i2 + (long)n2 * i3)];
+}
+// Element e of the cube from the transposed cube; `sum` is the forward's
+// final `smooth += xtmp` into a zeroed array (0 + v).
+PWD_SINT_HD void from_crossline_sample(const float* t, float* c, int n1, int n2, int n3, long e,
+                                       bool sum) {
+  const long i1 = e % n1, r = e / n1, i2 = r % n2, i3 = r / n2;
+  const float v = t[i1 + n1 * (i3 + (long)n3 * i2)];
+  c[e] = sum ? 0.f + v : v;
+}
+
+// The sequence of pwsmooth3_lop on primitives P: inline(mode, in, out) and
+// crossline(mode, in, out) apply the 2-D smoothing on the cube's slices or
+// the transposed cube's sections (mode 0: out = S in; 1: out += S' in; 2:
+// out = S' in), to_cross(c, t) and from_cross(t, c, sum) transpose.
+template <class P>
+int smooth3_forward(P& pr, float* trace, float* smooth, float* itmp, float* itmp2, float* xtmp) {
+  int rc;
+  if ((rc = pr.inline_(0, trace, itmp))) return rc;
+  if ((rc = pr.to_cross(itmp, itmp2))) return rc;
+  if ((rc = pr.crossline(0, itmp2, xtmp))) return rc;
+  return pr.from_cross(xtmp, smooth, true);
+}
+template <class P>
+int smooth3_adjoint_add(P& pr, float* smooth, float* trace, float* itmp, float* itmp2,
+                        float* xtmp) {
+  int rc;
+  if ((rc = pr.to_cross(smooth, xtmp))) return rc;
+  if ((rc = pr.crossline(2, xtmp, itmp2))) return rc;
+  if ((rc = pr.from_cross(itmp2, itmp, false))) return rc;
+  return pr.inline_(1, itmp, trace);
 }
 
 // Vector names the driver passes to Ops.

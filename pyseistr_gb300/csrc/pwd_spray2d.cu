@@ -534,22 +534,23 @@ int batch_table2(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
 
 }  // namespace
 
-// The 2-D plane-wave smoothing of one section for the sparse-data
-// interpolation (pwd_sint.cu): add = 0 gives out = S in (the weighted spray
-// mean, as pwd_somean2d), add = 1 gives out += S' in, the adjoint adding its
-// terms into out in the reference's order.  `in` and `out` must not overlap.
-size_t smooth2_workspace(int n1, int n2, int ns, int order) {
-  if (check2(n1, n2, 1, ns, order) != PWD_OK) return 0;
-  return std::max(need_single(n1, n2, 1, ns, order, kMean, 1),
-                  need_single(n1, n2, 1, ns, order, kMeanAdjAdd, 1));
+// The 2-D plane-wave smoothing of the n3 (n1, n2) slices of one section for
+// the sparse-data interpolation (pwd_sint.cu): mode 0 gives out = S in (the
+// weighted spray mean, as pwd_somean2d), mode 1 gives out += S' in, the
+// adjoint adding its terms into out in the reference's order, and mode 2
+// out = S' in (pwd_somean2d's adjoint).  `in` and `out` must not overlap.
+size_t smooth2_workspace(int n1, int n2, int n3, int ns, int order) {
+  if (check2(n1, n2, n3, ns, order) != PWD_OK) return 0;
+  return std::max(need_single(n1, n2, n3, ns, order, kMean, 1),
+                  need_single(n1, n2, n3, ns, order, kMeanAdjAdd, 1));
 }
 
-int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int ns, int order,
-                float eps, int add, void* ws, size_t wsb, cudaStream_t st) {
-  int rc = check2(n1, n2, 1, ns, order);
+int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int n3, int ns,
+                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st) {
+  int rc = check2(n1, n2, n3, ns, order);
   if (rc != PWD_OK) return rc;
-  return run_single(in, dip, out, n1, n2, 1, ns, order, eps, add ? kMeanAdjAdd : kMean, 1, 0, ws,
-                    wsb, st);
+  const int filter = mode == 1 ? kMeanAdjAdd : (mode == 2 ? kMeanAdj : kMean);
+  return run_single(in, dip, out, n1, n2, n3, ns, order, eps, filter, 1, 0, ws, wsb, st);
 }
 
 }  // namespace pwd

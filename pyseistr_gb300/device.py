@@ -396,3 +396,27 @@ def sint2d(din, dip, mask, n1, n2, niter, ns, order, eps, out=None, workspace=No
                             int(ns), int(order), float(eps), _ptr(ws),
                             ws.numel() * ws.element_size(), _stream()), "sint2d")
     return out
+
+
+def sint3d(din, dipi, dipx, mask, n, niter, ns, order, eps, out=None, workspace=None):
+    """Sparse-data interpolation of a cube (pwd_sint3d): n = (n1, n2, n3),
+    ns = (ns1, ns2) and order = (order1, order2) for the inline and the
+    crossline smoothing; flat column-major CUDA float32 arrays.  Synchronises
+    the current stream during the call."""
+    L = _lib.load()
+    n1, n2, n3 = (int(v) for v in n)
+    ns1, ns2 = (int(v) for v in ns)
+    o1, o2 = (int(v) for v in order)
+    m = n1 * n2 * n3
+    din = _as_flat(din, m, "din")
+    dipi = _as_flat(dipi, m, "dipi")
+    dipx = _as_flat(dipx, m, "dipx")
+    mask = _as_flat(mask, m, "mask")
+    ws = _workspace(L.pwd_sint3d_workspace_size(n1, n2, n3, ns1, ns2, o1, o2), din.device,
+                    workspace)
+    if out is None:
+        out = torch.empty(m, dtype=torch.float32, device=din.device)
+    _lib.check(L.pwd_sint3d(_ptr(din), _ptr(dipi), _ptr(dipx), _ptr(mask), _ptr(out), n1, n2, n3,
+                            int(niter), ns1, ns2, o1, o2, float(eps), _ptr(ws),
+                            ws.numel() * ws.element_size(), _stream()), "sint3d")
+    return out

@@ -139,3 +139,8 @@ def test_sint_entry_checks_arguments_on_the_host():
     assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, -1, 1, 1, 0.01, fake, need, None) == _lib.PWD_EINVAL
     assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, 5, 1, 5, 0.01, fake, need, None) == _lib.PWD_ENOTSUP
     assert lib.pwd_sint2d(fake, fake, fake, fake, 40, 10, 5, 2, 2, 0.01, fake, need - 256, None) == _lib.PWD_EWORKSPACE
+    need3 = lib.pwd_sint3d_workspace_size(24, 5, 6, 1, 2, 2, 1)
+    assert need3 >= 12 * 24 * 5 * 6 * 4
+    assert lib.pwd_sint3d_workspace_size(24, 5, 6, 1, 2, 2, 5) == 0
+    assert lib.pwd_sint3d(fake, fake, fake, fake, fake, 24, 5, 0, 5, 1, 1, 1, 1, 0.01, fake, need3, None) == _lib.PWD_EINVAL
+    assert lib.pwd_sint3d(fake, fake, fake, fake, fake, 24, 5, 6, 5, 1, 2, 2, 1, 0.01, fake, need3 - 256, None) == _lib.PWD_EWORKSPACE

@@ -117,3 +117,26 @@ def test_sparse_interpolation_api(ps):
     b = ps.sint2dc(torch.from_numpy(d), torch.from_numpy(mask), torch.from_numpy(dip),
                    niter=12, ns=2, order=2)
     assert tuple(b.shape) == (80, 24) and np.array_equal(b.numpy(), a)
+
+
+def test_sparse_interpolation_3d_api(ps, emulated, monkeypatch):
+    from pyseistr_gb300 import device as D
+
+    sint = emulated[2]
+    sint.emu_sint3d.argtypes = [P] * 5 + [I] * 8 + [F]
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def sint3d(din, dipi, dipx, mask, n, niter, ns, order, eps, out=None, workspace=None):
+        m = n[0] * n[1] * n[2]
+        assert all(t.numel() == m and t.is_contiguous() for t in (din, dipi, dipx, mask))
+        out = torch.empty(m, dtype=torch.float32)
+        assert sint.emu_sint3d(ptr(din), ptr(dipi), ptr(dipx), ptr(mask), ptr(out), *n, niter,
+                               *ns, *order, float(eps)) == 0
+        return out
+
+    monkeypatch.setattr(D, "sint3d", sint3d)
+    import test_gpu_zsint as T
+
+    T.test_sint3dc_matches_reference(ps)
+    for c in T.CASES3[1:]:
+        T.test_sint3dc_matches_oracle(ps, c)

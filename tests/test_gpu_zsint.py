@@ -89,3 +89,51 @@ def test_csint2d_refuses_bad_arguments(ps):
         ps.csint2d(d, d, d, 40, 11, 5, 1, 1, 0, 0.01)
     with pytest.raises(ValueError):  # short mask
         ps.csint2d(d, d, d[:100], 40, 10, 5, 1, 1, 0, 0.01)
+
+
+def test_sint3dc_matches_reference(ps):
+    z = np.load(GOLDEN)
+    for m in json.loads(bytes(z["meta"]).decode()):
+        if m["dim"] != 3:
+            continue
+        k = m["k"]
+        got = ps.sint3dc(z[f"d3_{k}"], z[f"m3_{k}"], z[f"pi3_{k}"], z[f"px3_{k}"],
+                         niter=m["niter"], eps=m["eps"], ns1=m["ns"][0], ns2=m["ns"][1],
+                         order1=m["order"][0], order2=m["order"][1])
+        want = z[f"o3_{k}"]
+        assert got.dtype == np.float32 and got.shape == want.shape
+        assert rel_l2(got, want) <= DIP_TOL, k
+
+
+CASES3 = [
+    # n1, n2, n3, niter, (ns1, ns2), (order1, order2), eps, known fraction, seed
+    (64, 20, 16, 10, (2, 2), (2, 2), 0.01, 0.5, 31),
+    (40, 9, 7, 8, (1, 2), (2, 1), 0.01, 0.3, 32),
+    (24, 5, 11, 12, (2, 1), (1, 3), 0.05, 0.5, 33),
+    (16, 6, 1, 6, (2, 2), (2, 2), 0.01, 0.4, 34),
+    (16, 1, 6, 6, (1, 1), (2, 2), 0.01, 0.4, 35),
+]
+
+
+def _case3(n1, n2, n3, frac, seed):
+    rng = np.random.default_rng(seed)
+    keep = (rng.random((n2, n3)) < frac).astype(np.float32)
+    mask = np.repeat(keep[None], n1, 0)
+    d = (rng.standard_normal((n1, n2, n3)) * mask).astype(np.float32)
+    pi = (rng.standard_normal((n1, n2, n3)) * 0.6).astype(np.float32)
+    px = (rng.standard_normal((n1, n2, n3)) * 0.6).astype(np.float32)
+    return d, mask, pi, px
+
+
+@pytest.mark.parametrize("case", CASES3, ids=[f"sint3d-{c[0]}x{c[1]}x{c[2]}-it{c[3]}"
+                                              for c in CASES3])
+def test_sint3dc_matches_oracle(ps, case):
+    from oracle import oracle as O
+
+    n1, n2, n3, niter, ns, order, eps, frac, seed = case
+    d, mask, pi, px = _case3(n1, n2, n3, frac, seed)
+    want = O.sint3d(d, mask, pi, px, niter=niter, eps=eps, ns1=ns[0], ns2=ns[1], order1=order[0],
+                    order2=order[1])
+    got = ps.sint3dc(d, mask, pi, px, niter=niter, eps=eps, ns1=ns[0], ns2=ns[1],
+                     order1=order[0], order2=order[1])
+    assert rel_l2(got, want) <= DIP_TOL
