@@ -358,6 +358,25 @@ int pwd_sint3d(const float *din, const float *dipi, const float *dipx, const flo
                int order2, float eps, void *workspace, size_t workspace_bytes,
                pwd_stream_t stream);
 
+/* ---- FK dip filter (pyseistr/fk.py fkdip) ---------------------------------
+ * Replaces fkdip (fk.py:2, numpy in the reference): the part of the
+ * (n1, n2) section d inside the cone of half-width w nk columns around k = 0
+ * of its FK spectrum, back in time and space, as float64 out[n2][n1] (the
+ * reference returns float64).  The FFTs are zero-padded to nf =
+ * nextpow2(n1) and nk = nextpow2(n2); the time and space FFTs run in the
+ * input's precision (complex64 for pwd_fkdip, complex128 for pwd_fkdip_f64,
+ * as numpy keeps the input's precision), the mask promotes to complex128 and
+ * the inverse FFTs run in complex128.  Not bit-identical to numpy's FFTs:
+ * about 1e-7 relative for float input, 1e-15 for double.  w = 0 is
+ * PWD_EINVAL (the reference divides by zero).  Device pointers; workspace
+ * of pwd_fkdip_workspace_size bytes (f64: the double entry's; 0 for
+ * invalid sizes). */
+size_t pwd_fkdip_workspace_size(int n1, int n2, int f64);
+int pwd_fkdip(const float *d, double *out, int n1, int n2, double w, void *workspace,
+              size_t workspace_bytes, pwd_stream_t stream);
+int pwd_fkdip_f64(const double *d, double *out, int n1, int n2, double w, void *workspace,
+                  size_t workspace_bytes, pwd_stream_t stream);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long pwd_launch_count(void);
 /* Start recording a CUDA event pair around every launch (process-wide; for

@@ -27,6 +27,7 @@ sm_103a kernels of libpwd_gb300.so:
                                    relative geological time (pyseistr/rgt.py)
     sint2dc, sint3dc,              sparse-data interpolation along the
     csint2d, csint3d               slopes (pyseistr/sint.py)
+    fkdip                          FK dip (cone) filter (pyseistr/fk.py)
 
 `pyseistr_gb300.device` has the device-resident (CUDA tensor) forms.
 """
@@ -51,6 +52,7 @@ from .api import (  # noqa: F401
     dip_soint3d_packed,
     dip3dc,
     dipc,
+    fkdip,
     patch2d,
     patch2d_inv,
     patch3d,

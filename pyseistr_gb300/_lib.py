@@ -55,6 +55,9 @@ SIGNATURES = {
     "pwd_sint2d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_sint2d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_sint3d_workspace_size": ([_I] * 7, _S),
+    "pwd_fkdip_workspace_size": ([_I, _I, _I], _S),
+    "pwd_fkdip": ([_P, _P, _I, _I, ctypes.c_double, _P, _S, _P], _I),
+    "pwd_fkdip_f64": ([_P, _P, _I, _I, ctypes.c_double, _P, _S, _P], _I),
     "pwd_sint3d": ([_P] * 5 + [_I] * 8 + [_F, _P, _S, _P], _I),
     "pwd_soint3d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_soint3d": ([_P, _P, _P, _P, _P] + [_I] * 10 + [_F, _P, _S, _P], _I),

@@ -749,3 +749,38 @@ def sint3dc(din, mask, dipi, dipx, niter=100, eps=0.01, ns1=1, ns2=1, order1=1, 
     if isinstance(dout, torch.Tensor):
         return _from_dev_flat(dout, (n1, n2, n3), True)
     return dout.reshape(n1, n2, n3, order="F")
+
+
+# --------------------------------------------------------------------------
+# FK dip filter (fk.py)
+# --------------------------------------------------------------------------
+def fkdip(d, w):
+    """fkdip (fk.py:2): the part of the 2-D section d inside the FK cone of
+    half-width w nk wavenumbers around k = 0 (nk = nextpow2 of the trace
+    count), back in time and space, as float64 (the reference's numpy
+    result type); the DAS chain subtracts it from the data.  float32 input
+    keeps its forward FFTs in complex64 and float64 input in complex128, as
+    numpy does (other types go through float64).  A CUDA tensor in gives a
+    float64 CUDA tensor out.  w = 0
+    raises ZeroDivisionError, as the reference's cone slope nrow / (w nk)
+    does."""
+    if len(d.shape) != 2:
+        raise ValueError("fkdip: d must be 2-D")
+    n1, n2 = (int(x) for x in d.shape)
+    if float(w) == 0.0:
+        raise ZeroDivisionError("float division by zero")
+    if isinstance(d, torch.Tensor):
+        t = d.to(device=_dev())
+        if t.dtype not in (torch.float32, torch.float16, torch.bfloat16):
+            t = t.to(torch.float64)
+        elif t.dtype != torch.float32:
+            t = t.to(torch.float32)
+        t = t.t().contiguous().view(-1)
+        out = D.fkdip(t, n1, n2, w)
+        return out.view(n2, n1).t()
+    a = np.asarray(d)
+    dt = np.float32 if a.dtype in (np.float32, np.float16) else np.float64
+    flat = np.ascontiguousarray(a.astype(dt, copy=False).reshape(-1, order="F"))
+    t = torch.from_numpy(flat).to(_dev())
+    out = D.fkdip(t, n1, n2, w)
+    return out.cpu().numpy().reshape(n1, n2, order="F")

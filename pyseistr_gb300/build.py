@@ -24,7 +24,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["pwd_capi.cu", "pwd_dip.cu", "pwd_spray2d.cu", "pwd_spray3d.cu", "pwd_soint3d.cu",
            "pwd_patch.cu", "pwd_bandpass.cu", "pwd_coh.cu",
-           "pwd_paint.cu", "pwd_sint.cu"]
+           "pwd_paint.cu", "pwd_sint.cu", "pwd_fk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]

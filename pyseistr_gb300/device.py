@@ -420,3 +420,25 @@ def sint3d(din, dipi, dipx, mask, n, niter, ns, order, eps, out=None, workspace=
                             int(niter), ns1, ns2, o1, o2, float(eps), _ptr(ws),
                             ws.numel() * ws.element_size(), _stream()), "sint3d")
     return out
+
+
+def fkdip(d, n1, n2, w, out=None, workspace=None):
+    """FK dip filter (pwd_fkdip / pwd_fkdip_f64) of the flat column-major
+    CUDA section d (float32 or float64, whose precision the forward FFTs
+    keep); returns the flat float64 cone-passed section."""
+    L = _lib.load()
+    n1, n2 = int(n1), int(n2)
+    if not isinstance(d, torch.Tensor) or not d.is_cuda:
+        raise TypeError("d must be a CUDA tensor")
+    if d.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"d must be float32 or float64, got {d.dtype}")
+    if d.numel() != n1 * n2 or not d.is_contiguous():
+        raise ValueError(f"d: size {d.numel()} does not match {n1} x {n2} or is not contiguous")
+    f64 = d.dtype == torch.float64
+    ws = _workspace(L.pwd_fkdip_workspace_size(n1, n2, int(f64)), d.device, workspace)
+    if out is None:
+        out = torch.empty(n1 * n2, dtype=torch.float64, device=d.device)
+    fn = L.pwd_fkdip_f64 if f64 else L.pwd_fkdip
+    _lib.check(fn(_ptr(d), _ptr(out), n1, n2, float(w), _ptr(ws), ws.numel() * ws.element_size(),
+                  _stream()), "fkdip")
+    return out

@@ -144,3 +144,16 @@ def test_sint_entry_checks_arguments_on_the_host():
     assert lib.pwd_sint3d_workspace_size(24, 5, 6, 1, 2, 2, 5) == 0
     assert lib.pwd_sint3d(fake, fake, fake, fake, fake, 24, 5, 0, 5, 1, 1, 1, 1, 0.01, fake, need3, None) == _lib.PWD_EINVAL
     assert lib.pwd_sint3d(fake, fake, fake, fake, fake, 24, 5, 6, 5, 1, 2, 2, 1, 0.01, fake, need3 - 256, None) == _lib.PWD_EWORKSPACE
+
+
+def test_fk_entry_checks_arguments_on_the_host():
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+    need = lib.pwd_fkdip_workspace_size(100, 30, 0)
+    need64 = lib.pwd_fkdip_workspace_size(100, 30, 1)
+    assert need > 0 and need64 > need and need % 256 == 0
+    assert lib.pwd_fkdip_workspace_size(0, 30, 0) == 0
+    assert lib.pwd_fkdip(fake, fake, 100, 30, 0.0, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_fkdip(None, fake, 100, 30, 0.05, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_fkdip(fake, fake, 100, 30, 0.05, fake, need - 256, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_fkdip_f64(fake, fake, 100, 30, 0.05, fake, need, None) == _lib.PWD_EWORKSPACE

@@ -140,3 +140,42 @@ def test_sparse_interpolation_3d_api(ps, emulated, monkeypatch):
     T.test_sint3dc_matches_reference(ps)
     for c in T.CASES3[1:]:
         T.test_sint3dc_matches_oracle(ps, c)
+
+
+def test_fk_api(ps, tmp_path, monkeypatch):
+    from pyseistr_gb300 import device as D
+
+    lib = _build(tmp_path, "fk_emu")
+    D_ = ctypes.c_double
+    lib.emu_fkdip.argtypes = lib.emu_fkdip_f64.argtypes = [P, P, I, I, D_]
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def fkdip(d, n1, n2, w, out=None, workspace=None):
+        assert d.numel() == n1 * n2 and d.is_contiguous()
+        assert d.dtype in (torch.float32, torch.float64)
+        out = torch.empty(n1 * n2, dtype=torch.float64)
+        fn = lib.emu_fkdip_f64 if d.dtype == torch.float64 else lib.emu_fkdip
+        assert fn(ptr(d), ptr(out), n1, n2, float(w)) == 0
+        return out
+
+    monkeypatch.setattr(D, "fkdip", fkdip)
+    monkeypatch.setattr(api_module(), "_dev", lambda: torch.device("cpu"))
+    import test_gpu_zfk as T
+
+    T.test_fkdip_matches_reference(ps)
+    for c in T.CASES[1:]:
+        T.test_fkdip_matches_oracle(ps, c)
+    T.test_fkdip_zero_width_raises_like_the_reference(ps)
+    d = np.random.default_rng(21).standard_normal((200, 64)).astype(np.float32)
+    a = ps.fkdip(d, 0.05)
+    b = ps.fkdip(torch.from_numpy(d), 0.05)
+    assert b.dtype == torch.float64 and np.array_equal(b.numpy(), a)
+    e = np.random.default_rng(22).standard_normal((200, 64)).astype(np.float32)
+    both = ps.fkdip((2 * d - 3 * e).astype(np.float32), 0.05)
+    assert T.rel_l2(both, 2 * a - 3 * ps.fkdip(e, 0.05)) <= 1e-5
+
+
+def api_module():
+    from pyseistr_gb300 import api
+
+    return api
