@@ -14,6 +14,10 @@ filter) over one batch of seeded synthetic input of a named workload:
              (r1 = r2 = 4)
   patches3d  64 cubes; dip3d + soint3d (order 2, niter 20)
 
+Opt-in legs of the steps either side of the path: patch2d (patch2d +
+patch2d_inv), bandpass2d (bandpassc of DAS records) and das_fkcoh (fkdip +
+cohc of a DAS detection window).
+
 metric: output samples per second (input samples fully processed by slope
 estimation and filter per second).  `value` is timed on the device with
 inputs resident in HBM; `e2e` is the same through the public drop-in API
@@ -881,13 +885,147 @@ def run_bandpass(args):
     return 0
 
 
+DASCOH = {"channels": 860, "w": 0.05, "nv": 100, "vmax": 0.005, "dt": 0.0005}
+
+
+def run_das_fkcoh(args):
+    """The DAS chain's last two steps on one detection window
+    (demos/test_pyseistr_das_massive.py:198-200): fkdip(w = 0.05) and the
+    adjoint coherence cohc over 100 linear slopes in [-0.005, 0.005] s per
+    channel, on a 2000-sample x 860-channel window of the DAS-like record.
+    Opt-in (--workload das_fkcoh); samples/s = window samples per step time."""
+    rank, world, local = dist_info()
+    p = DASCOH
+    d = np.ascontiguousarray(W.das2d(seed=args.seed + rank)[:, :p["channels"]])
+    n1, n2 = d.shape
+    v = np.linspace(-p["vmax"], p["vmax"], p["nv"]).astype(np.float32)
+    h = np.arange(n2, dtype=np.float32)
+    metric = "window samples/sec (fkdip + cohc adjoint, DAS detection window)"
+    config = {"workload": f"das_fkcoh: fkdip(w {p['w']}) + cohc(adjoint, linear, {p['nv']} "
+                          f"slopes) of one {n1} x {n2} window per step",
+              "samples_per_step": n1 * n2,
+              "l2": "the window (6.9 MB) fits in L2; the FFT buffers (about 400 MB) do not"}
+    if args.impl == "reference" or (rank == 0 and world == 1 and not args.no_cpu_baseline):
+        from oracle import fk_oracle as F
+        from oracle import oracle as O
+
+        def cpu_step():
+            t0 = time.perf_counter()
+            F.fkdip(d, p["w"])
+            O.Coherence()(d, v, h, 1, n1, p["dt"], -1)
+            return time.perf_counter() - t0
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        tt = 0.0
+        for k in range(args.warmup + args.steps):
+            t = cpu_step()
+            if k >= args.warmup:
+                tt += t
+        value = args.steps * n1 * n2 / tt
+        desc = "numpy fkdip restatement and the C coherence restatement, one core"
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": value, "unit": "samples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+            "config": dict(config, sample=desc),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": 1, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return 0
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import pyseistr_gb300 as ps
+    from pyseistr_gb300 import _lib
+    from pyseistr_gb300 import device as D
+
+    _lib.load()
+    dev = torch.device("cuda", local)
+    x = torch.from_numpy(np.ascontiguousarray(d.reshape(-1, order="F"))).to(dev)
+    vt, ht = torch.from_numpy(v).to(dev), torch.from_numpy(h).to(dev)
+    fk_out = torch.empty(n1 * n2, dtype=torch.float64, device=dev)
+    coh_out = torch.empty(n1 * p["nv"], dtype=torch.float32, device=dev)
+    ws = torch.empty(_lib.load().pwd_fkdip_workspace_size(n1, n2, 0), dtype=torch.uint8,
+                     device=dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def step():
+        D.fkdip(x, n1, n2, p["w"], out=fk_out, workspace=ws)
+        D.coherence(x, vt, ht, 1, n1, p["dt"], -1, 0.0, out=coh_out)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    fk_ms = coh_ms = 0.0
+    with ClockSampler(local) as clk:
+        l0 = _lib.launch_count()
+        t_all = 0.0
+        for _ in range(args.steps):
+            e[0].record()
+            D.fkdip(x, n1, n2, p["w"], out=fk_out, workspace=ws)
+            e[1].record()
+            D.coherence(x, vt, ht, 1, n1, p["dt"], -1, 0.0, out=coh_out)
+            e[2].record()
+            torch.cuda.synchronize()
+            fk_ms += e[0].elapsed_time(e[1])
+            coh_ms += e[1].elapsed_time(e[2])
+            t_all += e[0].elapsed_time(e[2])
+    launches = _lib.launch_count() - l0
+    ms = max_over_ranks(t_all, dev) if world > 1 else t_all
+    ms_step = ms / args.steps
+    # algorithmic bytes of the FK filter: the window read (4 B) and the
+    # float64 result written (8 B) per sample
+    fk_bytes = 12 * n1 * n2
+    achieved = fk_bytes / (fk_ms / args.steps / 1e3) / 1e9
+    peak, peak_src = measured_hbm_peak()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ps.cohc(d - ps.fkdip(d, p["w"]), {"h": h, "v": v, "nt": n1, "dt": p["dt"], "typ": 1})
+    e2e = world * n1 * n2 / ((time.perf_counter() - t0) / args.steps)
+    line = {
+        "metric": metric, "value": world * n1 * n2 / (ms_step / 1e3), "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
+        "config": dict(config, parallelism=f"replicas x{world}", fk_ms=fk_ms / args.steps,
+                       coh_ms=coh_ms / args.steps),
+        "e2e": {"value": e2e, "unit": "samples/s", "h2d_bytes_per_step": 4 * n1 * n2,
+                "d2h_bytes_per_step": 4 * n1 * p["nv"],
+                "path": "fkdip then cohc on the difference, host arrays, as the DAS demo"},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "kernel": "fkdip (all passes)", "achieved": achieved,
+                     "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "bytes_per_launch": fk_bytes},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t = cpu_step()
+        line["cpu_baseline"] = {"value": n1 * n2 / t, "unit": "samples/s", "cores": 1,
+                                "kind": "port",
+                                "sample": "one window: oracle/fk_oracle.py and the coherence "
+                                          "restatement of oracle/pwd_oracle.cpp"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["patch2d", "bandpass2d"], default="batch2d")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["patch2d", "bandpass2d",
+                                                               "das_fkcoh"], default="batch2d")
     ap.add_argument("--seed", type=int, default=2023)
     ap.add_argument("--sections", type=int, default=512,
                     help="sections of the batch2d workload, patches of patches3d (at most 64); "
@@ -910,6 +1048,8 @@ def main():
         return run_patch(args)
     if args.workload == "bandpass2d":
         return run_bandpass(args)
+    if args.workload == "das_fkcoh":
+        return run_das_fkcoh(args)
     if args.impl == "reference":
         return run_reference(args)
 
