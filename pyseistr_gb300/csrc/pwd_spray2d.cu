@@ -247,12 +247,13 @@ __global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ 
 
 // Adjoint of the weighted mean (pwsmooth_lop adjoint :1072-1086 with
 // pwspray_lop adjoint :957-989).  Thread per output trace; chain traces in a
-// per-thread buffer.  ADD: the terms are added into `out` as it stands (the
-// adjoint with add = true, as the sparse-data interpolation's CG applies it,
-// soint2d_cfuns.c:2194-2220) instead of into zeros.
-template <int NW, bool ADD = false>
+// per-thread buffer.  add != 0: the terms are added into `out` as it stands
+// (the adjoint with add = true, as the sparse-data interpolation's CG applies
+// it, soint2d_cfuns.c:2194-2220) instead of into zeros.
+template <int NW>
 __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restrict__ dip,
-                               float* __restrict__ out, SprayBufs bf, SprayB b, ApCoef c) {
+                               float* __restrict__ out, SprayBufs bf, SprayB b, ApCoef c,
+                               int add) {
   long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= b.ntr) return;
   long q;
@@ -283,7 +284,7 @@ __global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restr
     predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)(ip - 1) * n1, true, my, my.y);
   }
   for (int i1 = 0; i1 < n1; i1++) {
-    o[i1] = __fadd_rn(ADD ? o[i1] : 0.f, tr[i1]);
+    o[i1] = __fadd_rn(add ? o[i1] : 0.f, tr[i1]);
     tr[i1] = 0.f;
   }
   for (int is = b.ns - 1; is >= 0; is--) {
@@ -445,12 +446,9 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
     // the adjoint chains reuse the scratch region as their per-chain scratch
-    if (filter == kMeanAdj)
-      PWD_KERNEL(PWD_FAM_SPRAY, st,
-                 k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c));
-    else
-      PWD_KERNEL(PWD_FAM_SPRAY, st,
-                 (k_somean2d_adj<NW, true><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c)));
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c,
+                                                      filter == kMeanAdjAdd ? 1 : 0));
   } else {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
