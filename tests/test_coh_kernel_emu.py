@@ -80,6 +80,8 @@ CASES = [
     (3, 120, 11, 15, 0.002, 1, 7, (1500.0, 4000.0), (-300.0, 400.0)),
     (3, 120, 11, 15, 0.002, -1, 8, (1500.0, 4000.0), (-300.0, 400.0)),
     (7, 50, 5, 6, 0.004, -1, 9, (-0.01, 0.01), (0.0, 5.0)),  # unknown type: linear
+    (2, 80, 6, 9, 0.004, -1, 12, (-0.2, 0.1), (-60.0, 20.0)),  # negative hmax state
+    (3, 60, 7, 9, 0.002, 1, 13, (-3000.0, -1500.0), (-100.0, 100.0)),  # negative velocities
     (1, 1, 1, 1, 0.004, 1, 10, (0.0, 0.0), (0.0, 0.0)),
     (1, 1, 1, 1, 0.004, -1, 11, (0.0, 0.0), (0.0, 0.0)),
 ]

@@ -61,6 +61,8 @@ CASES = [
     (7, 1, 0.3, np.float32, 6),     # one trace
     (2, 2, 0.5, np.float64, 7),
     (257, 129, -0.03, np.float32, 8),  # negative width: the cone test as the reference's
+    (64, 40, 2.0, np.float32, 9),      # a cone wider than the plane
+    (3, 3, 0.5, np.float64, 10),
 ]
 
 

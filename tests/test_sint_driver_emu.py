@@ -56,6 +56,7 @@ CASES = [
     (40, 10, 10, 2, 2, 0.01, 1.0, 4),    # everything known
     (40, 10, 10, 2, 2, 0.01, 0.0, 5),    # nothing known: r0 = 0, returns S d
     (40, 10, 0, 1, 1, 0.01, 0.4, 6),     # no iterations
+    (16, 4, 30, 0, 1, 0.01, 0.5, 2),     # the stopping test ends the loop after one step
 ]
 
 
