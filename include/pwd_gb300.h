@@ -309,6 +309,15 @@ int pwd_bandpass(const float *in, float *out, int n1, int n2, int n3, float d1, 
  * workspace; `out` must not overlap `in`. */
 int pwd_coherence(const float *in, const float *v, const float *h, int typ, int nt, int nv,
                   int nh, float dt, int forw, float hmax, float *out, pwd_stream_t stream);
+/* nwin windows of the same sizes stacked one after another in `in` and
+ * `out` (the windows of a DAS record, as the detection loop of
+ * demos/test_pyseistr_das_massive.py:190-203 calls cohc on each), in one
+ * launch: the same results as one pwd_coherence call per window (each
+ * window's past-the-end sample reads as 0).  No single reference entry: it
+ * replaces that loop of cohc_fb calls. */
+int pwd_coherence_batch(const float *in, const float *v, const float *h, int typ, int nt, int nv,
+                        int nh, int nwin, float dt, int forw, float hmax, float *out,
+                        pwd_stream_t stream);
 
 /* ---- Plane-wave painting (pyseistr/rgt.py pwpaintc, rgt; src/paint_cfuns.c
  * cpaint2d) ---------------------------------------------------------------

@@ -20,9 +20,9 @@ sm_103a kernels of libpwd_gb300.so:
     patch2d_inv, patch3d_inv       overlap-add inverse (pyseistr/patch.py)
     bandpassc, cbp                 Butterworth band-pass along each trace
                                    (pyseistr/bp.py)
-    cohc, cohc_fb                  time-domain Radon coherence along
+    cohc, cohc_fb, cohc_batch      time-domain Radon coherence along
                                    linear, parabolic or hyperbolic curves
-                                   (pyseistr/das.py)
+                                   (pyseistr/das.py); many windows at once
     pwpaintc, rgt, cpaint2d        plane-wave painting of a seed trace and
                                    relative geological time (pyseistr/rgt.py)
     sint2dc, sint3dc,              sparse-data interpolation along the
@@ -35,6 +35,7 @@ from .api import (  # noqa: F401
     bandpassc,
     cbp,
     cohc,
+    cohc_batch,
     cohc_fb,
     cpaint2d,
     csint2d,

@@ -50,6 +50,7 @@ SIGNATURES = {
     "pwd_patch_inv": ([_P, _P] + [_I] * 9 + [_P], _I),
     "pwd_bandpass": ([_P, _P, _I, _I, _I, _F, _F, _F, _I, _I, _I, _P], _I),
     "pwd_coherence": ([_P, _P, _P, _I, _I, _I, _I, _F, _I, _F, _P, _P], _I),
+    "pwd_coherence_batch": ([_P, _P, _P, _I, _I, _I, _I, _I, _F, _I, _F, _P, _P], _I),
     "pwd_paint2d_workspace_size": ([_I, _I], _S),
     "pwd_paint2d": ([_P, _P, _P, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_sint2d_workspace_size": ([_I, _I, _I, _I], _S),

@@ -622,6 +622,44 @@ def cohc(din, par, operator=-1, verb=0):
     return dout.reshape(nt, ncol, order="F")
 
 
+def cohc_batch(windows, par, operator=-1, verb=0):
+    """cohc (das.py:92) of many windows of the same shape in one launch (the
+    DAS detection loop over the windows of a record): `windows` is a list of
+    (nt, nh) arrays for operator -1 ((nt, nv) for 1) or one (nwin, nt, n)
+    array; returns the list of results, each what cohc gives for that
+    window.  The parabolic hmax state is updated once, as one cohc call."""
+    h, v = _host_f32(par["h"], "h"), _host_f32(par["v"], "v")
+    nt, dt, typ = int(par["nt"]), par["dt"], int(par["typ"])
+    nh, nv = h.size, v.size
+    if operator not in (1, -1):
+        raise ValueError(f"cohc_batch: operator must be 1 or -1, got {operator}")
+    wins = list(windows)
+    if not wins:
+        return []
+    ncol_in = nv if operator == 1 else nh
+    for w in wins:
+        if tuple(w.shape) != (nt, ncol_in):
+            raise ValueError(f"cohc_batch: window of shape {tuple(w.shape)}, expected "
+                             f"{(nt, ncol_in)}")
+    if typ not in (1, 2, 3):
+        typ = 1
+    if typ == 2:
+        coh_state.update(h)
+    if not _coh_indices_usable(v, h, typ, nt, dt, coh_state.hmax):
+        raise ValueError("cohc_batch: curve sample indices not finite or beyond 2e9 samples")
+    parts = [_to_dev_flat(w) for w in wins]
+    x = torch.cat([t for t, _ in parts])
+    dev = x.device
+    out = D.coherence_batch(x, torch.from_numpy(v).to(dev), torch.from_numpy(h).to(dev), typ, nt,
+                            len(wins), dt, operator, coh_state.hmax)
+    ncol = nh if operator == 1 else nv
+    res = out.view(len(wins), ncol, nt).transpose(1, 2)
+    if parts[0][1]:
+        return [r for r in res]
+    host = res.cpu().numpy()
+    return [np.ascontiguousarray(r) for r in host]
+
+
 # --------------------------------------------------------------------------
 # plane-wave painting (rgt.py / paint_cfuns.c cpaint2d)
 # --------------------------------------------------------------------------

@@ -10,7 +10,9 @@
 //
 // Forward: one thread per output trace, which adds the model along the
 // curves in the reference's order (bit-identical output); the parallelism
-// is the trace count.
+// is the trace count.  The batch entry stacks the windows of a record (the
+// DAS detection loop, demos/test_pyseistr_das_massive.py:190-203) in one
+// launch, which multiplies that parallelism.
 #include <cuda_runtime.h>
 
 #include "pwd_coh.cuh"
@@ -19,27 +21,29 @@
 namespace pwd {
 namespace {
 
-__global__ void __launch_bounds__(256) k_coh_adjoint(coh::CohParams q, long nmod) {
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nmod; k += stride)
-    q.out[k] = coh::adjoint_sample(q, k);
+// nwin windows stacked one after another in `in` and `out` (one window:
+// nwin = 1).
+__global__ void __launch_bounds__(256) k_coh_adjoint(coh::CohParams q, int nwin) {
+  const long stride = (long)gridDim.x * blockDim.x, n = (long)q.nt * q.nv * nwin;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += stride)
+    coh::adjoint_item(q, g);
 }
 
-__global__ void __launch_bounds__(32) k_coh_forward(coh::CohParams q) {
-  const int ih = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ih < q.nh) coh::forward_trace(q, ih);
+__global__ void __launch_bounds__(32) k_coh_forward(coh::CohParams q, int nwin) {
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < (long)q.nh * nwin) coh::forward_item(q, g);
 }
 
 }  // namespace
 }  // namespace pwd
 
-extern "C" int pwd_coherence(const float* in, const float* v, const float* h, int typ, int nt,
-                             int nv, int nh, float dt, int forw, float hmax, float* out,
-                             pwd_stream_t stream) {
-  if (!in || !v || !h || !out || nt < 1 || nv < 1 || nh < 1) return PWD_EINVAL;
+extern "C" int pwd_coherence_batch(const float* in, const float* v, const float* h, int typ,
+                                   int nt, int nv, int nh, int nwin, float dt, int forw,
+                                   float hmax, float* out, pwd_stream_t stream) {
+  if (!in || !v || !h || !out || nt < 1 || nv < 1 || nh < 1 || nwin < 1) return PWD_EINVAL;
   if (forw != 1 && forw != -1) return PWD_EINVAL;
   const long nmod = (long)nt * nv, ndata = (long)nt * nh;
-  if (nmod > (1L << 40) || ndata > (1L << 40)) return PWD_EINVAL;
+  if (nmod * nwin > (1L << 40) || ndata * nwin > (1L << 40)) return PWD_EINVAL;
   if (typ != 1 && typ != 2 && typ != 3) typ = 1;  // coh_init2 :169
   pwd::coh::CohParams q;
   q.in = in;
@@ -56,12 +60,18 @@ extern "C" int pwd_coherence(const float* in, const float* v, const float* h, in
   if (forw == -1) {
     // a grid of at most 32 waves of 152 SMs x 8 blocks; the loop strides
     // over the rest
-    const long blocks = (nmod + 255) / 256;
+    const long blocks = (nmod * nwin + 255) / 256;
     const unsigned grid = (unsigned)(blocks < 152L * 8 * 32 ? blocks : 152L * 8 * 32);
-    PWD_KERNEL(PWD_FAM_OTHER, st, (pwd::k_coh_adjoint<<<grid, 256, 0, st>>>(q, nmod)));
+    PWD_KERNEL(PWD_FAM_OTHER, st, (pwd::k_coh_adjoint<<<grid, 256, 0, st>>>(q, nwin)));
   } else {
-    const unsigned grid = (unsigned)((nh + 31) / 32);
-    PWD_KERNEL(PWD_FAM_OTHER, st, (pwd::k_coh_forward<<<grid, 32, 0, st>>>(q)));
+    const unsigned grid = (unsigned)(((long)nh * nwin + 31) / 32);
+    PWD_KERNEL(PWD_FAM_OTHER, st, (pwd::k_coh_forward<<<grid, 32, 0, st>>>(q, nwin)));
   }
   return pwd::cuda_status(cudaGetLastError());
+}
+
+extern "C" int pwd_coherence(const float* in, const float* v, const float* h, int typ, int nt,
+                             int nv, int nh, float dt, int forw, float hmax, float* out,
+                             pwd_stream_t stream) {
+  return pwd_coherence_batch(in, v, h, typ, nt, nv, nh, 1, dt, forw, hmax, out, stream);
 }

@@ -108,5 +108,23 @@ PWD_COH_HD void forward_trace(const CohParams& q, int ih) {
   }
 }
 
+// Stacked windows: element g of nwin windows' models (adjoint) or trace g
+// of their data (forward), window g / (nt nv) or g / nh.
+PWD_COH_HD void adjoint_item(const CohParams& q, long g) {
+  const long nmod = (long)q.nt * q.nv, w = g / nmod;
+  CohParams p = q;
+  p.in = q.in + w * (long)q.nt * q.nh;
+  p.out = q.out + w * nmod;
+  const long k = g - w * nmod;
+  p.out[k] = adjoint_sample(p, k);
+}
+PWD_COH_HD void forward_item(const CohParams& q, long g) {
+  const long w = g / q.nh;
+  CohParams p = q;
+  p.in = q.in + w * (long)q.nt * q.nv;
+  p.out = q.out + w * (long)q.nt * q.nh;
+  forward_trace(p, (int)(g - w * q.nh));
+}
+
 }  // namespace coh
 }  // namespace pwd

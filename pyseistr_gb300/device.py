@@ -361,6 +361,23 @@ def coherence(x, v, h, typ, nt, dt, forw, hmax, out=None):
     return out
 
 
+def coherence_batch(x, v, h, typ, nt, nwin, dt, forw, hmax, out=None):
+    """pwd_coherence_batch: `nwin` windows stacked in the flat CUDA float32
+    array x (each a model [nv][nt] for forw = 1, data [nh][nt] for -1)."""
+    L = _lib.load()
+    nt, nv, nh, nwin = int(nt), int(v.numel()), int(h.numel()), int(nwin)
+    x = _as_flat(x, nwin * nt * (nv if forw == 1 else nh), "x")
+    v = _as_flat(v, nv, "v")
+    h = _as_flat(h, nh, "h")
+    if out is None:
+        out = torch.empty(nwin * nt * (nh if forw == 1 else nv), dtype=torch.float32,
+                          device=x.device)
+    _lib.check(L.pwd_coherence_batch(_ptr(x), _ptr(v), _ptr(h), int(typ), nt, nv, nh, nwin,
+                                     float(dt), int(forw), float(hmax), _ptr(out), _stream()),
+               "coherence_batch")
+    return out
+
+
 def paint2d(dip, seed, n1, n2, order, i0, eps, out=None, workspace=None):
     """Plane-wave painting (pwd_paint2d) of the seed trace (CUDA float32,
     n1 samples) from trace i0 along the flat column-major slopes `dip` of an

@@ -5,9 +5,10 @@
 // library.
 #include "../../pyseistr_gb300/csrc/pwd_coh.cuh"
 
-extern "C" int emu_coherence(const float* in, const float* v, const float* h, int typ, int nt,
-                             int nv, int nh, float dt, int forw, float hmax, float* out) {
-  if (nt < 1 || nv < 1 || nh < 1 || (forw != 1 && forw != -1)) return 1;
+extern "C" int emu_coherence_batch(const float* in, const float* v, const float* h, int typ,
+                                   int nt, int nv, int nh, int nwin, float dt, int forw,
+                                   float hmax, float* out) {
+  if (nt < 1 || nv < 1 || nh < 1 || nwin < 1 || (forw != 1 && forw != -1)) return 1;
   if (typ != 1 && typ != 2 && typ != 3) typ = 1;
   pwd::coh::CohParams q;
   q.in = in;
@@ -21,10 +22,15 @@ extern "C" int emu_coherence(const float* in, const float* v, const float* h, in
   q.dt = dt;
   q.hmax = hmax;
   if (forw == -1) {
-    const long nmod = (long)nt * nv;
-    for (long k = 0; k < nmod; k++) out[k] = pwd::coh::adjoint_sample(q, k);
+    const long n = (long)nt * nv * nwin;
+    for (long g = 0; g < n; g++) pwd::coh::adjoint_item(q, g);
   } else {
-    for (int ih = 0; ih < nh; ih++) pwd::coh::forward_trace(q, ih);
+    for (long g = 0; g < (long)nh * nwin; g++) pwd::coh::forward_item(q, g);
   }
   return 0;
+}
+
+extern "C" int emu_coherence(const float* in, const float* v, const float* h, int typ, int nt,
+                             int nv, int nh, float dt, int forw, float hmax, float* out) {
+  return emu_coherence_batch(in, v, h, typ, nt, nv, nh, 1, dt, forw, hmax, out);
 }

@@ -110,6 +110,7 @@ def test_coherence_entry_checks_arguments_on_the_host():
     assert lib.pwd_coherence(fake, fake, fake, 1, 10, 0, 2, 0.004, 1, 0.0, fake, None) == ok
     assert lib.pwd_coherence(fake, fake, fake, 1, 10, 2, 0, 0.004, 1, 0.0, fake, None) == ok
     assert lib.pwd_coherence(fake, fake, fake, 2, 10, 2, 2, 0.004, 0, 0.0, fake, None) == ok
+    assert lib.pwd_coherence_batch(fake, fake, fake, 1, 10, 2, 2, 0, 0.004, -1, 0.0, fake, None) == ok
 
 
 def test_paint_entry_checks_arguments_on_the_host():

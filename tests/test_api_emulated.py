@@ -28,6 +28,7 @@ def emulated(tmp_path_factory):
     tmp = tmp_path_factory.mktemp("api_emu")
     coh, paint, sint = _build(tmp, "coh_emu"), _build(tmp, "paint_emu"), _build(tmp, "sint_emu")
     coh.emu_coherence.argtypes = [P, P, P, I, I, I, I, F, I, F, P]
+    coh.emu_coherence_batch.argtypes = [P, P, P, I, I, I, I, I, F, I, F, P]
     paint.emu_paint2d.argtypes = [P, P, P, I, I, I, I, F]
     sint.emu_sint2d.argtypes = [P, P, P, P, I, I, I, I, I, F]
     return coh, paint, sint
@@ -74,7 +75,17 @@ def ps(emulated, monkeypatch):
 
     monkeypatch.setattr(api, "_to_dev_flat", to_flat)
     monkeypatch.setattr(D, "sint2d", sint2d)
+    def coherence_batch(x, v, h, typ, nt, nwin, dt, forw, hmax, out=None):
+        nv, nh = v.numel(), h.numel()
+        assert x.numel() == nwin * nt * (nv if forw == 1 else nh) and x.is_contiguous()
+        out = torch.empty(nwin * nt * (nh if forw == 1 else nv), dtype=torch.float32)
+        assert coh.emu_coherence_batch(ptr(x), ptr(v), ptr(h), int(typ), int(nt), nv, nh,
+                                       int(nwin), float(dt), int(forw), float(hmax),
+                                       ptr(out)) == 0
+        return out
+
     monkeypatch.setattr(D, "coherence", coherence)
+    monkeypatch.setattr(D, "coherence_batch", coherence_batch)
     monkeypatch.setattr(D, "paint2d", paint2d)
     import pyseistr_gb300
 
@@ -88,6 +99,7 @@ def test_coherence_api(ps):
     for c in T.CASES[1:]:  # the first, a DAS window's shape, is left to the GPU run
         T.test_cohc_matches_oracle(ps, c)
     T.test_cohc_refuses_what_the_reference_cannot_compute(ps)
+    T.test_cohc_batch_equals_one_call_per_window(ps)
 
 
 def test_painting_api(ps):

@@ -160,3 +160,30 @@ def test_hmax_state_follows_the_reference_static():
         op(np.zeros((8, h.size), np.float32), v, h, 2, 8, 0.004, -1)
         st.update(h)
         assert st.hmax == op.hmax[0]
+
+
+@pytest.mark.parametrize("forw", [-1, 1])
+def test_emulated_stacked_windows_equal_one_call_per_window(tmp_path, forw):
+    """The batch decomposition (window of each thread) over 3 stacked
+    windows gives each window's single-call result."""
+    so = str(tmp_path / "libcoh_emu.so")
+    subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-o", so,
+                    os.path.join(HERE, "emu", "coh_emu.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    lib.emu_coherence_batch.argtypes = [P, P, P, I, I, I, I, I, F, I, F, P]
+    rng = np.random.default_rng(40)
+    nt, nv, nh, nwin = 90, 11, 17, 3
+    v = np.sort(rng.uniform(-0.01, 0.01, nv)).astype(np.float32)
+    h = np.arange(nh, dtype=np.float32)
+    wins = [rng.standard_normal((nt, nv if forw == 1 else nh)).astype(np.float32)
+            for _ in range(nwin)]
+    x = np.ascontiguousarray(np.concatenate([w.reshape(-1, order="F") for w in wins]))
+    out = np.full(nwin * nt * (nh if forw == 1 else nv), 7.0, np.float32)
+    p = lambda a: a.ctypes.data_as(P)  # noqa: E731
+    assert lib.emu_coherence_batch(p(x), p(v), p(h), 1, nt, nv, nh, nwin, 0.004, forw, 0.0,
+                                   p(out)) == 0
+    m = out.size // nwin
+    for k, w in enumerate(wins):
+        want = O.Coherence()(w, v, h, 1, nt, 0.004, forw).reshape(-1, order="F")
+        assert agrees(out[k * m:(k + 1) * m], want, w, v, h, 1, nt, 0.004, 0.0), k

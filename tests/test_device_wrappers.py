@@ -60,6 +60,8 @@ def test_coherence_wrapper(fake):
     out = D.coherence(_f(50 * 5), _f(5), _f(8), 2, 50, 0.004, 1, 3.0)
     assert out.numel() == 50 * 8
     assert [c[0] for c in lib.calls] == ["pwd_coherence"] * 2
+    out = D.coherence_batch(_f(3 * 50 * 8), _f(5), _f(8), 1, 50, 3, 0.004, -1, 0.0)
+    assert out.numel() == 3 * 50 * 5 and lib.calls[-1][0] == "pwd_coherence_batch"
 
 
 def test_paint_wrapper(fake):

@@ -108,3 +108,21 @@ def test_cohc_refuses_what_the_reference_cannot_compute(ps):
         ps.cohc_fb(d, v, h, 1, 20, 2, 2, 0.004, 0, 0)
     with pytest.raises(ValueError):  # fewer values than nt * nh
         ps.cohc_fb(d[:10], v, h, 1, 20, 2, 2, 0.004, -1, 0)
+
+
+def test_cohc_batch_equals_one_call_per_window(ps):
+    """The windows of a record in one launch give what one cohc call per
+    window gives, adjoint and forward."""
+    rng = np.random.default_rng(41)
+    nt, nh = 400, 64
+    v = np.linspace(-0.005, 0.005, 30).astype(np.float32)
+    h = np.arange(nh, dtype=np.float32)
+    par = {"h": h, "v": v, "nt": nt, "dt": 0.0005, "typ": 1}
+    wins = [rng.standard_normal((nt, nh)).astype(np.float32) for _ in range(5)]
+    got = ps.cohc_batch(wins, par)
+    for w, g in zip(wins, got):
+        assert np.array_equal(g, ps.cohc(w, par))
+    models = [rng.standard_normal((nt, v.size)).astype(np.float32) for _ in range(3)]
+    got = ps.cohc_batch(models, par, operator=1)
+    for m, g in zip(models, got):
+        assert np.array_equal(g, ps.cohc(m, par, operator=1))
