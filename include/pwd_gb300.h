@@ -335,6 +335,14 @@ int pwd_coherence_batch(const float *in, const float *v, const float *h, int typ
 size_t pwd_paint2d_workspace_size(int n1, int order);
 int pwd_paint2d(const float *dip, const float *seed, float *out, int n1, int n2, int order,
                 int i0, float eps, void *workspace, size_t workspace_bytes, pwd_stream_t stream);
+/* nsec sections of one size stacked one after another (dip and out at s n1
+ * n2, seed at s n1), each painted from its own seed trace at trace i0, in
+ * one launch: the same results as one pwd_paint2d call per section.  No
+ * single reference entry: it replaces a loop of cpaint2d calls. */
+size_t pwd_paint2d_batch_workspace_size(int n1, int nsec, int order);
+int pwd_paint2d_batch(const float *dip, const float *seed, float *out, int n1, int n2, int nsec,
+                      int order, int i0, float eps, void *workspace, size_t workspace_bytes,
+                      pwd_stream_t stream);
 
 /* ---- Sparse-data interpolation (pyseistr/sint.py sint2dc, src/soint2d_cfuns.c
  * csint2d) ------------------------------------------------------------------

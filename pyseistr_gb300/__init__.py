@@ -23,8 +23,8 @@ sm_103a kernels of libpwd_gb300.so:
     cohc, cohc_fb, cohc_batch      time-domain Radon coherence along
                                    linear, parabolic or hyperbolic curves
                                    (pyseistr/das.py); many windows at once
-    pwpaintc, rgt, cpaint2d        plane-wave painting of a seed trace and
-                                   relative geological time (pyseistr/rgt.py)
+    pwpaintc, rgt, cpaint2d,       plane-wave painting of a seed trace and
+    pwpaintc_batch                 relative geological time (pyseistr/rgt.py)
     sint2dc, sint3dc,              sparse-data interpolation along the
     csint2d, csint3d               slopes (pyseistr/sint.py)
     fkdip                          FK dip (cone) filter (pyseistr/fk.py)
@@ -59,6 +59,7 @@ from .api import (  # noqa: F401
     patch3d,
     patch3d_inv,
     pwpaintc,
+    pwpaintc_batch,
     rgt,
     sint2dc,
     sint3dc,

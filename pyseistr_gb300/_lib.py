@@ -53,6 +53,8 @@ SIGNATURES = {
     "pwd_coherence_batch": ([_P, _P, _P, _I, _I, _I, _I, _I, _F, _I, _F, _P, _P], _I),
     "pwd_paint2d_workspace_size": ([_I, _I], _S),
     "pwd_paint2d": ([_P, _P, _P, _I, _I, _I, _I, _F, _P, _S, _P], _I),
+    "pwd_paint2d_batch_workspace_size": ([_I, _I, _I], _S),
+    "pwd_paint2d_batch": ([_P, _P, _P, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_sint2d_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_sint2d": ([_P, _P, _P, _P, _I, _I, _I, _I, _I, _F, _P, _S, _P], _I),
     "pwd_sint3d_workspace_size": ([_I] * 7, _S),

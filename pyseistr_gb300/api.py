@@ -699,6 +699,31 @@ def pwpaintc(dip, trace, order=1, i0=0, eps=0.01, verb=False):
     return dout.reshape(n1, n2, order="F")
 
 
+def pwpaintc_batch(dips, traces, order=1, i0=0, eps=0.01):
+    """pwpaintc (rgt.py:51) of many (n1, n2) sections of one size in one
+    launch: `dips` a list of slope sections, `traces` their seed traces;
+    returns the list of painted sections, each what pwpaintc gives."""
+    dips, traces = list(dips), list(traces)
+    if not dips or len(dips) != len(traces):
+        raise ValueError("pwpaintc_batch: as many seed traces as sections, at least one")
+    n1, n2 = (int(x) for x in dips[0].shape)
+    if any(tuple(p.shape) != (n1, n2) for p in dips):
+        raise ValueError("pwpaintc_batch: the sections must have one size")
+    if not 0 <= int(i0) < n2 or n1 < 4:
+        raise ValueError("pwpaintc_batch: i0 outside [0, n2) or n1 < 4")
+    pp = [_to_dev_flat(p) for p in dips]
+    tt = [_to_dev_flat(t)[0] for t in traces]
+    if any(t.numel() < n1 for t in tt):
+        raise ValueError(f"pwpaintc_batch: seed traces need {n1} values")
+    p = torch.cat([x for x, _ in pp])
+    t = torch.cat([x[:n1] for x in tt])
+    out = D.paint2d_batch(p, t, n1, n2, len(dips), order, i0, eps).view(len(dips), n2, n1)
+    res = out.transpose(1, 2)
+    if pp[0][1]:
+        return [r for r in res]
+    return [np.ascontiguousarray(r) for r in res.cpu().numpy()]
+
+
 def rgt(dip, o1=0, d1=0.004, order=1, i0=0, eps=0.01, verb=False):
     """rgt (rgt.py:4): relative geological time, the time axis o1 + d1 i1
     painted along the slopes dip from trace i0."""

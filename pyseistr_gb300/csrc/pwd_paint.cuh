@@ -196,6 +196,19 @@ PWD_PAINT_HD void paint_side(const PaintParams& q, int side) {
   }
 }
 
+// Stacked sections of one size: thread g paints side g % 2 of section g / 2
+// (slopes and output at section * n1 n2, seed at section * n1, band arrays
+// in slices 2 section and 2 section + 1 of the workspace).
+PWD_PAINT_HD void paint_item(const PaintParams& q, long g) {
+  const long sec = g / 2, n12 = (long)q.n1 * q.n2;
+  PaintParams p = q;
+  p.dip = q.dip + sec * n12;
+  p.seed = q.seed + sec * q.n1;
+  p.out = q.out + sec * n12;
+  p.ws = q.ws + sec * 2 * slice_floats(q.n1, q.nw);
+  paint_side(p, (int)(g - 2 * sec));
+}
+
 // apfilt_init (paint_cfuns.c, the dip_cfuns.c:835-855 code), in double.
 inline void filter_constants(int nw, double* b) {
   const int nf = 2 * nw;

@@ -459,3 +459,19 @@ def fkdip(d, n1, n2, w, out=None, workspace=None):
     _lib.check(fn(_ptr(d), _ptr(out), n1, n2, float(w), _ptr(ws), ws.numel() * ws.element_size(),
                   _stream()), "fkdip")
     return out
+
+
+def paint2d_batch(dip, seed, n1, n2, nsec, order, i0, eps, out=None, workspace=None):
+    """pwd_paint2d_batch: nsec (n1, n2) sections stacked in the flat CUDA
+    float32 slopes `dip`, their seed traces stacked in `seed`."""
+    L = _lib.load()
+    n1, n2, nsec, order, i0 = int(n1), int(n2), int(nsec), int(order), int(i0)
+    dip = _as_flat(dip, nsec * n1 * n2, "dip")
+    seed = _as_flat(seed, nsec * n1, "seed")
+    ws = _workspace(L.pwd_paint2d_batch_workspace_size(n1, nsec, order), dip.device, workspace)
+    if out is None:
+        out = torch.empty(nsec * n1 * n2, dtype=torch.float32, device=dip.device)
+    _lib.check(L.pwd_paint2d_batch(_ptr(dip), _ptr(seed), _ptr(out), n1, n2, nsec, order, i0,
+                                   float(eps), _ptr(ws), ws.numel() * ws.element_size(),
+                                   _stream()), "paint2d_batch")
+    return out

@@ -127,6 +127,9 @@ def test_paint_entry_checks_arguments_on_the_host():
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 5, 0, 0.1, fake, need, None) == _lib.PWD_ENOTSUP
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, fake, need - 256, None) == _lib.PWD_EWORKSPACE
     assert lib.pwd_paint2d(fake, fake, fake, 100, 10, 2, 0, 0.1, ctypes.c_void_p(300), need, None) == _lib.PWD_EWORKSPACE
+    assert lib.pwd_paint2d_batch_workspace_size(100, 3, 2) >= 3 * (need - 256)
+    assert lib.pwd_paint2d_batch(fake, fake, fake, 100, 10, 0, 2, 0, 0.1, fake, need, None) == _lib.PWD_EINVAL
+    assert lib.pwd_paint2d_batch(fake, fake, fake, 100, 10, 3, 2, 0, 0.1, fake, need, None) == _lib.PWD_EWORKSPACE
 
 
 def test_sint_entry_checks_arguments_on_the_host():

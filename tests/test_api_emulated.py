@@ -30,6 +30,7 @@ def emulated(tmp_path_factory):
     coh.emu_coherence.argtypes = [P, P, P, I, I, I, I, F, I, F, P]
     coh.emu_coherence_batch.argtypes = [P, P, P, I, I, I, I, I, F, I, F, P]
     paint.emu_paint2d.argtypes = [P, P, P, I, I, I, I, F]
+    paint.emu_paint2d_batch.argtypes = [P, P, P, I, I, I, I, I, F]
     sint.emu_sint2d.argtypes = [P, P, P, P, I, I, I, I, I, F]
     return coh, paint, sint
 
@@ -86,7 +87,16 @@ def ps(emulated, monkeypatch):
 
     monkeypatch.setattr(D, "coherence", coherence)
     monkeypatch.setattr(D, "coherence_batch", coherence_batch)
+    def paint2d_batch(dip, seed, n1, n2, nsec, order, i0, eps, out=None, workspace=None):
+        assert dip.numel() == nsec * n1 * n2 and seed.numel() == nsec * n1
+        assert dip.is_contiguous() and seed.is_contiguous()
+        out = torch.empty(nsec * n1 * n2, dtype=torch.float32)
+        assert paint.emu_paint2d_batch(ptr(dip), ptr(seed), ptr(out), n1, n2, nsec, order, i0,
+                                       float(eps)) == 0
+        return out
+
     monkeypatch.setattr(D, "paint2d", paint2d)
+    monkeypatch.setattr(D, "paint2d_batch", paint2d_batch)
     import pyseistr_gb300
 
     return pyseistr_gb300
@@ -109,6 +119,7 @@ def test_painting_api(ps):
     for c in T.CASES:
         T.test_rgt_matches_oracle(ps, c)
     T.test_cpaint2d_refuses_bad_arguments(ps)
+    T.test_pwpaintc_batch_equals_one_call_per_section(ps)
     rng = np.random.default_rng(21)
     dip = rng.standard_normal((80, 30)).astype(np.float32)
     tr = rng.standard_normal(80).astype(np.float32)

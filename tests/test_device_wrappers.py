@@ -69,6 +69,8 @@ def test_paint_wrapper(fake):
     out = D.paint2d(_f(40 * 9), _f(40), 40, 9, 2, 3, 0.1)
     assert out.numel() == 40 * 9
     assert [c[0] for c in lib.calls] == ["pwd_paint2d_workspace_size", "pwd_paint2d"]
+    out = D.paint2d_batch(_f(3 * 40 * 9), _f(3 * 40), 40, 9, 3, 2, 3, 0.1)
+    assert out.numel() == 3 * 40 * 9 and lib.calls[-1][0] == "pwd_paint2d_batch"
 
 
 def test_sint_wrappers(fake):

@@ -79,3 +79,12 @@ def test_cpaint2d_refuses_bad_arguments(ps):
         ps.cpaint2d(dip, np.zeros(16, np.float32), 16, 5, 2, 0, 0.1, 0)  # dimension mismatch
     with pytest.raises(ValueError):
         ps.cpaint2d(dip, np.zeros(8, np.float32), 16, 4, 2, 0, 0.1, 0)   # short seed
+
+
+def test_pwpaintc_batch_equals_one_call_per_section(ps):
+    rng = np.random.default_rng(31)
+    dips = [(rng.standard_normal((120, 30)) * 1.2).astype(np.float32) for _ in range(6)]
+    seeds = [rng.standard_normal(120).astype(np.float32) for _ in range(6)]
+    got = ps.pwpaintc_batch(dips, seeds, order=2, i0=12, eps=0.1)
+    for p, s, g in zip(dips, seeds, got):
+        assert np.array_equal(g, ps.pwpaintc(p, s, order=2, i0=12, eps=0.1))

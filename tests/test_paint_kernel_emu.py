@@ -68,3 +68,26 @@ def test_emulated_kernel_matches_oracle(emu, case):
     want = O.paint2d(dip, tr, order=order, i0=i0, eps=eps)
     got = emu(dip, tr, order, i0, eps)
     assert np.array_equal(got, want)
+
+
+def test_emulated_stacked_sections_match_oracle(tmp_path):
+    """The batch decomposition over 4 stacked sections (threads run in
+    reverse order) gives each section's oracle painting."""
+    so = str(tmp_path / "libpaint_emu.so")
+    subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17", "-o", so,
+                    os.path.join(HERE, "emu", "paint_emu.cpp")], check=True)
+    lib = ctypes.CDLL(so)
+    P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    lib.emu_paint2d_batch.argtypes = [P, P, P, I, I, I, I, I, F]
+    rng = np.random.default_rng(30)
+    n1, n2, nsec, i0 = 60, 17, 4, 5
+    dips = [(rng.standard_normal((n1, n2)) * 1.2).astype(np.float32) for _ in range(nsec)]
+    seeds = [rng.standard_normal(n1).astype(np.float32) for _ in range(nsec)]
+    d = np.ascontiguousarray(np.concatenate([p.reshape(-1, order="F") for p in dips]))
+    s = np.ascontiguousarray(np.concatenate(seeds))
+    out = np.full(nsec * n1 * n2, 7.0, np.float32)
+    p = lambda a: a.ctypes.data_as(P)  # noqa: E731
+    assert lib.emu_paint2d_batch(p(d), p(s), p(out), n1, n2, nsec, 2, i0, 0.1) == 0
+    for k in range(nsec):
+        want = O.paint2d(dips[k], seeds[k], order=2, i0=i0, eps=0.1).reshape(-1, order="F")
+        assert np.array_equal(out[k * n1 * n2:(k + 1) * n1 * n2], want), k
