@@ -9,14 +9,20 @@
  *   - arrays are float32, column-major (Fortran order, time axis n1
  *     fastest: i = i1 + n1*(i2 + n2*i3)), exactly as the reference's Python
  *     wrappers flatten them before calling C;
- *   - every pointer is a device pointer the caller allocated; the library
- *     never allocates, its scratch is the caller's `workspace` of at least
- *     the size the matching *_workspace_size() returns (256-byte aligned);
+ *   - every pointer is a device pointer the caller allocated; the entry
+ *     points allocate no device memory, their scratch is the caller's
+ *     `workspace` of at least the size the matching *_workspace_size()
+ *     returns (256-byte aligned) -- except pwd_dip_static, whose scratch is
+ *     a fixed device array of the library (below);
  *   - work is enqueued on `stream` (NULL = legacy default stream) and the
  *     call returns without synchronising; results are ready once the
  *     stream has been synchronised;
- *   - the library holds no global state: calls on different streams with
- *     different workspaces may run concurrently;
+ *   - results depend only on the arguments: calls on different streams
+ *     with different workspaces may run concurrently.  The library's own
+ *     process-wide state is limited to pwd_dip_static's scratch array
+ *     (shared by every call of that entry) and the launch counter and
+ *     optional timing profiler of pwd_launch_count / pwd_profile_*
+ *     (bookkeeping guarded by a mutex, never read by the compute path);
  *   - errors are returned as pwd_status codes (the reference prints and
  *     returns NULL, which surfaces as SystemError).
  *
@@ -79,9 +85,14 @@ int pwd_dip(const float *data, const float *mask, float *dip_out, int n1, int n2
  * bytes (64 MiB), resident on every GPU that loads the library until the
  * process exits.  Sections whose pwd_dip_workspace_size() exceeds it are
  * rejected with PWD_EWORKSPACE before any work is enqueued.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress, with that device current) and caches it; make
- *     that first call before any stream capture on the device.
+ *   - Every call looks up the array's device address in the current
+ *     context (cudaGetSymbolAddress, with the device current; it allocates
+ *     nothing), so a cudaDeviceReset between calls is harmless.  The first
+ *     call in a context loads the library's device code there (lazy module
+ *     loading, the CUDA default), which commits the array's memory and can
+ *     stall like an allocation: make one warm-up call at start-up, before
+ *     any stream capture on the device (or set CUDA_MODULE_LOADING=EAGER,
+ *     which commits the array when the library is loaded).
  *   - Every call uses the same array; each call initialises the parts it
  *     reads, but calls that overlap on the GPU (different streams, or
  *     threads without ordering) race on it and give wrong results.

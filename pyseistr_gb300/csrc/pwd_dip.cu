@@ -14,7 +14,6 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
-#include <mutex>
 #include <vector>
 
 #include "pwd_batch.cuh"
@@ -1713,23 +1712,17 @@ namespace {
 constexpr size_t kDipStaticScratchBytes = size_t(64) << 20;  // 64 MiB per device
 static __device__ __align__(256) unsigned char g_dip_static_scratch[kDipStaticScratchBytes];
 
-constexpr int kMaxDevices = 128;
-std::mutex g_static_mu;
-void* g_static_addr[kMaxDevices];  // device address of the array, per device
-
-// Device address of the array on the current device.  The host-side name of
-// a __device__ array is not a device address, so it is looked up once per
-// device (with that device current) and cached.
+// Device address of the array in the current context.  The host-side name
+// of a __device__ array is not a device address, so it is looked up with the
+// device current.  The lookup allocates nothing and is repeated on every
+// call rather than cached: after a cudaDeviceReset the module is loaded
+// again in a new context, possibly at another address, and a cached pointer
+// would then be stale.  The first lookup in a context loads the module (lazy
+// loading, the CUDA default), which commits the array's memory there.
 int static_scratch(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PWD_ECUDA;
-  std::lock_guard<std::mutex> lk(g_static_mu);
-  if (!g_static_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_dip_static_scratch) != cudaSuccess || !p) return PWD_ECUDA;
-    g_static_addr[dev] = p;
-  }
-  *out = g_static_addr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_dip_static_scratch) != cudaSuccess || !p) return PWD_ECUDA;
+  *out = p;
   return PWD_OK;
 }
 

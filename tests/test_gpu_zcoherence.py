@@ -126,3 +126,22 @@ def test_cohc_batch_equals_one_call_per_window(ps):
     got = ps.cohc_batch(models, par, operator=1)
     for m, g in zip(models, got):
         assert np.array_equal(g, ps.cohc(m, par, operator=1))
+
+
+def test_cohc_batch_parabolic_equals_one_call_per_window(ps):
+    """The parabolic type (typ 2) in one launch: its hmax state is the same
+    for every window of one offset axis, so the batch equals per-window
+    calls, adjoint and forward."""
+    rng = np.random.default_rng(43)
+    nt, nh = 300, 48
+    v = np.linspace(-0.004, 0.004, 24).astype(np.float32)
+    h = (np.arange(nh, dtype=np.float32) - 20.0)
+    par = {"h": h, "v": v, "nt": nt, "dt": 0.0005, "typ": 2}
+    wins = [rng.standard_normal((nt, nh)).astype(np.float32) for _ in range(4)]
+    got = ps.cohc_batch(wins, par)
+    for w, g in zip(wins, got):
+        assert np.array_equal(g, ps.cohc(w, par))
+    models = [rng.standard_normal((nt, v.size)).astype(np.float32) for _ in range(3)]
+    got = ps.cohc_batch(models, par, operator=1)
+    for m, g in zip(models, got):
+        assert np.array_equal(g, ps.cohc(m, par, operator=1))

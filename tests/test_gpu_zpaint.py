@@ -88,3 +88,14 @@ def test_pwpaintc_batch_equals_one_call_per_section(ps):
     got = ps.pwpaintc_batch(dips, seeds, order=2, i0=12, eps=0.1)
     for p, s, g in zip(dips, seeds, got):
         assert np.array_equal(g, ps.pwpaintc(p, s, order=2, i0=12, eps=0.1))
+
+
+def test_pwpaintc_batch_many_sections_across_blocks(ps):
+    """48 sections: 96 threads (two per section), so the batch spans two
+    64-thread blocks and the section index g / 2 crosses a block boundary."""
+    rng = np.random.default_rng(32)
+    dips = [(rng.standard_normal((40, 12)) * 1.1).astype(np.float32) for _ in range(48)]
+    seeds = [rng.standard_normal(40).astype(np.float32) for _ in range(48)]
+    got = ps.pwpaintc_batch(dips, seeds, order=2, i0=5, eps=0.1)
+    for p, s, g in zip(dips, seeds, got):
+        assert np.array_equal(g, ps.pwpaintc(p, s, order=2, i0=5, eps=0.1))
