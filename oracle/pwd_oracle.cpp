@@ -43,6 +43,8 @@ enum {
   ORC_TRI_CHUNK = 4,     // triangle running sums as a 32-element chunked scan
   ORC_FILTER_FF = 8,     // filter products in float-float (pair) arithmetic
   ORC_TRI_EXACT = 16,    // triangle smoothing evaluated in double, rounded once
+  ORC_GPU_DOTS = 32,     // dot products and residual energies summed in the
+                         // GPU plain path's order (see gpuorder::dot)
 };
 
 // Float-float helpers (Dekker / Knuth error-free transformations) used by
@@ -187,6 +189,79 @@ static double dsdot(long n, const R* x, const R* y) {
   for (long i = 0; i < n; i++) dot += (double)x[i] * y[i];
   return dot;
 }
+
+// The GPU plain path's summation order for a dot product of float vectors
+// (pyseistr_gb300/csrc/pwd_dip.cu sec_sum_last, pwd_common.cuh ffacc and
+// block_sum): the section is cut into tiles of 8192 samples; in a tile,
+// thread j of 256 accumulates samples j, j+256, ... as a float-float pair
+// (error-free product and two-sum), converts it to double (h + l), and the
+// block sums its threads by the warp shuffle-down tree (offsets 16..1, then
+// the 8 warp sums by the same tree); the last tile then has thread j sum the
+// tile partials j, j+256, ... in double, in tile order, and reduces those
+// 256 values by the same block tree.  Model of the GPU only (to show which
+// of its results differ from the reference by summation order alone).
+namespace gpuorder {
+constexpr long kTile = 8192;
+constexpr int kThreads = 256;
+static inline void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+static double tree32(double* v) {  // lane 0 of a shuffle-down tree
+  for (int o = 16; o > 0; o >>= 1)
+    for (int l = 0; l < o; l++) v[l] = v[l] + v[l + o];
+  return v[0];
+}
+static double block_sum(const double* t) {  // 256 thread values
+  double w[32];
+  for (int k = 0; k < 32; k++) w[k] = 0.0;
+  for (int wi = 0; wi < kThreads / 32; wi++) {
+    double v[32];
+    for (int l = 0; l < 32; l++) v[l] = t[wi * 32 + l];
+    w[wi] = tree32(v);
+  }
+  return tree32(w);
+}
+static double dot(long n, const float* x, const float* y) {
+  const long ntile = (n + kTile - 1) / kTile;
+  std::vector<double> part(ntile);
+  double tv[kThreads];
+  for (long t = 0; t < ntile; t++) {
+    const long lo = t * kTile, hi = std::min(n, lo + kTile);
+    for (int j = 0; j < kThreads; j++) {
+      float h = 0.f, l = 0.f;
+      for (long i = lo + j; i < hi; i += kThreads) {
+        const float p = x[i] * y[i];
+        const float pe = std::fma(x[i], y[i], -p);
+        float sh, sl;
+        two_sum(h, p, sh, sl);
+        h = sh;
+        l = l + (sl + pe);
+      }
+      tv[j] = (double)h + (double)l;
+    }
+    part[t] = block_sum(tv);
+  }
+  for (int j = 0; j < kThreads; j++) {
+    double v = 0.0;
+    for (long i = j; i < ntile; i += kThreads) v += part[i];
+    tv[j] = v;
+  }
+  return block_sum(tv);
+}
+}  // namespace gpuorder
+
+static bool g_gpu_dots = false;  // ORC_GPU_DOTS for the float dip path
+
+template <class R>
+static double dsdot_dip(long n, const R* x, const R* y) {
+  if constexpr (sizeof(R) == 4) {
+    if (g_gpu_dots) return gpuorder::dot(n, (const float*)x, (const float*)y);
+  }
+  return dsdot(n, x, y);
+}
+
 template <class R>
 static void saxpy(long n, R a, const R* x, R* y) {
   for (long i = 0; i < n; i++) y[i] += a * x[i];
@@ -390,7 +465,7 @@ struct ConjGrad {
     for (long i = 0; i < n; i++) r[i] = -dat[i];
     for (long i = 0; i < n; i++) p[i] = 0;
     for (long i = 0; i < n; i++) x[i] = 0;
-    r0 = dsdot(n, r.data(), r.data());
+    r0 = dsdot_dip(n, r.data(), r.data());
     if (r0 == 0.) return 0;
     int iter;
     for (iter = 0; iter < niter; iter++) {
@@ -400,7 +475,7 @@ struct ConjGrad {
       S.lop(true, true, gp.data(), gx.data());              // gp += S' gx
       S.lop(false, false, gp.data(), gx.data());            // gx = S gp
       for (long i = 0; i < n; i++) gr[i] = (R)0 + gx[i] * w[i];  // gr = W gx
-      gn = dsdot(n, gp.data(), gp.data());
+      gn = dsdot_dip(n, gp.data(), gp.data());
       if (iter == 0) {
         g0 = gn;
         sp = gp; sx = gx; sr = gr;
@@ -413,8 +488,8 @@ struct ConjGrad {
         saxpy(n, a, sx.data(), gx.data()); std::swap(sx, gx);
         saxpy(n, a, sr.data(), gr.data()); std::swap(sr, gr);
       }
-      beta = dsdot(n, sr.data(), sr.data()) +
-             (double)eps * (dsdot(n, sp.data(), sp.data()) - dsdot(n, sx.data(), sx.data()));
+      beta = dsdot_dip(n, sr.data(), sr.data()) +
+             (double)eps * (dsdot_dip(n, sp.data(), sp.data()) - dsdot_dip(n, sx.data(), sx.data()));
       alpha = -gn / beta;
       R a = (R)alpha;
       saxpy(n, a, sp.data(), p);
@@ -439,7 +514,7 @@ static void divne(ConjGrad<R>& cg, TriangleN<R>& S, std::vector<R>& pbuf, R* num
       den[i] = (R)(den[i] * norm);
     }
   }
-  norm = dsdot(n, den, den);
+  norm = dsdot_dip(n, den, den);
   if (norm == 0.0) {
     for (long i = 0; i < n; i++) rat[i] = 0;
     return;
@@ -533,7 +608,7 @@ struct DipState {
   // Residual energy: float serial sum as the reference (:1653, :1681), or
   // the double sum the GPU path uses (ORC_USUM_DOUBLE).
   double energy(const R* v) const {
-    if (flags & ORC_USUM_DOUBLE) return dsdot(nd, v, v);
+    if (flags & (ORC_USUM_DOUBLE | ORC_GPU_DOTS)) return dsdot_dip(nd, v, v);
     R s = 0;
     for (long i = 0; i < nd; i++) s += v[i] * v[i];
     return (double)s;
@@ -588,6 +663,7 @@ static int dipc(const R* u, const R* maskdata, R* pout, int n1, int n2, int n3, 
   int n4 = (n3 == 1) ? 0 : 2;
   DipState<R> st;
   st.flags = flags;
+  g_gpu_dots = (flags & ORC_GPU_DOTS) != 0;
   st.init(n1, n2, n3, rect);
   std::vector<uint8_t> m0, m1;
   if (maskdata) mask32(order, n1, n2, n3, maskdata, m0, m1);

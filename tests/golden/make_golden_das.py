@@ -2,11 +2,13 @@
 dip2d niter=5, liter=20, order=2, rect=10,10,1).
 
 Runs the reference's own FP32 dipc (oracle/_ref/dipcfun, compiled from the
-reference sources by ``make -C oracle ref``) and the FP64 evaluation of the
-same algorithm (the oracle's double instantiation) on the seeded record of
-``workloads.das2d(seed=2023)``, and stores both slope fields at 32768 seeded
-random samples, plus each field's relative L2 distance to the FP64 field
-over the whole record.
+reference sources by ``make -C oracle ref``), the FP64 evaluation of the
+same algorithm (the oracle's double instantiation) and the oracle's FP32
+restatement with its dot products and residual energies summed in the GPU
+plain path's order (flag GPU_DOTS; everything else is the reference's
+float arithmetic) on the seeded record of ``workloads.das2d(seed=2023)``,
+and stores the three slope fields at 32768 seeded random samples, plus
+their relative L2 distances to each other over the whole record.
 
     make -C oracle ref && python tests/golden/make_golden_das.py
 
@@ -49,15 +51,25 @@ def main():
         os.close(nul)
     ref = ref.reshape(n1, n2, order="F")
     f64 = O.dip2d(d, 5, 20, 2, (10, 10, 1), precision="f64")
+    gpuo = O.dip2d(d, 5, 20, 2, (10, 10, 1), flags=O.GPU_DOTS)
     rng = np.random.default_rng(7)
     idx = np.sort(rng.choice(d.size, NSAMPLE, replace=False)).astype(np.int64)
     flat = lambda a: np.asarray(a).reshape(-1, order="F")  # noqa: E731
-    rel = float(np.linalg.norm(np.float64(flat(ref)) - flat(f64)) / np.linalg.norm(flat(f64)))
+    def rel_l2(a, b):
+        a, b = np.float64(flat(a)), np.float64(flat(b))
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    rel = rel_l2(ref, f64)
     np.savez_compressed(os.path.join(HERE, "golden_das_full.npz"), idx=idx,
                         ref32=flat(ref)[idx].astype(np.float32),
                         f64=flat(f64)[idx].astype(np.float64),
-                        ref32_rel_l2_vs_f64=np.float64(rel), shape=np.array([n1, n2]))
+                        gpuorder32=flat(gpuo)[idx].astype(np.float32),
+                        ref32_rel_l2_vs_f64=np.float64(rel),
+                        gpuorder32_rel_l2_vs_ref32=np.float64(rel_l2(gpuo, ref)),
+                        gpuorder32_rel_l2_vs_f64=np.float64(rel_l2(gpuo, f64)),
+                        shape=np.array([n1, n2]))
     print("reference FP32 vs FP64 relative L2 over the record:", rel)
+    print("GPU-order FP32 vs reference FP32:", rel_l2(gpuo, ref), " vs FP64:", rel_l2(gpuo, f64))
 
 
 if __name__ == "__main__":

@@ -65,3 +65,26 @@ def test_oracle_f64_close_to_reference(case):
     _, fn, p, a = case
     for got, want in zip(run_oracle(fn, p, a, "f64"), expected(a)):
         assert rel_l2(got, want) < 2e-3
+
+
+DIP_CASES = [c for c in C2 + C3 if c[1] == "dip"]
+
+
+@pytest.mark.parametrize("case", DIP_CASES, ids=[f"dip-{c[0]}" for c in DIP_CASES])
+def test_oracle_gpu_summation_order_on_golden_slopes(case):
+    """The oracle's model of the GPU plain path's summation order (GPU_DOTS:
+    tile, warp-tree and tile-order sums of float-float dot products) changes
+    no slope of the golden cases, on which the GPU plain path is bit-exact
+    with the reference; on the full DAS record it moves them 3.7e-2, which
+    the GPU matches bit for bit (tests/test_gpu_mixed.py)."""
+    _, fn, p, a = case
+    d = a["d"]
+    mask = a.get("mask")
+    if d.ndim == 2:
+        got = (O.dip2d(d, p["niter"], p["liter"], p["order"], p["rect"], mask=mask,
+                       flags=O.GPU_DOTS),)
+    else:
+        got = O.dip3d(d, p["niter"], p["liter"], p["order"], p["rect"], mask=mask,
+                      flags=O.GPU_DOTS)
+    for g, w in zip(got, expected(a)):
+        assert np.array_equal(g, w)
