@@ -228,20 +228,28 @@ __global__ void k_weighted_mean(SprayBufs bf, float* __restrict__ out, SprayB b,
   }
 }
 
-// mf centre row (sof_cfuns.c:1294-1332 via csomf2d :1623-1649).
+// mf centre row (sof_cfuns.c:1294-1332 via csomf2d :1623-1649).  WARP:
+// one warp per output sample (windows longer than kNetWin), else one thread.
+template <bool WARP>
 __global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ out, SprayB b,
                                int nmf) {
   const TileRange tr = tile_range(b, blockIdx.x);
   const SecDesc& s = b.secs[tr.sec];
   const int m = (nmf - 1) / 2, c = (b.np - 1) / 2;
-  float v[kMaxWin];
-  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const long first = WARP ? (threadIdx.x >> 5) : threadIdx.x;
+  const long step = WARP ? (blockDim.x >> 5) : blockDim.x;
+  for (long j = tr.lo + first; j < tr.hi; j += step) {
     const unsigned jj = (unsigned)j;
     const long trc = jj / (unsigned)s.n1;
     const int i1 = (int)(jj % (unsigned)s.n1);
-    const float* panel = u + s.u0 + trc * b.np * (long)s.n1 + i1;
-    for (int k = 0; k < nmf; k++) v[k] = panel[(long)clampi(c + k - m, 0, b.np - 1) * s.n1];
-    out[s.pout + j] = select_rank(v, nmf, m);
+    const float* col = u + s.u0 + trc * b.np * (long)s.n1 + i1;
+    if (WARP) {
+      const float r = select_warp(col, s.n1, c - m, b.np, nmf, m);
+      if (lane == 0) out[s.pout + j] = r;
+    } else {
+      out[s.pout + j] = select_thread(col, s.n1, c - m, b.np, nmf, m);
+    }
   }
 }
 
@@ -453,8 +461,12 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     if (option == 1) {
-      PWD_KERNEL(PWD_FAM_FILTER, st,
-                 k_median_tiles<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
+      if (nmf > kNetWin)
+        PWD_KERNEL(PWD_FAM_FILTER, st,
+                   k_median_tiles<true><<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
+      else
+        PWD_KERNEL(PWD_FAM_FILTER, st,
+                   k_median_tiles<false><<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf.u, out, b, nmf));
     } else {
       for (const SecDesc& s : secs) {  // svmf needs whole-panel means: per section
         int rc = launch_panel_median(w.bf.u + s.u0, out + s.pout, w.v2 + s.u0, w.avg + s.tr0,

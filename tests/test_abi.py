@@ -70,7 +70,7 @@ def test_calls_reject_bad_arguments_before_touching_the_gpu():
     assert lib.pwd_dip(fake, None, fake, 100, 10, 1, 5, 10, 2, rect, ctypes.c_void_p(300), 1 << 30, None) == _lib.PWD_EWORKSPACE
     assert lib.pwd_somean2d(fake, fake, fake, 3, 10, 1, 2, 2, 0, 0.01, fake, 1 << 20, None) == _lib.PWD_EINVAL
     assert lib.pwd_somf2d(fake, fake, fake, 50, 10, 1, 2, 5, 1, 2, 0.01, fake, 16, None) == _lib.PWD_EWORKSPACE
-    assert lib.pwd_somf3d(fake, fake, fake, fake, 50, 10, 10, 2, 2, 200, 1, 2, 0.01, fake, 1 << 30, None) == _lib.PWD_ENOTSUP
+    assert lib.pwd_somf3d(fake, fake, fake, fake, 50, 10, 10, 2, 2, 70000, 1, 2, 0.01, fake, 1 << 30, None) == _lib.PWD_ENOTSUP
     assert lib.pwd_soint3d(fake, None, fake, fake, fake, 8, 8, 8, 2, 1, 1, 5, 0, 1, 1, 0.0, fake, 1 << 30, None) == _lib.PWD_EINVAL
 
 
