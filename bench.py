@@ -200,6 +200,77 @@ class DeviceState:
         self.graph.data.copy_(self.d)
 
 
+def accuracy_vs_fp64(wl, st, seed):
+    """Relative L2 distance of the step's outputs to the FP64 evaluation of
+    the reference algorithm, from the committed fixtures (sampled indices):
+    the batched workload's slopes and mean per section
+    (tests/golden/golden_batch_f64.npz, 512 samples a section) and the DAS
+    record's slopes (tests/golden/golden_das_full.npz, 32768 samples).
+    None when no fixture matches the workload."""
+    def rel(a, b):
+        a, b = np.float64(a), np.float64(b)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    g = os.path.join(ROOT, "tests", "golden")
+    if wl.name == "batch2d" and seed == 2023 and len(st.shapes) == 512:
+        path = os.path.join(g, "golden_batch_f64.npz")
+        if not os.path.exists(path):
+            return None
+        z = np.load(path)
+        if [tuple(x) for x in z["shapes"]] != [tuple(x) for x in st.shapes]:
+            return None
+        dip, mean = st.p.cpu().numpy(), st.f.cpu().numpy()
+        k = j = 0
+        es, em = [], []
+        for shp, c in zip(st.shapes, z["count"]):
+            n = int(np.prod(shp))
+            ii = z["idx"][j:j + c]
+            es.append(rel(dip[k:k + n][ii], z["dip64"][j:j + c]))
+            em.append(rel(mean[k:k + n][ii], z["mean64"][j:j + c]))
+            k += n
+            j += c
+        return {"slopes_rel_l2_max_section": max(es),
+                "slopes_rel_l2_median_section": float(np.median(es)),
+                "sections_over_1e-4": int(sum(max(a, b) > 1e-4 for a, b in zip(es, em))),
+                "mean_rel_l2_max_section": max(em),
+                "reference_fp32_slopes_rel_l2_max_section":
+                float(np.max(z["ref32_rel_l2_vs_f64"])),
+                "reference_fp32_sections_over_1e-4":
+                int(np.sum(z["ref32_rel_l2_vs_f64"] > 1e-4)),
+                "samples": "512 per section (tests/golden/golden_batch_f64.npz)"}
+    if wl.name == "patches3d" and seed == 2023 and len(st.shapes) == 64:
+        path = os.path.join(g, "golden_patches_f64.npz")
+        if not os.path.exists(path):
+            return None
+        z = np.load(path)
+        if [tuple(x) for x in z["shapes"]] != [tuple(x) for x in st.shapes]:
+            return None
+        x = st.f.cpu().numpy()
+        k = j = 0
+        es = []
+        for shp, c in zip(st.shapes, z["count"]):
+            n = int(np.prod(shp))
+            es.append(rel(x[k:k + n][z["idx"][j:j + c]], z["interp64"][j:j + c]))
+            k += n
+            j += c
+        return {"masked_traces_rel_l2_max_patch": max(es),
+                "masked_traces_rel_l2_median_patch": float(np.median(es)),
+                "reference_fp32_masked_traces_rel_l2_max_patch":
+                float(np.max(z["ref32_rel_l2_vs_f64"])),
+                "fp64_chain_vs_true_data_median_patch": float(np.median(z["f64_rel_l2_vs_truth"])),
+                "samples": "2048 of the masked traces per patch "
+                           "(tests/golden/golden_patches_f64.npz)"}
+    if wl.name == "das2d" and seed == 2023:
+        z = np.load(os.path.join(g, "golden_das_full.npz"))
+        if tuple(z["shape"]) != tuple(st.shapes[0]):
+            return None
+        dip = st.p.cpu().numpy()
+        return {"slopes_rel_l2": rel(dip[z["idx"]], z["f64"]),
+                "reference_fp32_slopes_rel_l2": float(z["ref32_rel_l2_vs_f64"]),
+                "samples": "32768 (tests/golden/golden_das_full.npz)"}
+    return None
+
+
 def gpu_step(wl, st, mixed=False):
     D = st.D
     d = wl.dip
@@ -1152,6 +1223,8 @@ def main():
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dev)
     e2e = world * wl.samples() / e2e_s
 
+    # accuracy of the timed path's outputs (still in place from the last step)
+    acc = accuracy_vs_fp64(wl, dst, args.seed + rank) if rank == 0 else None
     plain = None
     if mixed:
         # the plain FP32 path on the same inputs: the mixed/plain ratio and
@@ -1199,6 +1272,8 @@ def main():
     }
     if plain is not None:
         line["plain_fp32"] = plain
+    if acc is not None:
+        line["accuracy_vs_fp64"] = acc
     if rank == 0 and fam_ms.get("spray", 0.0) > 0 and spray_flops_per_sample(wl):
         # the spray is bound by FP32 issue and latency, not by HBM: its
         # algorithmic flops per second against the measured FMA peak

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "pwd_batch.cuh"
@@ -29,6 +30,7 @@ struct DipScalars {
   double usum, usum2, r0, norm2;
   double gn, gnp, g0, alpha, step;
   int zero, cg_done, ls_done, ls_trials, cg_iters;
+  int stage_timeout;  // a bulk copy of the section's tile did not complete in time
   unsigned cnt[8];
 };
 
@@ -730,7 +732,19 @@ __global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
 // ---------------------------------------------------------------------------
 // Column strips of the axis-1 pass: kSmStrip columns (one thread each) by up
 // to kSmB2 rows; inputs staged kSmStages - 1 rows ahead.
-constexpr int kSmStrip = 64, kSmB2 = 128, kSmStages = 4;
+#ifndef PWD_SM_STAGES
+#define PWD_SM_STAGES 4
+#endif
+constexpr int kSmStrip = 64, kSmB2 = 128, kSmStages = PWD_SM_STAGES;
+
+// Strip height of the axis-1 passes: kSmB2 unless PWD_CG_STRIP in the
+// environment gives 32, 64, 128 or 256 (a tuning knob: shorter strips give
+// more tiles for small batches, longer ones fewer halo rows).
+inline int strip_rows() {
+  const char* e = getenv("PWD_CG_STRIP");
+  const int v = e ? atoi(e) : kSmB2;
+  return (v == 32 || v == 64 || v == 128 || v == 256) ? v : kSmB2;
+}
 
 enum { SM_IN_ARR = 0, SM_IN_CG1 = 1 };
 enum { SM_OUT_ARR = 0, SM_OUT_CG1 = 1, SM_OUT_CG2 = 2 };
@@ -747,6 +761,8 @@ struct SmParams {
   float *xn, *rn;
   const int4* c0map;  // axis-0 tiles: section, first trace, first sample, lines << 16 | length
   int c0buf;          // floats per axis-0 staging buffer
+  int tma;            // axis-0 tiles staged by bulk copies (else 4-byte cp.async)
+  int b2;             // rows of an axis-1 strip
 };
 
 __device__ __forceinline__ bool sm_selected(int sel, const SecDesc& s) {
@@ -985,6 +1001,74 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
   const int w = len + 2 * h0;  // staged samples per line
   const int nbuf = q.c0buf;
   const bool stepped = IN == SM_IN_CG1 && q.iter > 0;
+  if (q.tma) {
+    // The tile's samples of each input array are one contiguous range of
+    // the array (whole traces, or one trace's segment and its halo): the
+    // 16-byte-aligned range that covers it is copied to a staging buffer by
+    // one bulk copy per array, then the lines (with mirrored margins) are
+    // formed from the staging buffers.  Buffers: the lines (nbuf), then
+    // one staging buffer per array.
+    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ int s_ok;
+    const int p0 = max(0, o1 - h0), p1 = min(n1, o1 + len + h0);
+    const long g0 = so + p0, g1 = so + (long)(nl - 1) * n1 + p1;
+    const long ga = g0 & ~3L, gb = (g1 + 3) & ~3L;
+    const unsigned bytes = (unsigned)((gb - ga) * 4);
+    constexpr int NA = IN == SM_IN_ARR ? 1 : 5;
+    const int narr = IN == SM_IN_ARR ? 1 : (stepped ? 5 : 3);
+    float* stg = buf + nbuf;
+    if (threadIdx.x == 0) {
+      mbar_init(&s_bar, 1);
+      mbar_fence_init();
+      mbar_arrive_expect_tx(&s_bar, bytes * narr);
+      const float* src[NA];
+      if (IN == SM_IN_ARR) {
+        src[0] = q.in;
+      } else {
+        src[0] = q.xo;
+        src[1 % NA] = q.ro;
+        src[2 % NA] = a.u1;
+        src[3 % NA] = a.sx;
+        src[4 % NA] = a.sr;
+      }
+      for (int ar = 0; ar < narr; ar++) bulk_copy_g2s(stg + ar * nbuf, src[ar] + ga, bytes, &s_bar);
+      // a copy that does not complete in time marks the section and the
+      // tile is skipped (after a second bounded wait for the copies)
+      // (a tile's copies take microseconds; the limits are 50 ms)
+      int ok = mbar_wait_bounded(&s_bar, 0, 50000000ull);
+      if (!ok) {
+        atomicExch(&S->stage_timeout, 1);
+        mbar_wait_bounded(&s_bar, 0, 50000000ull);
+      }
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const float st = stepped ? __double2float_rn(S->step) : 0.f;
+    for (int k = 0; k < nl; k++) {
+      float* bl = buf + k * stride;
+      for (int c = threadIdx.x; c < w; c += NT) {  // slot c: sample o1 - h0 + c
+        const int pos = o1 - h0 + c;
+        const long i = so + k * n1 + ((unsigned)pos < (unsigned)n1 ? pos : mirror_idx(pos, n1)) - ga;
+        if (IN == SM_IN_ARR) {
+          bl[c] = stg[i];
+        } else {
+          float xi = stg[i], ri = stg[nbuf + i];
+          if (stepped) {
+            xi = __fmaf_rn(st, stg[3 * nbuf + i], xi);
+            ri = __fmaf_rn(st, stg[4 * nbuf + i], ri);
+          }
+          bl[c] = __fmaf_rn(ri, stg[2 * nbuf + i], -xi);  // gx = -eps x + W' r
+          if (c >= h0 && c < h0 + len) {                    // this tile's own sample
+            const long e = so + k * n1 + o1 - h0 + c;
+            q.xn[e] = xi;
+            q.rn[e] = ri;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  } else {
   for (int k = 0; k < nl; k++) {
     float* bl = buf + k * stride;
     for (int c = threadIdx.x; c < w; c += NT) {  // slot c: sample o1 - h0 + c
@@ -1025,6 +1109,7 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
       }
     }
     __syncthreads();
+  }
   }
   const int gpl = (len + OUTS - 1) / OUTS;  // output groups per line
   if ((int)threadIdx.x >= nl * gpl) return;
@@ -1098,11 +1183,12 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
   if (S->cg_done) return;
   const int tile0 = AX == 1 ? s.ftile0 : s.gtile0, ntile = AX == 1 ? s.nftile : s.ngtile;
   const int n1 = AX == 1 ? s.n1 : s.n1 * s.n2, n2 = AX == 1 ? s.n2 : s.n3;
-  const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + kSmB2 - 1) / kSmB2;
+  const int b2 = q.b2;
+  const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + b2 - 1) / b2;
   const int lt = t - tile0;
   const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
-  const int o2 = t2 * kSmB2;
-  const int rows = min(kSmB2, n2 - o2);
+  const int o2 = t2 * b2;
+  const int rows = min(b2, n2 - o2);
   const long so = s.off + (long)i3 * n1 * n2;
   const int j = threadIdx.x;
   const int g1 = t1 * kSmStrip + j;
@@ -1235,6 +1321,8 @@ struct DipLayout {
   int nftiles;  // column-strip tiles (mixed mode)
   int nctiles;  // row-segment tiles (mixed mode)
   int ngtiles;  // axis-2 strip tiles of cubes (mixed mode)
+  int b2;       // rows of an axis-1 / axis-2 strip (mixed mode)
+  long ftiles_max;  // strip tiles with the shortest strips (sizes the partial sums)
   long scr_total;
   long nlines[3];
   bool any3d, any2d;
@@ -1245,6 +1333,7 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
   DipLayout L{};
   long scr[3] = {0, 0, 0}, lines[3] = {0, 0, 0};
   int tiles = 0;
+  const int b2 = L.b2 = strip_rows();
   for (auto& s : secs) {
     s.n = (long)s.n1 * s.n2 * s.n3;
     L.ntot = std::max(L.ntot, s.off + s.n);
@@ -1254,10 +1343,13 @@ DipLayout layout(std::vector<SecDesc>& secs, const int rect[3]) {
     s.ntile = (int)((s.n + kTile - 1) / kTile);
     tiles += s.ntile;
     s.ftile0 = L.nftiles;
-    s.nftile = ((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + kSmB2 - 1) / kSmB2) * s.n3;
+    s.nftile = ((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + b2 - 1) / b2) * s.n3;
     L.nftiles += s.nftile;
+    L.ftiles_max += (long)((s.n1 + kSmStrip - 1) / kSmStrip) * ((s.n2 + 31) / 32) * s.n3 +
+                    (s.n3 > 1 ? (long)((s.n1 * s.n2 + kSmStrip - 1) / kSmStrip) * ((s.n3 + 31) / 32)
+                              : 0);
     s.gtile0 = L.ngtiles;
-    s.ngtile = s.n3 > 1 ? ((s.n1 * s.n2 + kSmStrip - 1) / kSmStrip) * ((s.n3 + kSmB2 - 1) / kSmB2)
+    s.ngtile = s.n3 > 1 ? ((s.n1 * s.n2 + kSmStrip - 1) / kSmStrip) * ((s.n3 + b2 - 1) / b2)
                         : 0;
     L.ngtiles += s.ngtile;
     s.ctile0 = L.nctiles;
@@ -1317,7 +1409,7 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.tile_sec = cv.take<int>(L.ntiles);
   w.S = cv.take<DipScalars>(nsec);
   w.partials = cv.take<double>(
-      (size_t)std::max(L.ntiles, mixed ? std::max(L.nftiles, L.ngtiles) : 0) * 3);
+      (size_t)std::max((long)L.ntiles, mixed ? L.ftiles_max : 0L) * 3);
   *total = cv.size();
   return w;
 }
@@ -1409,8 +1501,13 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const unsigned gt = (unsigned)L.ntiles, gf = (unsigned)L.nftiles;
   const unsigned gc = (unsigned)L.nctiles, gg = (unsigned)L.ngtiles;
   q.c0map = a.c0map;
+  q.b2 = L.b2;
   q.c0buf = conv0_buffer(q.nb0 - 1);
-  const size_t smem0 = sizeof(float) * q.c0buf, smem0cg = 5 * smem0;
+  // axis-0 staging by bulk copies unless PWD_CONV0_TMA=0 in the environment
+  const char* tma_env = getenv("PWD_CONV0_TMA");
+  q.tma = !(tma_env && atoi(tma_env) == 0);
+  const size_t smem0 = sizeof(float) * q.c0buf * (q.tma ? 2 : 1),
+               smem0cg = sizeof(float) * q.c0buf * (q.tma ? 6 : 5);
   const bool ring1 = !(q.nb1 == 10 || q.nb1 == 5);
   const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));

@@ -470,7 +470,10 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
 // samples ahead by cp.async into the thread's ring in shared memory: ring
 // element e of slot q at ring[(q*apply_elems(NW) + e)*rs] (rs = threads of the
 // block, so consecutive threads hit consecutive banks).
-constexpr int kApplyStages = 4;
+#ifndef PWD_APPLY_STAGES
+#define PWD_APPLY_STAGES 4
+#endif
+constexpr int kApplyStages = PWD_APPLY_STAGES;
 __host__ __device__ constexpr int apply_elems(int nw) { return 4 * nw + 3; }  // NA + NB + 2
 
 template <int NW, bool RHS2>

@@ -8,6 +8,7 @@
 // trace of ones (the normalisation spray of pwsmooth_set) and the data are
 // predicted through the same factorisation in the same chain.
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "pwd_batch.cuh"
@@ -414,7 +415,13 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   const int nsec = (int)secs.size();
   const ApCoef c = make_apcoef(NW);
   SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, L.ntp, ns, 2 * ns + 1, eps * eps, eps * eps};
-  const int bs = 64;
+  // tuning knobs (environment): threads per block of the chain kernels
+  // (PWD_SPRAY_BLOCK 32 or 64) and the factor kernel's form (PWD_SPRAY_SPLIT
+  // 1: a thread per filter orientation, 0: per trace, unset: by the wave count)
+  const char* eb = getenv("PWD_SPRAY_BLOCK");
+  const int bs = (eb && atoi(eb) == 32) ? 32 : 64;
+  const char* esp = getenv("PWD_SPRAY_SPLIT");
+  const int split = esp ? (atoi(esp) != 0) : -1;
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_tile_map<<<(unsigned)((L.ntiles + 255) / 256), 256, 0, st>>>(w.secs, nsec, L.ntiles, w.tile_sec));
   PWD_KERNEL(PWD_FAM_OTHER, st,
@@ -434,7 +441,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spray2_factor<NW, true>, bs, 0);
-  if (2 * L.ntp <= (long)sms * per * bs) {
+  if (split == 1 || (split < 0 && 2 * L.ntp <= (long)sms * per * bs)) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                (k_spray2_factor<NW, true><<<(unsigned)((2 * L.ntp + bs - 1) / bs), bs, 0, st>>>(
                    dip, w.bf, b, c)));

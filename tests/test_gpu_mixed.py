@@ -181,10 +181,13 @@ def test_das_full_record_mixed_vs_fp64_and_plain_vs_reference(D):
     reference's FP32 slopes are 8.8e-2 from FP64 over the record: the serial
     running sums of the triangle smoothing lose precision along the
     5000-trace lines, and the CG amplifies any rounding difference.  The
-    plain path performs the same float operations but sums its FP64 dot
-    products in another order, so on this record it lands a few 1e-2 from
-    the reference's FP32 slopes, as far from FP64 as they are.  The mixed
-    slopes are within 1e-5 of FP64."""
+    plain path performs the reference's float operations but sums its FP64
+    dot products (and the line search's residual energies) in another order.
+    The fixture holds the oracle's FP32 restatement with exactly that
+    summation order (flag GPU_DOTS) and everything else the reference's:
+    the plain GPU slopes equal it bit for bit, so summation order is the
+    whole difference from the reference's slopes (3.7e-2 over the record).
+    The mixed slopes are within 1e-5 of FP64."""
     import workloads
 
     g = _das_golden()
@@ -196,8 +199,10 @@ def test_das_full_record_mixed_vs_fp64_and_plain_vs_reference(D):
     ref_err = float(g["ref32_rel_l2_vs_f64"])
     assert ref_err > 1e-2
     assert rel_l2(mixed, g["f64"]) <= 1e-5
-    assert rel_l2(plain, g["f64"]) <= 2 * ref_err
-    assert rel_l2(plain, g["ref32"]) <= 2 * ref_err
+    assert np.array_equal(plain, g["gpuorder32"])
+    # the summation order's effect on the record, measured by the oracle
+    gap = float(g["gpuorder32_rel_l2_vs_ref32"])
+    assert rel_l2(plain, g["ref32"]) <= 1.1 * gap + 1e-3
 
 
 @pytest.mark.parametrize("mixed", [False, True])
@@ -239,3 +244,79 @@ def test_packed_host_api_equals_list_api(D):
             assert np.array_equal(p[k:k + s.size].numpy().reshape(s.shape, order="F"), a)
             assert np.array_equal(f[k:k + s.size].numpy().reshape(s.shape, order="F"), b)
             k += s.size
+
+
+def test_batched_workload_every_section_vs_fp64(D):
+    """The benchmark's batched workload at full size (512 sections of
+    workloads.batch2d(seed=2023), dip2d(5, 10, rect 10,10,1) then
+    somean2d(ns 6)) against the FP64 fixture made by
+    tests/golden/make_golden_batch.py (at its 512 samples per section).  The
+    mixed slopes and the mean filtered with them are within 1e-4 relative L2
+    of the FP64 evaluation on every section but at most one; that one is an
+    ill-conditioned section on which the reference's own FP32 is 2.5e-3 from
+    FP64: it is held to 3e-4 and to a tenth of the reference's error (the
+    float CG's rounding grows about tenfold per iteration there, so any
+    float arithmetic lands 1e-5 .. 3e-4 from FP64).  The plain path, the
+    reference's float arithmetic, exceeds 1e-4 on about sixty sections."""
+    import os
+
+    import torch
+    import workloads
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "golden_batch_f64.npz")
+    g = np.load(path)
+    secs = workloads.batch2d(seed=2023, count=512)
+    shapes = [s.shape for s in secs]
+    assert [tuple(x) for x in g["shapes"]] == shapes
+    flat = torch.from_numpy(np.concatenate([s.reshape(-1, order="F") for s in secs])).cuda()
+    dip = D.dip_batch(flat, shapes, 5, 10, 2, (10, 10, 1), mixed=True)
+    mean = D.sofilter2d_batch(flat, dip, shapes, 6, 2, 0.01)
+    dip, mean = dip.cpu().numpy(), mean.cpu().numpy()
+    cnt, idx, ref32 = g["count"], g["idx"], g["ref32_rel_l2_vs_f64"]
+    k = j = 0
+    over = []
+    for q, (s, c) in enumerate(zip(secs, cnt)):
+        ii = idx[j:j + c]
+        es = rel_l2(dip[k:k + s.size][ii], g["dip64"][j:j + c])
+        em = rel_l2(mean[k:k + s.size][ii], g["mean64"][j:j + c])
+        if max(es, em) > MIXED_TOL:
+            over.append((q, es, em, float(ref32[q])))
+        k += s.size
+        j += c
+    assert len(over) <= 1, over
+    for q, es, em, r in over:
+        assert max(es, em) <= 3e-4 and es <= r / 10, (q, es, em, r)
+
+
+def test_patches3d_masked_traces_vs_fp64(D):
+    """The batched 3-D interpolation workload at full size (64 patches of
+    workloads.patches3d(seed=2023): mixed dip3d(5, 10, rect 5,5,5) on each
+    patch, then soint3d(order 2, niter 20) of the patch with half its traces
+    masked): the reconstruction on the masked traces against the FP64
+    evaluation of the same chain (tests/golden/make_golden_patches.py, 2048
+    samples of the masked traces per patch), within 1e-4 relative L2 on
+    every patch."""
+    import os
+
+    import torch
+    import workloads
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "golden_patches_f64.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden_patches_f64.npz not generated")
+    g = np.load(path)
+    pairs = workloads.patches3d(seed=2023, count=64)
+    shapes = [d.shape for d, _ in pairs]
+    assert [tuple(x) for x in g["shapes"]] == shapes
+    full = torch.from_numpy(np.concatenate([d.reshape(-1, order="F") for d, _ in pairs])).cuda()
+    mask = torch.from_numpy(np.concatenate([m.reshape(-1, order="F") for _, m in pairs])).cuda()
+    p = D.dip_batch(full, shapes, 5, 10, 2, (5, 5, 5), mixed=True)
+    x = D.soint3d_batch(full * mask, mask, p, shapes, order=2, niter=20).cpu().numpy()
+    k = j = 0
+    errs = []
+    for (d, _), c in zip(pairs, g["count"]):
+        ii = g["idx"][j:j + c]
+        errs.append(rel_l2(x[k:k + d.size][ii], g["interp64"][j:j + c]))
+        k += d.size
+        j += c
+    assert max(errs) <= MIXED_TOL, (max(errs), int(np.argmax(errs)))
