@@ -253,6 +253,19 @@ static double dot(long n, const float* x, const float* y) {
 }  // namespace gpuorder
 
 static bool g_gpu_dots = false;  // ORC_GPU_DOTS for the float dip path
+static int g_store16 = 0;        // spray factor-store precision model (0 off, 1 FP16, 2 BF16)
+static int g_cg_store16 = 0;     // CG direction-store precision model (same codes)
+static float round16(float x) {
+  if (g_store16 == 1) return (float)(_Float16)x;
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  float y;
+  std::memcpy(&y, &u, 4);
+  return y;
+}
 
 template <class R>
 static double dsdot_dip(long n, const R* x, const R* y) {
@@ -487,6 +500,13 @@ struct ConjGrad {
         saxpy(n, a, sp.data(), gp.data()); std::swap(sp, gp);
         saxpy(n, a, sx.data(), gx.data()); std::swap(sx, gx);
         saxpy(n, a, sr.data(), gr.data()); std::swap(sr, gr);
+      }
+      if (g_cg_store16) {  // precision model: the conjugate directions stored in 16 bits
+        const int keep = g_store16;
+        g_store16 = g_cg_store16;
+        for (auto* v : {&sp, &sx, &sr})
+          for (auto& e : *v) e = (R)round16((float)e);
+        g_store16 = keep;
       }
       beta = dsdot_dip(n, sr.data(), sr.data()) +
              (double)eps * (dsdot_dip(n, sp.data(), sp.data()) - dsdot_dip(n, sx.data(), sx.data()));
@@ -818,6 +838,17 @@ struct Predict {
     w1.init(n1, nw);
     if (two) w2.init(n1, nw);
   }
+  // Precision model of a factor store kept in 16 bits (g_store16: 1 FP16,
+  // 2 BF16): the taps the filter application reads and the LDL' factors the
+  // solves read rounded to 16 bits; the band itself is formed from the
+  // exact taps, as a factor kernel would.
+  void store16() {
+    for (auto& col : w1.a)
+      for (auto& v : col) v = (R)round16((float)v);
+    for (auto& v : slv.d) v = (R)round16((float)v);
+    for (auto& col : slv.o)
+      for (auto& v : col) v = (R)round16((float)v);
+  }
   // regularization :603-620
   void regularization() {
     for (int i1 = 0; i1 < n1; i1++) {
@@ -835,6 +866,7 @@ struct Predict {
     regularization();
     w1.define(forw, pp, diag.data(), offd);
     slv.define(diag.data(), offd);
+    if (g_store16) store16();
     if (adj) slv.solve(trace);
     R t0 = trace[0], t1 = trace[1], t2 = trace[n1 - 2], t3 = trace[n1 - 1];
     w1.set(adj, trace, trace, diag.data());
@@ -1906,6 +1938,8 @@ inline int bandpass(const float* in, float* out, int n1, long ntr, float d1, flo
 }  // namespace orc
 
 extern "C" {
+void orc_set_store16(int mode) { orc::g_store16 = mode; }
+void orc_set_cg_store16(int mode) { orc::g_cg_store16 = mode; }
 
 int orc_dip_f32(const float* u, const float* mask, float* p, int n1, int n2, int n3, int niter,
                 int liter, int order, int r1, int r2, int r3, int flags, int* ls) {
