@@ -1089,6 +1089,44 @@ def run_das_fkcoh(args):
     return 0
 
 
+# The other configurations, each measured by its own bench.py run (a fresh
+# process: its own device state, workspaces and clock sampler) and reported
+# inside the headline line; a leg that fails reports its error instead.
+LEGS = [("das2d", "configuration 3"), ("patches3d", "configuration 5"),
+        ("plain2d", "configuration 1"), ("plain3d", "configuration 2"),
+        ("das_fkcoh", "DAS chain: fkdip + cohc")]
+LEG_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
+            "gpu_launches", "clocks", "roofline", "accuracy_vs_fp64", "plain_fp32", "spray_fp32",
+            "cpu_baseline")
+
+
+def run_legs(args):
+    legs = {}
+    for name, what in LEGS:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name, "--steps",
+               str(min(args.steps, 5)), "--warmup", "3", "--cpu-budget", "5", "--no-legs",
+               "--seed", str(args.seed)]
+        if args.no_cpu_baseline:
+            cmd.append("--no-cpu-baseline")
+        if args.no_tune:
+            cmd.append("--no-tune")
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            out = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not out:
+                legs[name] = {"what": what, "error": (r.stderr or r.stdout)[-400:]}
+                continue
+            d = json.loads(out[-1])
+            leg = {k: d[k] for k in LEG_KEYS if k in d}
+            leg["what"] = what
+            leg["wall_s"] = round(time.perf_counter() - t0, 1)
+            legs[name] = leg
+        except (subprocess.SubprocessError, ValueError) as e:
+            legs[name] = {"what": what, "error": str(e)[-400:]}
+    return legs
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1111,6 +1149,10 @@ def main():
                     help="records per step of the patch2d and bandpass2d workloads (default "
                          "16); smaller counts for profiler captures")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (library defaults for the launch-shape knobs)")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="batch2d only: skip the other configurations' legs of the line")
     ap.add_argument("--cpu-budget", type=float, default=15.0,
                     help="seconds of single-core CPU work for the cpu_baseline sample")
     args = ap.parse_args()
@@ -1145,6 +1187,23 @@ def main():
             torch.distributed.barrier()
 
     mixed = args.precision == "mixed"
+    tuning = None
+    if mixed and not args.no_tune and wl.name in ("batch2d", "das2d"):
+        # the library's launch-shape knobs tuned on this workload (direct
+        # launches: the knobs are read when the launch sequence is enqueued,
+        # so before the graph capture), outside any timed region
+        from pyseistr_gb300 import tune
+
+        cache = os.environ.get("PWD_TUNE_CACHE") or os.path.join(
+            os.path.expanduser("~"), ".cache", "pyseistr_gb300", "tune.json")
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        timer = tune.gpu_step_timer(lambda: gpu_step(wl, dst, mixed), reps=2, warmup=1)
+        t0 = time.perf_counter()
+        choice, key = tune.autotune(dst.shapes, wl.filt["ns"], wl.dip["order"], wl.dip["rect"],
+                                    True, timer, cache_path=cache)
+        tune.apply(choice)
+        tuning = {"class": key, "choice": choice,
+                  "tuning_s": round(time.perf_counter() - t0, 1)}
     if not args.no_graph:
         dst.capture(wl, mixed)
     for _ in range(max(3, args.warmup)):
@@ -1274,6 +1333,12 @@ def main():
         line["plain_fp32"] = plain
     if acc is not None:
         line["accuracy_vs_fp64"] = acc
+    if tuning is not None:
+        line["config"]["tuning"] = tuning
+    if (rank == 0 and world == 1 and args.workload == "batch2d" and not args.no_legs
+            and args.impl == "gb300"):
+        torch.cuda.synchronize()
+        line["legs"] = run_legs(args)
     if rank == 0 and fam_ms.get("spray", 0.0) > 0 and spray_flops_per_sample(wl):
         # the spray is bound by FP32 issue and latency, not by HBM: its
         # algorithmic flops per second against the measured FMA peak
