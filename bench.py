@@ -406,18 +406,20 @@ def family_bytes(wl, launches, mixed=False):
             trials = max(0, cnt - 1 - niter)
             bps = (12.0 + 24.0 * niter + 16.0 * trials) / max(1, 1 + niter + trials)
         elif fam == "cg" and mixed and d["rect"][2] > 1 and wl.name in ("plain3d", "patches3d"):
-            # cubes, per CG iteration: axis 0 with the step and gradient 32
-            # (24 first), axis 1 8, axis 2 with gp 20 (12 first), axis 0 8,
-            # axis 1 8, axis 2 with the update 36 (24 first); scale 28 and
-            # final step 12 per Gauss-Newton iteration
-            per_outer = 28 + (24 + 8 + 12 + 8 + 8 + 24) + (liter - 1) * 112 + 12
+            # cubes, per CG iteration: axis 0 with the step and gradient 24
+            # (read x, W, num, sx; write x, t; 20 first), axis 1 8, axis 2
+            # with gp 20 (12 first), axis 0 8, axis 1 8, axis 2 with the
+            # update 28 (read t, gp, W, sp, sx; write sp, sx; 20 first);
+            # scale 28 and final step 12 per Gauss-Newton iteration
+            per_outer = 28 + (20 + 8 + 12 + 8 + 8 + 20) + (liter - 1) * 96 + 12
             bps = per_outer / (2.0 + 6.0 * liter)
         elif fam == "cg" and mixed:
-            # per CG iteration: axis 0 with the step and gradient 32 (24
-            # first), axis 1 with gp 20 (12 first), axis 0 of gp 8, axis 1
-            # with the conjugate update 36 (24 first); scale 28 and final
-            # step 12 per Gauss-Newton iteration
-            per_outer = 28 + (24 + 12 + 8 + 24) + (liter - 1) * 96 + 12
+            # per CG iteration: axis 0 with the step and gradient 24 (read
+            # x, W, num, sx; write x, t; 20 first), axis 1 with gp 20 (12
+            # first), axis 0 of gp 8, axis 1 with the conjugate update 28
+            # (read t, gp, W, sp, sx; write sp, sx; 20 first); scale 28 and
+            # final step 12 per Gauss-Newton iteration
+            per_outer = 28 + (20 + 12 + 8 + 20) + (liter - 1) * 80 + 12
             bps = per_outer / (2.0 + 4.0 * liter)
         elif fam == "cg":
             # per Gauss-Newton iteration: scale 28, first gradient 16, later

@@ -28,6 +28,7 @@ TRI_CHUNK = 4
 FILTER_FF = 8
 TRI_EXACT = 16  # triangle smoothing in double, rounded once per output
 GPU_DOTS = 32  # dot products and residual energies in the GPU plain path's summation order
+TRUE_RESIDUAL = 512  # precision model: CG residual formed as W x - dat each iteration
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int

@@ -45,6 +45,8 @@ enum {
   ORC_TRI_EXACT = 16,    // triangle smoothing evaluated in double, rounded once
   ORC_GPU_DOTS = 32,     // dot products and residual energies summed in the
                          // GPU plain path's order (see gpuorder::dot)
+  ORC_TRUE_RESIDUAL = 512,  // CG residual formed as W x - dat each iteration
+                            // and sr as W sx, instead of their recurrences
 };
 
 // Float-float helpers (Dekker / Knuth error-free transformations) used by
@@ -472,6 +474,7 @@ struct ConjGrad {
     r.assign(n, 0); sp.assign(n, 0); gp.assign(n, 0); sx.assign(n, 0);
     gx.assign(n, 0); sr.assign(n, 0); gr.assign(n, 0);
   }
+  bool true_residual = false;  // ORC_TRUE_RESIDUAL precision model
   // returns the number of iterations run (for diagnostics)
   int solve(TriangleN<R>& S, const R* w, R* p, R* x, const R* dat, int niter) {
     double gn, gnp = 0., alpha, beta, g0 = 0., dg = 0., r0;
@@ -483,6 +486,9 @@ struct ConjGrad {
     int iter;
     for (iter = 0; iter < niter; iter++) {
       for (long i = 0; i < n; i++) gp[i] = eps * p[i];
+      if (true_residual) {  // precision model: r = W x - dat formed afresh, one rounding
+        for (long i = 0; i < n; i++) r[i] = (R)((double)w[i] * (double)x[i] - (double)dat[i]);
+      }
       for (long i = 0; i < n; i++) gx[i] = -eps * x[i];
       for (long i = 0; i < n; i++) gx[i] += r[i] * w[i];  // W' r (add)
       S.lop(true, true, gp.data(), gx.data());              // gp += S' gx
@@ -508,6 +514,8 @@ struct ConjGrad {
           for (auto& e : *v) e = (R)round16((float)e);
         g_store16 = keep;
       }
+      if (true_residual)  // sr = W sx (its value in exact arithmetic)
+        for (long i = 0; i < n; i++) sr[i] = w[i] * sx[i];
       beta = dsdot_dip(n, sr.data(), sr.data()) +
              (double)eps * (dsdot_dip(n, sp.data(), sp.data()) - dsdot_dip(n, sx.data(), sx.data()));
       alpha = -gn / beta;
@@ -644,6 +652,7 @@ struct DipState {
       tri.tr[i].chunked = (flags & ORC_TRI_CHUNK) != 0;
       tri.tr[i].exact = (flags & ORC_TRI_EXACT) != 0;
     }
+    cg.true_residual = (flags & ORC_TRUE_RESIDUAL) != 0;
     allpass(dip, false, af, nw, n1, n2, n3, u, p, u2.data());
     for (int iter = 0; iter < niter; iter++) {
       allpass(dip, true, af, nw, n1, n2, n3, u, p, u1.data());

@@ -47,7 +47,7 @@ struct DipArrays {
   float* p;        // slopes (output)
   const uint8_t* mask;
   float *u1, *u2, *dp, *p0, *pcg, *r, *gp, *tmp, *sp, *sx, *sr, *tri;
-  float *x2, *r2;  // mixed mode: second buffers of x (dp) and r
+  float *x2, *r2;  // mixed mode: second buffer of x (dp); r2 unused
   float* t2;       // mixed mode: axes 0-1 result of cubes
   int4* c0map;     // mixed mode: tile table of the axis-0 pass
 };
@@ -726,9 +726,13 @@ __global__ void k_skip_2d(const SecDesc* secs, int nsec, DipScalars* S) {
 // one thread per column streaming down the rows with the CG output
 // operation and its dot products (axis 2 of cubes in a third, elementwise
 // pass).  One CG iteration of a 2-D section is four launches instead of
-// three elementwise kernels and four line sweeps.  The x and r vectors are
-// double-buffered across iterations because a segment's halo reads
-// neighbours that another segment steps.
+// three elementwise kernels and four line sweeps.  The residual and its
+// conjugate direction are not kept as vectors: r = W x - num and sr = W sx
+// hold in exact arithmetic (ps_conjgrad starts from x = 0, r = -num and
+// steps both alike), so they are formed afresh where needed, one rounding
+// each; the reference's recurrences for them would cost 16 of the
+// iteration's 96 bytes a sample.  x is double-buffered across iterations
+// because a segment's halo reads neighbours that another segment steps.
 // ---------------------------------------------------------------------------
 // Column strips of the axis-1 pass: kSmStrip columns (one thread each) by up
 // to kSmB2 rows; inputs staged kSmStages - 1 rows ahead.
@@ -757,8 +761,8 @@ struct SmParams {
   const float* in;   // SM_IN_ARR input
   float* out;        // SM_OUT_ARR output
   const float* gpc;  // gp, read at the output sample by SM_OUT_CG2 of axis 2
-  const float *xo, *ro;
-  float *xn, *rn;
+  const float* xo;  // x before the iteration (read) and after it (written):
+  float* xn;        // double-buffered, a segment's halo reads other tiles' x
   const int4* c0map;  // axis-0 tiles: section, first trace, first sample, lines << 16 | length
   int c0buf;          // floats per axis-0 staging buffer
   int tma;            // axis-0 tiles staged by bulk copies (else 4-byte cp.async)
@@ -867,34 +871,20 @@ struct CgOut {
     a.gp[i] = g;
     a0.add_prod(g, g);
   }
+  // The mixed mode keeps no residual vectors: r = W x - num and sr = W sx
+  // (their values in exact arithmetic; each formed afresh with one
+  // rounding), so the directions step only p and x and the update writes
+  // sp and sx.  gx = S gp arrives as the smoothed value.
   __device__ __forceinline__ void cg2v(const DipArrays& a, long i, float gx, float gpv, float al,
-                                       int iter, float wv, float spv, float sxv, float srv) {
-    const float gr = __fmul_rn(gx, wv);
-    float vp = gpv, vx = gx, vr = gr;
+                                       int iter, float wv, float spv, float sxv) {
+    float vp = gpv, vx = gx;
     if (iter > 0) {
       vp = __fmaf_rn(al, spv, vp);
       vx = __fmaf_rn(al, sxv, vx);
-      vr = __fmaf_rn(al, srv, vr);
     }
     a.sp[i] = vp;
     a.sx[i] = vx;
-    a.sr[i] = vr;
-    a0.add_prod(vr, vr);
-    a1.add_prod(vp, vp);
-    a2.add_prod(vx, vx);
-  }
-  __device__ __forceinline__ void cg2(const DipArrays& a, long i, float gx, float gpv, float al,
-                                      int iter) {
-    const float gr = __fmul_rn(gx, a.u1[i]);
-    float vp = gpv, vx = gx, vr = gr;
-    if (iter > 0) {
-      vp = __fmaf_rn(al, a.sp[i], vp);
-      vx = __fmaf_rn(al, a.sx[i], vx);
-      vr = __fmaf_rn(al, a.sr[i], vr);
-    }
-    a.sp[i] = vp;
-    a.sx[i] = vx;
-    a.sr[i] = vr;
+    const float vr = __fmul_rn(wv, vx);  // sr = W sx
     a0.add_prod(vr, vr);
     a1.add_prod(vp, vp);
     a2.add_prod(vx, vx);
@@ -973,8 +963,9 @@ template <int IN, int NB0>
 __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipBatch b,
                                                               SmParams q) {
   constexpr int NT = conv0_threads<IN>(), OUTS = conv0_outs<IN>();
-  // buffers of q.c0buf floats: the input (SM_IN_ARR); x (becoming gx), r,
-  // u1, sx, sr (SM_IN_CG1)
+  // buffers of q.c0buf floats: the input (SM_IN_ARR); x (becoming gx), W,
+  // num, sx (SM_IN_CG1); with bulk staging the lines come first, then one
+  // staging buffer per array
   extern __shared__ __align__(16) float buf[];
   const int4 tm = q.c0map[blockIdx.x];
   const SecDesc& s = b.secs[tm.x];
@@ -994,7 +985,6 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
         for (int i = threadIdx.x; i < len; i += NT) {
           const long e = so + k * n1 + o1 + i;
           q.xn[e] = q.xo[e];
-          q.rn[e] = q.ro[e];
         }
     return;
   }
@@ -1014,8 +1004,8 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
     const long g0 = so + p0, g1 = so + (long)(nl - 1) * n1 + p1;
     const long ga = g0 & ~3L, gb = (g1 + 3) & ~3L;
     const unsigned bytes = (unsigned)((gb - ga) * 4);
-    constexpr int NA = IN == SM_IN_ARR ? 1 : 5;
-    const int narr = IN == SM_IN_ARR ? 1 : (stepped ? 5 : 3);
+    constexpr int NA = IN == SM_IN_ARR ? 1 : 4;
+    const int narr = IN == SM_IN_ARR ? 1 : (stepped ? 4 : 3);
     float* stg = buf + nbuf;
     if (threadIdx.x == 0) {
       mbar_init(&s_bar, 1);
@@ -1026,10 +1016,9 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
         src[0] = q.in;
       } else {
         src[0] = q.xo;
-        src[1 % NA] = q.ro;
-        src[2 % NA] = a.u1;
+        src[1 % NA] = a.u1;
+        src[2 % NA] = a.u2;  // num, the division's right-hand side
         src[3 % NA] = a.sx;
-        src[4 % NA] = a.sr;
       }
       for (int ar = 0; ar < narr; ar++) bulk_copy_g2s(stg + ar * nbuf, src[ar] + ga, bytes, &s_bar);
       // a copy that does not complete in time marks the section and the
@@ -1053,17 +1042,12 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
         if (IN == SM_IN_ARR) {
           bl[c] = stg[i];
         } else {
-          float xi = stg[i], ri = stg[nbuf + i];
-          if (stepped) {
-            xi = __fmaf_rn(st, stg[3 * nbuf + i], xi);
-            ri = __fmaf_rn(st, stg[4 * nbuf + i], ri);
-          }
-          bl[c] = __fmaf_rn(ri, stg[2 * nbuf + i], -xi);  // gx = -eps x + W' r
-          if (c >= h0 && c < h0 + len) {                    // this tile's own sample
-            const long e = so + k * n1 + o1 - h0 + c;
-            q.xn[e] = xi;
-            q.rn[e] = ri;
-          }
+          float xi = stg[i];
+          if (stepped) xi = __fmaf_rn(st, stg[3 * nbuf + i], xi);
+          const float wi = stg[nbuf + i];
+          const float ri = __fmaf_rn(wi, xi, -stg[2 * nbuf + i]);  // r = W x - num
+          bl[c] = __fmaf_rn(ri, wi, -xi);                           // gx = -eps x + W' r
+          if (c >= h0 && c < h0 + len) q.xn[so + k * n1 + o1 - h0 + c] = xi;  // own sample
         }
       }
     }
@@ -1078,12 +1062,9 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
         cp_async4(bl + c, q.in + so + i);
       } else {
         cp_async4(bl + c, q.xo + so + i);
-        cp_async4(bl + nbuf + c, q.ro + so + i);
-        cp_async4(bl + 2 * nbuf + c, a.u1 + so + i);
-        if (stepped) {
-          cp_async4(bl + 3 * nbuf + c, a.sx + so + i);
-          cp_async4(bl + 4 * nbuf + c, a.sr + so + i);
-        }
+        cp_async4(bl + nbuf + c, a.u1 + so + i);
+        cp_async4(bl + 2 * nbuf + c, a.u2 + so + i);
+        if (stepped) cp_async4(bl + 3 * nbuf + c, a.sx + so + i);
       }
     }
   }
@@ -1095,17 +1076,12 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
     for (int k = 0; k < nl; k++) {
       float* bl = buf + k * stride;
       for (int c = threadIdx.x; c < w; c += NT) {
-        float xi = bl[c], ri = bl[nbuf + c];
-        if (stepped) {
-          xi = __fmaf_rn(st, bl[3 * nbuf + c], xi);
-          ri = __fmaf_rn(st, bl[4 * nbuf + c], ri);
-        }
-        bl[c] = __fmaf_rn(ri, bl[2 * nbuf + c], -xi);  // gx = -eps x + W' r
-        if (c >= h0 && c < h0 + len) {                  // this tile's own sample
-          const long e = so + k * n1 + o1 - h0 + c;
-          q.xn[e] = xi;
-          q.rn[e] = ri;
-        }
+        float xi = bl[c];
+        if (stepped) xi = __fmaf_rn(st, bl[3 * nbuf + c], xi);
+        const float wi = bl[nbuf + c];
+        const float ri = __fmaf_rn(wi, xi, -bl[2 * nbuf + c]);  // r = W x - num
+        bl[c] = __fmaf_rn(ri, wi, -xi);                         // gx = -eps x + W' r
+        if (c >= h0 && c < h0 + len) q.xn[so + k * n1 + o1 - h0 + c] = xi;  // own sample
       }
     }
     __syncthreads();
@@ -1219,7 +1195,6 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
           if (q.iter > 0) {
             cp_async4(sg + 3 * kSmStrip, a.sp + i);
             cp_async4(sg + 4 * kSmStrip, a.sx + i);
-            cp_async4(sg + 5 * kSmStrip, a.sr + i);
           }
         }
       }
@@ -1247,7 +1222,7 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
     else if (OUT == SM_OUT_CG1)
       co.cg1v(a, i, acc, st, q.iter, ov[0], ov[1]);
     else
-      co.cg2v(a, i, acc, ov[0], al, q.iter, ov[1], ov[2], ov[3], ov[4]);
+      co.cg2v(a, i, acc, ov[0], al, q.iter, ov[1], ov[2], ov[3]);
   };
   for (int k = 0; k < kSmStages - 1; k++) issue(k);
   if (NB1 > 0) {
@@ -1400,7 +1375,6 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.sr = cv.take<float>(n);
   w.a.tri = mixed ? nullptr : cv.take<float>(L.scr_total);
   w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
-  w.a.r2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.t2 = mixed && L.any3d ? cv.take<float>(n) : nullptr;
   w.a.c0map = mixed ? cv.take<int4>(L.nctiles) : nullptr;
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
@@ -1507,7 +1481,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const char* tma_env = getenv("PWD_CONV0_TMA");
   q.tma = !(tma_env && atoi(tma_env) == 0);
   const size_t smem0 = sizeof(float) * q.c0buf * (q.tma ? 2 : 1),
-               smem0cg = sizeof(float) * q.c0buf * (q.tma ? 6 : 5);
+               smem0cg = sizeof(float) * q.c0buf * (q.tma ? 5 : 4);
   const bool ring1 = !(q.nb1 == 10 || q.nb1 == 5);
   const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));
@@ -1528,7 +1502,6 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   for (SmKernel k : {c2_cg1, c2_cg2})
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
   float* X[2] = {a.dp, a.x2};
-  float* Rv[2] = {a.r, a.r2};
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_conv0_map<<<(gc + 255) / 256, 256, 0, st>>>(b.secs, b.nsec, (int)gc, q.nb0 - 1,
                                                              a.c0map));
@@ -1539,9 +1512,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
     for (int it = 0; it < liter; it++) {
       q.iter = it;
       q.xo = X[it & 1];
-      q.ro = Rv[it & 1];
       q.xn = X[(it + 1) & 1];
-      q.rn = Rv[(it + 1) & 1];
       // 2-D sections (every section when no cube is smoothed along axis 2):
       // axis 0 with the input operation, axis 1 with the output operation;
       // the axis-2 smoothing of a length-1 line is the identity
@@ -1580,7 +1551,6 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
     }
     DipArrays af = a;  // x and r after the last iteration
     af.dp = X[liter & 1];
-    af.r = Rv[liter & 1];
     if (liter > 0) PWD_KERNEL(PWD_FAM_CG, st, k_cg_step<<<gt, kTileThreads, 0, st>>>(af, b));
     for (int k = 0; k < 8; k++)
       PWD_KERNEL(PWD_FAM_PWD, st,
