@@ -16,7 +16,9 @@
  *     a fixed device array of the library (below);
  *   - work is enqueued on `stream` (NULL = legacy default stream) and the
  *     call returns without synchronising; results are ready once the
- *     stream has been synchronised;
+ *     stream has been synchronised (pwd_sint2d, pwd_sint3d and
+ *     pwd_soint2d_prec read values back and synchronise `stream` before
+ *     they return);
  *   - results depend only on the arguments: calls on different streams
  *     with different workspaces may run concurrently.  The library's own
  *     process-wide state is limited to pwd_dip_static's scratch array
@@ -238,6 +240,22 @@ int pwd_soint3d(const float *data, const float *mask, const float *dip_inline,
                 int nj2, int niter, int drift, int seed, int hasmask, float var,
                 void *workspace, size_t workspace_bytes, pwd_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * 2-D interpolation preconditioned by plane-wave integration.
+ * Replaces the prec = 1 branches of csoint2d, pyseistr/src/soint2d_cfuns.c:
+ * 2354-2398 (soint2dc(..., prec=1), soint2d.py:92): ps_solver_prec
+ * (:1704) on M P p = d with ps_cgstep, P = predict_lop (:1537) along dip1,
+ * or predict2_lop (:1597) chaining dip1 and dip2 when twoplane; out = P p.
+ * known = (mask != 0) if hasmask == 1, else (data != 0).  n1 >= 2.  The
+ * call synchronises `stream` (it reads back a completion flag) and returns
+ * PWD_ECUDA if a trace's factor copy did not complete in time.
+ */
+size_t pwd_soint2d_prec_workspace_size(int n1, int n2, int order, int twoplane);
+int pwd_soint2d_prec(const float *data, const float *mask, const float *dip1, const float *dip2,
+                     float *out, int n1, int n2, int order, int niter, int hasmask,
+                     int twoplane, void *workspace, size_t workspace_bytes,
+                     pwd_stream_t stream);
+
 /* Many patches of uneven size in one launch sequence (the batched
  * interpolation workflow): a loop of csoint3d calls over patches without
  * noise (var = 0).  sections[k].offset places patch k in data, mask and
@@ -398,7 +416,8 @@ int pwd_sint3d(const float *din, const float *dipi, const float *dipx, const flo
  * about 1e-7 relative for float input, 1e-15 for double.  w = 0 is
  * PWD_EINVAL (the reference divides by zero).  Device pointers; workspace
  * of pwd_fkdip_workspace_size bytes (f64: the double entry's; 0 for
- * invalid sizes). */
+ * invalid sizes).  Each call uploads its twiddle tables from host memory
+ * with cudaMemcpyAsync, so it cannot be captured into a CUDA graph. */
 size_t pwd_fkdip_workspace_size(int n1, int n2, int f64);
 int pwd_fkdip(const float *d, double *out, int n1, int n2, double w, void *workspace,
               size_t workspace_bytes, pwd_stream_t stream);

@@ -57,6 +57,7 @@ def lib():
             getattr(L, f"orc_somean3d_{pre}").argtypes = [_P, _P, _P, _P] + [_I] * 6
             getattr(L, f"orc_somf3d_{pre}").argtypes = [_P, _P, _P, _P] + [_I] * 8
             getattr(L, f"orc_soint3d_{pre}").argtypes = [_P] * 5 + [_I] * 10 + [R]
+            getattr(L, f"orc_soint2d_prec_{pre}").argtypes = [_P] * 5 + [_I] * 5
         L.orc_pwspray2d_f32.argtypes = [_P, _P, _P, _I, _I, _I, _I, _F]
         L.orc_pwspray3d_f32.argtypes = [_P, _P, _P, _P] + [_I] * 6
         L.orc_spray_median_f32.argtypes = [_P, _P, _I, _I, _L, _I, _I]
@@ -188,6 +189,24 @@ def soint3d(din, mask, dipi, dipx, order=1, niter=100, njs=(1, 1), drift=0, seed
         drift, seed, hasmask, var)
     _check(rc, "soint3d")
     return out.reshape(n1, n2, n3, order="F")
+
+
+def soint2d_prec(din, mask, dip, order=1, niter=100, hasmask=1, twoplane=0, precision="f32"):
+    """csoint2d with prec = 1: dip is [n1, n2] (one plane) or [n1, n2, 2]
+    (twoplane, the two planes' slopes)."""
+    dt = _dt(precision)
+    n1, n2 = din.shape[:2]
+    d, m = _flat(din, dt), _flat(mask, dt)
+    if twoplane:
+        p, q = _flat(dip[:, :, 0], dt), _flat(dip[:, :, 1], dt)
+    else:
+        p, q = _flat(dip, dt), None
+    out = np.empty(n1 * n2, dtype=dt)
+    rc = getattr(lib(), f"orc_soint2d_prec_{precision}")(
+        _ptr(d), _ptr(m), _ptr(p), _ptr(q) if q is not None else None, _ptr(out), n1, n2, order,
+        niter, hasmask)
+    _check(rc, "soint2d_prec")
+    return out.reshape(n1, n2, order="F")
 
 
 def pwspray2d(dn, dip, ns, order, eps):

@@ -24,6 +24,9 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# run as a script, this folder is first on the path and its oracle.py would
+# shadow the oracle package
+sys.path[:] = [p for p in sys.path if os.path.abspath(p or ".") != HERE]
 sys.path.insert(0, os.path.dirname(HERE))
 
 import workloads as W  # noqa: E402

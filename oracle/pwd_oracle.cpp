@@ -1811,6 +1811,151 @@ static int soint3d(const R* din, const R* mask, const R* pp, const R* qq, R* dou
   return ORC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Preconditioned 2-D interpolation, the prec = 1 branches of csoint2d
+// (soint2d_cfuns.c:2354-2398): ps_solver_prec (:1704-2034) with ps_mask_lop
+// (:145-159) as the operator, ps_cgstep (:493-544) as the step and
+// predict_lop (:1537-1571) or predict2_lop (:1597-1616) as the
+// preconditioner, x = P p, eps = 0, no weights, no x0.
+// ---------------------------------------------------------------------------
+
+// predict_lop: trace-by-trace integration along the slopes.  Forward:
+// tt += xx[i2], yy[i2] += tt, tt = predict_step(tt; dip[i2]) for ascending
+// i2; the adjoint runs the steps backwards.  forw = true throughout.
+template <class R>
+static void predict_lop(Predict<R>& pr, bool adj, bool add, int n1, int n2, const R* dip, R* xx,
+                        R* yy) {
+  const long n = (long)n1 * n2;
+  if (!add) std::fill(adj ? xx : yy, (adj ? xx : yy) + n, (R)0);
+  std::vector<R> tt(n1, (R)0);
+  if (adj) {
+    for (int i2 = n2 - 1; i2 >= 0; i2--) {
+      pr.step(true, true, tt.data(), dip + (long)i2 * n1);
+      for (int i1 = 0; i1 < n1; i1++) tt[i1] += yy[i1 + (long)i2 * n1];
+      for (int i1 = 0; i1 < n1; i1++) xx[i1 + (long)i2 * n1] += tt[i1];
+    }
+  } else {
+    for (int i2 = 0; i2 < n2; i2++) {
+      for (int i1 = 0; i1 < n1; i1++) tt[i1] += xx[i1 + (long)i2 * n1];
+      for (int i1 = 0; i1 < n1; i1++) yy[i1 + (long)i2 * n1] += tt[i1];
+      pr.step(false, true, tt.data(), dip + (long)i2 * n1);
+    }
+  }
+}
+
+// The preconditioner: predict_lop with pp, or predict2_lop (the chain of
+// the pp and qq integrations) when qq is given; tmp holds the
+// intermediate of the chain.
+template <class R>
+static void prec_lop(Predict<R>& pr, bool adj, int n1, int n2, const R* pp, const R* qq, R* x,
+                     R* y, R* tmp) {
+  if (!qq) {
+    predict_lop(pr, adj, false, n1, n2, pp, x, y);
+  } else if (adj) {
+    predict_lop(pr, true, false, n1, n2, qq, tmp, y);
+    predict_lop(pr, true, false, n1, n2, pp, x, tmp);
+  } else {
+    predict_lop(pr, false, false, n1, n2, pp, x, tmp);
+    predict_lop(pr, false, false, n1, n2, qq, tmp, y);
+  }
+}
+
+// ps_solver_prec as csoint2d calls it: x and dat are the same array (mm);
+// dat is read once, into rr = -dat, and x is the chain's intermediate until
+// the final x = P p.  The model-space half of p beyond nprec (eps p = 0
+// with eps = 0) never reaches x and is left out; its zeros do enter gg
+// through the saxpy with eps = 0, kept here.
+template <class R>
+static void solver_prec(int n1, int n2, int nw, const R* pp, const R* qq, const uint8_t* known,
+                        R* x, int niter) {
+  const long n = (long)n1 * n2;
+  Predict<R> pr;
+  pr.init(n1, (R)0.0001f, nw, false);  // predict_init(n1, n2, 0.0001, nw, 1, false)
+  std::vector<R> p(n, (R)0), g(n), rr(n), gg(n), S(n, (R)0), Ss(n, (R)0), tmp(n);
+  for (long i = 0; i < n; i++) rr[i] = -x[i];
+  double dprr, dpgm, dprr0 = 1., dpgm0 = 1.;
+  const double TOL = (double)1.e-12f, EPS = (double)1.e-12f;
+  bool forget = true;  // ps_cgstep's first call restarts
+  for (int iter = 0; iter < niter; iter++) {
+    // g = P' M rr
+    for (long i = 0; i < n; i++) {
+      x[i] = 0;
+      if (known[i]) x[i] += rr[i];
+    }
+    prec_lop(pr, true, n1, n2, pp, qq, g.data(), x, tmp.data());
+    // gg = M P g + eps g[nprec:] with g[nprec:] = eps rr
+    prec_lop(pr, false, n1, n2, pp, qq, g.data(), x, tmp.data());
+    for (long i = 0; i < n; i++) {
+      gg[i] = 0;
+      if (known[i]) gg[i] += x[i];
+    }
+    for (long i = 0; i < n; i++) gg[i] += (R)0.f * (R)(0. * rr[i]);
+    if (iter == 0) {
+      dprr0 = snrm2(n, rr.data());
+      dpgm0 = snrm2(n, g.data());
+      dprr = 1.;
+      dpgm = 1.;
+    } else {
+      dprr = snrm2(n, rr.data()) / dprr0;
+      dpgm = snrm2(n, g.data()) / dpgm0;
+    }
+    if (dprr < TOL || dpgm < TOL) {
+      prec_lop(pr, false, n1, n2, pp, qq, p.data(), x, tmp.data());
+      return;
+    }
+    // ps_cgstep(forget, nprec + ny, ny, p, g, rr, gg)
+    double alfa = 0, beta = 0;
+    bool skip = false;
+    if (forget) {
+      std::fill(S.begin(), S.end(), (R)0);
+      std::fill(Ss.begin(), Ss.end(), (R)0);
+      alfa = dsdot(n, gg.data(), gg.data());
+      if (alfa <= 0.) skip = true;
+      else alfa = -dsdot(n, gg.data(), rr.data()) / alfa;
+    } else {
+      double gdg = dsdot(n, gg.data(), gg.data());
+      double sds = dsdot(n, Ss.data(), Ss.data());
+      double gds = dsdot(n, gg.data(), Ss.data());
+      if (gdg == 0. || sds == 0.) {
+        skip = true;
+      } else {
+        double determ = 1.0 - (gds / gdg) * (gds / sds);
+        if (determ > EPS) determ *= gdg * sds;
+        else determ = gdg * sds * EPS;
+        double gdr = -dsdot(n, gg.data(), rr.data());
+        double sdr = -dsdot(n, Ss.data(), rr.data());
+        alfa = (sds * gdr - gds * sdr) / determ;
+        beta = (-gds * gdr + gdg * sdr) / determ;
+      }
+    }
+    forget = false;
+    if (!skip) {
+      const R b = (R)beta, a = (R)alfa;
+      for (long i = 0; i < n; i++) S[i] *= b;
+      saxpy(n, a, g.data(), S.data());
+      for (long i = 0; i < n; i++) Ss[i] *= b;
+      saxpy(n, a, gg.data(), Ss.data());
+      for (long i = 0; i < n; i++) p[i] += S[i];
+      for (long i = 0; i < n; i++) rr[i] += Ss[i];
+    }
+    if (iter == niter - 1) prec_lop(pr, false, n1, n2, pp, qq, p.data(), x, tmp.data());
+  }
+}
+
+// csoint2d with prec = 1: dout = din interpolated; known = (mask != 0)
+// when hasmask == 1, else (din != 0); qq = nullptr for one plane.
+template <class R>
+static int soint2d_prec(const R* din, const R* mask, const R* pp, const R* qq, R* dout, int n1,
+                        int n2, int nw, int niter, int hasmask) {
+  if (n1 < 2 || n2 < 1 || nw < 1 || nw > 8 || niter < 0) return ORC_EINVAL;
+  const long n = (long)n1 * n2;
+  std::vector<uint8_t> known(n);
+  for (long i = 0; i < n; i++) known[i] = hasmask == 1 ? (mask[i] != (R)0) : (din[i] != (R)0);
+  for (long i = 0; i < n; i++) dout[i] = din[i];
+  solver_prec(n1, n2, nw, pp, qq, known.data(), dout, niter);
+  return ORC_OK;
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -2069,6 +2214,18 @@ int orc_soint3d_f64(const double* din, const double* mask, const double* pp, con
   DefaultFpEnv fpenv;
   return orc::soint3d<double>(din, mask, pp, qq, out, n1, n2, n3, nw, nj1, nj2, niter, drift,
                               seed, hasmask, var);
+}
+
+int orc_soint2d_prec_f32(const float* din, const float* mask, const float* pp, const float* qq,
+                         float* out, int n1, int n2, int nw, int niter, int hasmask) {
+  DefaultFpEnv fpenv;
+  return orc::soint2d_prec<float>(din, mask, pp, qq, out, n1, n2, nw, niter, hasmask);
+}
+int orc_soint2d_prec_f64(const double* din, const double* mask, const double* pp,
+                         const double* qq, double* out, int n1, int n2, int nw, int niter,
+                         int hasmask) {
+  DefaultFpEnv fpenv;
+  return orc::soint2d_prec<double>(din, mask, pp, qq, out, n1, n2, nw, niter, hasmask);
 }
 
 int orc_bandpass_f32(const float* in, float* out, int n1, long ntr, float d1, float flo,

@@ -127,15 +127,18 @@ def csoint2d(din, mask, dip1, dip2, n1, n2, nw, nj1, nj2, niter, drift, hasmask,
     rows are empty), computed here by pwd_soint3d; the two-plane branch
     without preconditioning returns din unchanged, as the reference's (its
     solver call is commented out).  The preconditioned branches (prec 1:
-    predict_lop / predict2_lop in ps_solver_prec) are not built."""
-    if prec:
-        raise NotImplementedError("csoint2d: prec=1 (plane-wave construction "
-                                  "preconditioning) is not implemented")
+    ps_solver_prec with predict_lop along dip1, or predict2_lop chaining dip1
+    and dip2 when twoplane) run in pwd_soint2d_prec."""
     n = n1 * n2
     d, as_t = _to_dev_flat(din)
     if d.numel() != n:
         raise ValueError(f"csoint2d: din has {d.numel()} values, expected {n}")
-    if twoplane:
+    if prec:
+        m, _ = _to_dev_flat(mask)
+        p1, _ = _to_dev_flat(dip1)
+        p2 = _to_dev_flat(dip2)[0] if twoplane else None
+        out = D.soint2d_prec(d, m, p1, p2, n1, n2, nw, niter, hasmask, twoplane)
+    elif twoplane:
         out = d.clone()
     else:
         m, _ = _to_dev_flat(mask)
@@ -247,13 +250,18 @@ def soint2dc(din, mask, dip, order=1, niter=100, njs=[1, 1], drift=0, hasmask=1,
     n1, n2 = din.shape[:2]
     dip1 = dip if twoplane == 0 else dip[:, :, 0]
     d, as_t = _to_dev_flat(din)
-    if twoplane:
-        if prec:
-            raise NotImplementedError("soint2dc: prec=1 is not implemented")
-        return _from_dev_flat(d.clone(), (n1, n2), as_t)
     if prec:
-        raise NotImplementedError("soint2dc: prec=1 (plane-wave construction "
-                                  "preconditioning) is not implemented")
+        # soint2d_cfuns.c:2354-2398: CG on M P p = d with the plane-wave
+        # integration P (predict_lop, or predict2_lop chaining both planes)
+        m, _ = _to_dev_flat(mask)
+        p1, _ = _to_dev_flat(dip1)
+        p2 = _to_dev_flat(dip[:, :, 1])[0] if twoplane else None
+        out = D.soint2d_prec(d, m, p1, p2, n1, n2, order, niter, hasmask, twoplane)
+        return _from_dev_flat(out, (n1, n2), as_t)
+    if twoplane:
+        # the reference's two-plane branch without preconditioning runs no
+        # solver and returns the data unchanged
+        return _from_dev_flat(d.clone(), (n1, n2), as_t)
     m, _ = _to_dev_flat(mask)
     p, _ = _to_dev_flat(dip1)
     out = D.soint3d(d, m, p, p, n1, n2, 1, order, njs[0], njs[1], niter, drift, 202223, hasmask,

@@ -23,6 +23,7 @@ LIB = os.path.join(HERE, "libpwd_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["pwd_capi.cu", "pwd_dip.cu", "pwd_spray2d.cu", "pwd_spray3d.cu", "pwd_soint3d.cu",
+           "pwd_soint2d_prec.cu",
            "pwd_patch.cu", "pwd_bandpass.cu", "pwd_coh.cu",
            "pwd_paint.cu", "pwd_sint.cu", "pwd_fk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

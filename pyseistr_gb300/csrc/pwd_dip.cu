@@ -216,8 +216,8 @@ __global__ void k_scale(DipArrays a, DipBatch b, int dip) {
   DipScalars* S = b.S + tr.sec;
   const bool zero = S->zero;
   const double nrm = S->norm2;
-  float *num = a.u2 + s.off, *den = a.u1 + s.off, *r = a.r + s.off, *pcg = a.pcg + s.off,
-        *x = a.dp + s.off;
+  float *num = a.u2 + s.off, *den = a.u1 + s.off, *r = a.r ? a.r + s.off : nullptr,
+        *pcg = a.pcg + s.off, *x = a.dp + s.off;
   const float nh = __double2float_rn(nrm);
   const float nl = __double2float_rn(nrm - (double)nh);
   ffacc a0;
@@ -229,7 +229,7 @@ __global__ void k_scale(DipArrays a, DipBatch b, int dip) {
     num[i] = va;
     den[i] = vb;
     float ri = -va;
-    r[i] = ri;
+    if (r) r[i] = ri;  // the mixed CG keeps no residual vector
     pcg[i] = 0.f;
     a0.add_prod(ri, ri);
   }
@@ -1367,12 +1367,12 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.dp = cv.take<float>(n);
   w.a.p0 = cv.take<float>(n);
   w.a.pcg = cv.take<float>(n);
-  w.a.r = cv.take<float>(n);
+  w.a.r = mixed ? nullptr : cv.take<float>(n);
   w.a.gp = cv.take<float>(n);
   w.a.tmp = cv.take<float>(n);
   w.a.sp = cv.take<float>(n);
   w.a.sx = cv.take<float>(n);
-  w.a.sr = cv.take<float>(n);
+  w.a.sr = mixed ? nullptr : cv.take<float>(n);
   w.a.tri = mixed ? nullptr : cv.take<float>(L.scr_total);
   w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.t2 = mixed && L.any3d ? cv.take<float>(n) : nullptr;

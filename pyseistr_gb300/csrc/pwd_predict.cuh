@@ -395,11 +395,12 @@ __device__ void predict_factor_pair(int n1, float eps, float eps2, const ApCoef&
 
 // One factor of slope trace pp (the band and LDL' steps of predict_fwd with
 // one filter): side 0 the unreversed filter (forw = false, into F.f0, also
-// storing the taps), side 1 the reversed one (F.f1).  The two sides are
-// independent and run on two threads.
+// storing the taps), side 1 the reversed one (F.f1; the taps too when
+// with_taps).  The two sides are independent and run on two threads.
 template <int NW>
 __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
-                               const float* __restrict__ pp, const PredictFactor& F, int side) {
+                               const float* __restrict__ pp, const PredictFactor& F, int side,
+                               bool with_taps = false) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW;
   const RegConst rc = reg_const(eps, eps2);
   FilterWin<NW> w;
@@ -420,7 +421,7 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
     passfilter<NW>(c, pp[cn], t);
 #pragma unroll
     for (int j = 0; j < NA; j++) {
-      if (side == 0) F.taps[((long)j * n1 + cn) * F.ss] = t[j];
+      if (side == 0 || with_taps) F.taps[((long)j * n1 + cn) * F.ss] = t[j];
       col[j] = side ? t[NA - 1 - j] : t[j];
     }
   };

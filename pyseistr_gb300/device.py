@@ -130,6 +130,26 @@ def soint3d(data, mask, dipi, dipx, n1, n2, n3, order=1, nj1=1, nj2=1, niter=100
     return out
 
 
+def soint2d_prec(data, mask, dip1, dip2, n1, n2, order=1, niter=100, hasmask=1, twoplane=0,
+                 out=None, workspace=None):
+    """csoint2d with prec = 1: the interpolation preconditioned by the
+    plane-wave integration along dip1 (and, when twoplane, chained with the
+    one along dip2).  Synchronises the current stream."""
+    L = _lib.load()
+    n = n1 * n2
+    data = _as_flat(data, n, "data")
+    mask = _as_flat(mask, n, "mask") if mask is not None else None
+    dip1 = _as_flat(dip1, n, "dip1")
+    dip2 = _as_flat(dip2, n, "dip2") if twoplane else None
+    ws = _workspace(L.pwd_soint2d_prec_workspace_size(n1, n2, order, int(bool(twoplane))),
+                    data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_soint2d_prec(_ptr(data), _ptr(mask), _ptr(dip1), _ptr(dip2), _ptr(out), n1,
+                                  n2, order, niter, int(hasmask), int(bool(twoplane)), _ptr(ws),
+                                  ws.numel(), _stream()), "soint2d_prec")
+    return out
+
+
 def panel_median(panels, nmf, option=1, out=None, workspace=None):
     """Median row (np-1)/2 of sprayed panels [ntr][np][n1] -> [ntr][n1]
     (the reference's mf/svmf as the somf filters use them)."""

@@ -71,9 +71,3 @@ def test_soint2dc_vs_oracle_larger(ps):
     want = O.soint3d(din[:, :, None], mask[:, :, None], dip[:, :, None], dip[:, :, None],
                      order=2, niter=25)[:, :, 0]
     assert np.array_equal(got, want)
-
-
-def test_prec_is_refused(ps):
-    m, din, mask, dip, _ = CASES[0]
-    with pytest.raises(NotImplementedError):
-        ps.soint2dc(din, mask, dip, prec=1, verb=0)
