@@ -162,43 +162,53 @@ __device__ __forceinline__ float subst_row(float t, const float (&ov)[NB], float
 // ps_banded_solve (:1317-1337) in place on b[plane] for every plane, called
 // by all threads: the forward substitution on one thread per plane, then
 // b[k] / d[k] by all threads (the back substitution's first operation on
-// each row), then the back substitution.
+// each row), then the back substitution.  The serial thread takes its rows
+// in blocks of kRows: it loads a block's operands and right-hand sides,
+// solves the block, then stores it, so that no load waits behind a store
+// and only the arithmetic chain of each row is exposed (about 26 cycles a
+// row at NB = 4 on the GB300, against 52 with a load and a store per row).
+constexpr int kRows = 8;
+
+template <int NB>
+__device__ __forceinline__ void subst_pass(const float* __restrict__ ops, float* __restrict__ v,
+                                           int n1, bool down) {
+  constexpr int RS = row_stride(NB);
+  float W[NB];
+#pragma unroll
+  for (int m = 0; m < NB; m++) W[m] = 0.f;
+  const int nblk = n1 / kRows;
+  for (int q = 0; q < nblk; q++) {
+    float ov[kRows][NB], t[kRows];
+#pragma unroll
+    for (int r = 0; r < kRows; r++) {
+      const int k = down ? n1 - 1 - (q * kRows + r) : q * kRows + r;
+      load_row<NB>(ops + (long)k * RS, ov[r]);
+      t[r] = v[k];
+    }
+#pragma unroll
+    for (int r = 0; r < kRows; r++) t[r] = subst_row<NB>(t[r], ov[r], W);
+#pragma unroll
+    for (int r = 0; r < kRows; r++) v[down ? n1 - 1 - (q * kRows + r) : q * kRows + r] = t[r];
+  }
+  for (int j = nblk * kRows; j < n1; j++) {
+    const int k = down ? n1 - 1 - j : j;
+    float ov[NB];
+    load_row<NB>(ops + (long)k * RS, ov);
+    v[k] = subst_row<NB>(v[k], ov, W);
+  }
+}
+
 template <int NB>
 __device__ void banded_solve_all(const TraceFac* f, float* const* b, int P) {
-  constexpr int RS = row_stride(NB);
   const int n1 = f[0].n1;
   const bool solver = (threadIdx.x & 31) == 0 && (int)(threadIdx.x >> 5) < P;
   const int pl = threadIdx.x >> 5;
-  if (solver) {
-    const float* __restrict__ fo = f[pl].fo;
-    float* __restrict__ v = b[pl];
-    float Y[NB];
-#pragma unroll
-    for (int m = 0; m < NB; m++) Y[m] = 0.f;
-#pragma unroll 4
-    for (int k = 0; k < n1; k++) {
-      float ov[NB];
-      load_row<NB>(fo + (long)k * RS, ov);
-      v[k] = subst_row<NB>(v[k], ov, Y);
-    }
-  }
+  if (solver) subst_pass<NB>(f[pl].fo, b[pl], n1, false);
   __syncthreads();
   for (int q = 0; q < P; q++)
     for (int k = threadIdx.x; k < n1; k += blockDim.x) b[q][k] = __fdiv_rn(b[q][k], f[q].d[k]);
   __syncthreads();
-  if (solver) {
-    const float* __restrict__ bo = f[pl].bo;
-    float* __restrict__ v = b[pl];
-    float X[NB];
-#pragma unroll
-    for (int m = 0; m < NB; m++) X[m] = 0.f;
-#pragma unroll 4
-    for (int k = n1 - 1; k >= 0; k--) {
-      float ov[NB];
-      load_row<NB>(bo + (long)k * RS, ov);
-      v[k] = subst_row<NB>(v[k], ov, X);
-    }
-  }
+  if (solver) subst_pass<NB>(f[pl].bo, b[pl], n1, true);
 }
 
 // pwd_set forward (:1139-1157) into tv: tmp[i] = sum_j a[j][i] tt[i+j-nw]
