@@ -692,7 +692,7 @@ def run_reference(args):
         "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
-        "config": dict(wl.config(), sample=desc),
+        "config": wl.config(),
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": kind,
                          "sample": desc},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
@@ -749,7 +749,7 @@ def run_patch(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
-            "config": dict(config, sample=desc),
+            "config": dict(config),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": 1, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
@@ -913,7 +913,7 @@ def run_bandpass(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
-            "config": dict(config, sample=desc),
+            "config": dict(config),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads,
                              "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
@@ -1050,7 +1050,7 @@ def run_das_fkcoh(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, workloads.py)",
-            "config": dict(config, sample=desc),
+            "config": dict(config),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": 1, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,

@@ -402,6 +402,11 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
+// 8-byte form: both addresses 8-byte aligned
+__device__ __forceinline__ void cp_async8(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -462,6 +467,32 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
   while (!mbar_try_wait(bar, parity))
     if (global_ns() - t0 > limit_ns) return false;
   return true;
+}
+
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs (add / mul / fma .rn.f32x2): two independent IEEE
+// operations per instruction, each rounded as its scalar form.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
+  return ((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x);
+}
+__device__ __forceinline__ float2 f2_from(unsigned long long d) {
+  return make_float2(__uint_as_float((unsigned)d), __uint_as_float((unsigned)(d >> 32)));
+}
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(d);
+}
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
+  return f2_from(d);
 }
 
 // ---------------------------------------------------------------------------

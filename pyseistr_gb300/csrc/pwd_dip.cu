@@ -1287,6 +1287,147 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
   }
 }
 
+// The same pass with two adjacent columns per thread (kSmStrip / 2 threads
+// per strip), for the compiled radii: the convolution runs on packed FP32
+// pairs (add / mul / fma .rn.f32x2, each lane rounded as the scalar form, so
+// a column's smoothed values are those of k_conv1), the two columns' rows are
+// staged by one 8-byte copy where aligned, and the CG output operation runs
+// per column.  Only the dot products' accumulation order differs from
+// k_conv1 (a thread's partial sums interleave its two columns).
+template <int OUT, int NB1, int AX = 1>
+__global__ void __launch_bounds__(kSmStrip / 2, 24) k_conv1p(DipArrays a, DipBatch b,
+                                                             SmParams q) {
+  extern __shared__ __align__(16) float sm[];
+  const int t = blockIdx.x;
+  const int si = find_section(b.nsec, (long)t, [&](int k) {
+    return (long)(AX == 1 ? b.secs[k].ftile0 : b.secs[k].gtile0);
+  });
+  const SecDesc& s = b.secs[si];
+  if (!sm_selected(q.sel, s)) return;
+  DipScalars* S = b.S + si;
+  if (S->cg_done) return;
+  const int tile0 = AX == 1 ? s.ftile0 : s.gtile0, ntile = AX == 1 ? s.nftile : s.ngtile;
+  const int n1 = AX == 1 ? s.n1 : s.n1 * s.n2, n2 = AX == 1 ? s.n2 : s.n3;
+  const int b2 = q.b2;
+  const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + b2 - 1) / b2;
+  const int lt = t - tile0;
+  const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
+  const int o2 = t2 * b2;
+  const int rows = min(b2, n2 - o2);
+  const long so = s.off + (long)i3 * n1 * n2;
+  const int c0 = 2 * threadIdx.x;  // this thread's columns c0, c0 + 1 of the strip
+  const int g1 = t1 * kSmStrip + c0;
+  const bool ok0 = g1 < n1, ok1 = g1 + 1 < n1;
+  constexpr int H1 = NB1 - 1, RING = 2 * H1 + 1;
+  const float st = (OUT == SM_OUT_CG1 && q.iter > 0) ? __double2float_rn(S->step) : 0.f;
+  const float al = (OUT == SM_OUT_CG2 && q.iter > 0) ? __double2float_rn(S->alpha) : 0.f;
+  constexpr int SE = 6 * kSmStrip;  // staging slot: [6][kSmStrip]
+  float* stg = sm;
+  const int nsteps = rows + 2 * H1;
+  // both columns of a row: one 8-byte copy when both exist and the global
+  // address is 8-byte aligned (n1 odd makes every other row unaligned)
+  auto cp2 = [&](float* dst, const float* src) {
+    if (ok1 && ((reinterpret_cast<uintptr_t>(src) & 7) == 0)) {
+      cp_async8(dst, src);
+    } else {
+      cp_async4(dst, src);
+      if (ok1) cp_async4(dst + 1, src + 1);
+    }
+  };
+  auto issue = [&](int step) {
+    if (step < nsteps && ok0) {
+      float* sg = stg + (step % kSmStages) * SE + c0;
+      const int g2 = mirror_idx(o2 - H1 + step, n2);
+      cp2(sg, q.in + so + (long)g2 * n1 + g1);
+      const int orow = step - 2 * H1;
+      if (OUT != SM_OUT_ARR && orow >= 0) {
+        const long i = so + (long)(o2 + orow) * n1 + g1;
+        if (OUT == SM_OUT_CG1) {
+          cp2(sg + kSmStrip, a.pcg + i);
+          if (q.iter > 0) cp2(sg + 2 * kSmStrip, a.sp + i);
+        } else {
+          cp2(sg + kSmStrip, q.gpc + i);
+          cp2(sg + 2 * kSmStrip, a.u1 + i);
+          if (q.iter > 0) {
+            cp2(sg + 3 * kSmStrip, a.sp + i);
+            cp2(sg + 4 * kSmStrip, a.sx + i);
+          }
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  CgOut co;
+  float2 ov[5];
+  // this step's staged input pair and output operand pairs (a missing
+  // second column holds stale values; its results are not stored)
+  auto take = [&](int step) -> float2 {
+    issue(step + kSmStages - 1);
+    cp_async_wait<kSmStages - 1>();
+    const float* sg = stg + (step % kSmStages) * SE + c0;
+    if (OUT != SM_OUT_ARR) {
+#pragma unroll
+      for (int k = 0; k < 5; k++) ov[k] = *reinterpret_cast<const float2*>(sg + (k + 1) * kSmStrip);
+    }
+    return *reinterpret_cast<const float2*>(sg);
+  };
+  auto out_op = [&](int orow, float2 acc) {
+    if (!ok0) return;
+    const long i = so + (long)(o2 + orow) * n1 + g1;
+    if (OUT == SM_OUT_ARR) {
+      q.out[i] = acc.x;
+      if (ok1) q.out[i + 1] = acc.y;
+    } else if (OUT == SM_OUT_CG1) {
+      co.cg1v(a, i, acc.x, st, q.iter, ov[0].x, ov[1].x);
+      if (ok1) co.cg1v(a, i + 1, acc.y, st, q.iter, ov[0].y, ov[1].y);
+    } else {
+      co.cg2v(a, i, acc.x, ov[0].x, al, q.iter, ov[1].x, ov[2].x, ov[3].x);
+      if (ok1) co.cg2v(a, i + 1, acc.y, ov[0].y, al, q.iter, ov[1].y, ov[2].y, ov[3].y);
+    }
+  };
+  for (int k = 0; k < kSmStages - 1; k++) issue(k);
+  float2 rg[RING];
+  for (int step0 = 0; step0 < nsteps; step0 += RING) {
+#pragma unroll
+    for (int u = 0; u < RING; u++) {
+      const int step = step0 + u;
+      if (step < nsteps) {
+        rg[u] = take(step);
+        if (step >= 2 * H1) {
+          const float w0 = tri_tap_c<NB1>(0);
+          float2 acc = mul2_rn(make_float2(w0, w0), rg[(u - H1 + RING) % RING]);
+          float2 acc2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int k = 1; k <= H1; k++) {
+            const float wk = tri_tap_c<NB1>(k);
+            const float2 pr = add2_rn(rg[(u - H1 - k + 2 * RING) % RING],
+                                      rg[(u - H1 + k + RING) % RING]);
+            if (k & 1)
+              acc2 = fma2_rn(make_float2(wk, wk), pr, acc2);
+            else
+              acc = fma2_rn(make_float2(wk, wk), pr, acc);
+          }
+          out_op(step - 2 * H1, add2_rn(acc, acc2));
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();
+  if (OUT == SM_OUT_CG1) {
+    dvec<1> acc = {{co.a0.value()}};
+    dvec<1> tot;
+    if (tiles_sum_last<1>(acc, b.partials, t, tile0, ntile, &S->cnt[2], tot) &&
+        threadIdx.x == 0)
+      cg1_finish(S, tot.v[0], q.iter);
+  } else if (OUT == SM_OUT_CG2) {
+    dvec<3> acc = {{co.a0.value(), co.a1.value(), co.a2.value()}};
+    dvec<3> tot;
+    if (tiles_sum_last<3>(acc, b.partials, t, tile0, ntile, &S->cnt[3], tot) &&
+        threadIdx.x == 0)
+      cg2_finish(S, tot, q.iter);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1452,10 +1593,17 @@ SmKernel conv0_kernel(int nb) {
   return k_conv0<IN, 0>;
 }
 template <int OUT, int AX = 1>
-SmKernel conv1_kernel(int nb) {
-  if (nb == 10) return k_conv1<OUT, 10, AX>;
-  if (nb == 5) return k_conv1<OUT, 5, AX>;
+SmKernel conv1_kernel(int nb, bool pair) {
+  if (nb == 10) return pair ? k_conv1p<OUT, 10, AX> : k_conv1<OUT, 10, AX>;
+  if (nb == 5) return pair ? k_conv1p<OUT, 5, AX> : k_conv1<OUT, 5, AX>;
   return k_conv1<OUT, 0, AX>;
+}
+// Threads of an axis-1 (or axis-2) launch: paired columns for the compiled
+// radii when PWD_CONV1_PAIR=1 (a tuning knob: on the batched workload the
+// paired kernel measured 4 % slower, 137.0 against 132.9 ms of CG a step).
+bool conv1_paired(int nb) {
+  const char* e = getenv("PWD_CONV1_PAIR");
+  return (nb == 10 || nb == 5) && e && atoi(e) == 1;
 }
 
 // Mixed mode of dip3: FP32 filter taps, the fused smoothing passes of the
@@ -1486,9 +1634,11 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const size_t smem1 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring1 ? (2 * q.nb1 - 1) * kSmStrip : 0));
   const SmKernel c0_cg = conv0_kernel<SM_IN_CG1>(q.nb0), c0_arr = conv0_kernel<SM_IN_ARR>(q.nb0);
-  const SmKernel c1_cg1 = conv1_kernel<SM_OUT_CG1>(q.nb1),
-                 c1_cg2 = conv1_kernel<SM_OUT_CG2>(q.nb1),
-                 c1_arr = conv1_kernel<SM_OUT_ARR>(q.nb1);
+  const bool p1 = conv1_paired(q.nb1), p2 = conv1_paired(q.nb2);
+  const int c1t = p1 ? kSmStrip / 2 : kSmStrip, c2t = p2 ? kSmStrip / 2 : kSmStrip;
+  const SmKernel c1_cg1 = conv1_kernel<SM_OUT_CG1>(q.nb1, p1),
+                 c1_cg2 = conv1_kernel<SM_OUT_CG2>(q.nb1, p1),
+                 c1_arr = conv1_kernel<SM_OUT_ARR>(q.nb1, p1);
   cudaFuncSetAttribute(c0_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0cg);
   cudaFuncSetAttribute(c0_arr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
   for (SmKernel k : {c1_cg1, c1_cg2, c1_arr})
@@ -1497,8 +1647,8 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   const bool ring2 = !(q.nb2 == 10 || q.nb2 == 5);
   const size_t smem2 = sizeof(float) * (kSmStages * 6 * kSmStrip +
                                         (ring2 ? (2 * q.nb2 - 1) * kSmStrip : 0));
-  const SmKernel c2_cg1 = conv1_kernel<SM_OUT_CG1, 2>(q.nb2),
-                 c2_cg2 = conv1_kernel<SM_OUT_CG2, 2>(q.nb2);
+  const SmKernel c2_cg1 = conv1_kernel<SM_OUT_CG1, 2>(q.nb2, p2),
+                 c2_cg2 = conv1_kernel<SM_OUT_CG2, 2>(q.nb2, p2);
   for (SmKernel k : {c2_cg1, c2_cg2})
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
   float* X[2] = {a.dp, a.x2};
@@ -1521,13 +1671,13 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
         q.out = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, conv0_threads<SM_IN_CG1>(), smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg1<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg1<<<gf, c1t, smem1, st>>>(a, b, q)));
         q.in = a.gp;
         q.out = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
         q.in = a.tmp;
         q.gpc = a.gp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg2<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_cg2<<<gf, c1t, smem1, st>>>(a, b, q)));
       }
       if (ax2) {  // cubes: axes 0 and 1, then axis 2 with the CG operation
         q.sel = 2;
@@ -1535,18 +1685,18 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
         PWD_KERNEL(PWD_FAM_CG, st, (c0_cg<<<gc, conv0_threads<SM_IN_CG1>(), smem0cg, st>>>(a, b, q)));
         q.in = a.tmp;
         q.out = a.t2;
-        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, c1t, smem1, st>>>(a, b, q)));
         q.in = a.t2;
-        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg1<<<gg, kSmStrip, smem2, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg1<<<gg, c2t, smem2, st>>>(a, b, q)));
         q.in = a.gp;
         q.out = a.tmp;
         PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
         q.in = a.tmp;
         q.out = a.t2;
-        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, kSmStrip, smem1, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, c1t, smem1, st>>>(a, b, q)));
         q.in = a.t2;
         q.gpc = a.gp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg2<<<gg, kSmStrip, smem2, st>>>(a, b, q)));
+        PWD_KERNEL(PWD_FAM_CG, st, (c2_cg2<<<gg, c2t, smem2, st>>>(a, b, q)));
       }
     }
     DipArrays af = a;  // x and r after the last iteration

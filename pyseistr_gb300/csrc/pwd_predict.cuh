@@ -681,102 +681,108 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
   cp_async_wait<0>();
 }
 
-// Adjoint prediction in place (predict_step adj=true, sof_cfuns.c:622-649):
-// solve, then the adjoint pwd_set, then the boundary terms.  `tr` is the
-// trace (contiguous), `xs` a per-thread interleaved scratch of n1 floats.
+// Adjoint prediction in place with a stored factor (predict_step adj=true,
+// sof_cfuns.c:622-649, with the factor k_spray2_factor stored): the banded
+// solve with the stored LDL' factor, the adjoint pwd_set with the stored
+// taps (reversed when forw), then the eps2 boundary terms; the float
+// operations of predict_adj in its order.  tr (the chain's trace) and y (its
+// scratch, holding the forward-substituted and then the solved trace) are
+// interleaved, element k at k * yss; taps and fac point at the slope trace's
+// column (element (e, k) at (e * n1 + k) * fss).  Operands are loaded in
+// blocks of kAdjRows samples ahead of the arithmetic that uses them.
+constexpr int kAdjRows = 8;
 template <int NW>
-__device__ void predict_adj(int n1, float eps, float eps2, const ApCoef& c, float* __restrict__ tr,
-                            const float* __restrict__ pp, bool forw, const PredictScratch& sc,
-                            float* __restrict__ xs) {
-  constexpr int NA = 2 * NW + 1, NB = 2 * NW;
-  const RegConst rc = reg_const(eps, eps2);
-  FilterWin<NW> w1;
-  float O[NB][NB], D[NB], Y[NB];
+__device__ void predict_adj_stored(int n1, float eps2, const float* __restrict__ taps,
+                                   const float* __restrict__ fac, long fss, bool forw,
+                                   float* __restrict__ tr, float* __restrict__ y, long yss) {
+  constexpr int NA = 2 * NW + 1, NB = 2 * NW, R = kAdjRows;
+  auto o_at = [&](int m, int k) { return fac[((long)m * n1 + k) * fss]; };
+  // pass 1: y[i] = tr[i] - sum_{m < min(i, NB)} o[m][i-1-m] y[i-1-m]; rows
+  // with fewer terms carry zero operands against the zero window
+  {
+    float Y[NB];
 #pragma unroll
-  for (int cc = 0; cc < NA; cc++)
+    for (int m = 0; m < NB; m++) Y[m] = 0.f;
+    for (int i0 = 0; i0 < n1; i0 += R) {
+      float t[R], ov[R][NB];
 #pragma unroll
-    for (int j = 0; j < NA; j++) w1.a[cc][j] = 0.f;
+      for (int r = 0; r < R; r++) {
+        const int i = i0 + r;
+        t[r] = i < n1 ? tr[(long)i * yss] : 0.f;
 #pragma unroll
-  for (int m = 0; m < NB; m++) {
-    D[m] = 0.f;
-    Y[m] = 0.f;
+        for (int m = 0; m < NB; m++) ov[r][m] = (i < n1 && i - 1 - m >= 0) ? o_at(m, i - 1 - m) : 0.f;
+      }
 #pragma unroll
-    for (int q = 0; q < NB; q++) O[m][q] = 0.f;
-  }
+      for (int r = 0; r < R; r++) {
+        if (i0 + r < n1) {
+          float v = t[r];
 #pragma unroll
-  for (int cc = 0; cc < NW; cc++)
-    if (cc < n1) filter_column<NW>(c, pp[cc], forw, w1.a[NW + 1 + cc]);
-  // pass 1: factor + forward substitution of the trace itself
-  for (int i = 0; i < n1; i++) {
-    const int cn = i + NW;
-    shift_win<NW>(w1);
-    if (cn < n1)
-      filter_column<NW>(c, pp[cn], forw, w1.a[2 * NW]);
-    else
+          for (int m = 0; m < NB; m++) v = __fsub_rn(v, __fmul_rn(ov[r][m], Y[m]));
 #pragma unroll
-      for (int j = 0; j < NA; j++) w1.a[2 * NW][j] = 0.f;
-    float diag, offd[NB];
-    reg_row<NB>(i, n1, rc, diag, offd);
-    band_add<NW>(w1, i, n1, diag, offd);
-    float dk, ok[NB];
-    ldl_row<NB>(i, n1, diag, offd, O, D, dk, ok);
-    float y = tr[i];
-#pragma unroll
-    for (int m = 0; m < NB; m++)
-      if (m < i) y = __fsub_rn(y, __fmul_rn(O[m][m], Y[m]));
-#pragma unroll
-    for (int m = 0; m < NB; m++) sc.o[((long)m * n1 + i) * sc.ss] = ok[m];
-    sc.d[(long)i * sc.ss] = dk;
-    sc.y[(long)i * sc.ss] = y;
-#pragma unroll
-    for (int m = NB - 1; m > 0; m--) {
-      D[m] = D[m - 1];
-      Y[m] = Y[m - 1];
-#pragma unroll
-      for (int q = 0; q < NB; q++) O[m][q] = O[m - 1][q];
+          for (int m = NB - 1; m > 0; m--) Y[m] = Y[m - 1];
+          Y[0] = v;
+          y[(long)(i0 + r) * yss] = v;
+        }
+      }
     }
-    D[0] = dk;
-    Y[0] = y;
-#pragma unroll
-    for (int q = 0; q < NB; q++) O[0][q] = ok[q];
   }
-  // pass 2: back substitution into xs
-  float X[NB];
+  // pass 2: x[k] = y[k] / d[k] - sum_{m < min(n1-k-1, NB)} o[m][k] x[k+m+1]
+  // (the stored o[m][k] are 0 beyond the band), in place in y
+  {
+    float X[NB];
 #pragma unroll
-  for (int m = 0; m < NB; m++) X[m] = 0.f;
-  for (int k = n1 - 1; k >= 0; k--) {
-    float t = __fdiv_rn(sc.y[(long)k * sc.ss], sc.d[(long)k * sc.ss]);
+    for (int m = 0; m < NB; m++) X[m] = 0.f;
+    for (int j0 = 0; j0 < n1; j0 += R) {
+      float t[R], dv[R], ov[R][NB];
 #pragma unroll
-    for (int m = 0; m < NB; m++)
-      if (m < n1 - k - 1) t = __fsub_rn(t, __fmul_rn(sc.o[((long)m * n1 + k) * sc.ss], X[m]));
+      for (int r = 0; r < R; r++) {
+        const int k = n1 - 1 - (j0 + r);
+        t[r] = k >= 0 ? y[(long)k * yss] : 0.f;
+        dv[r] = k >= 0 ? o_at(NB, k) : 1.f;
 #pragma unroll
-    for (int m = NB - 1; m > 0; m--) X[m] = X[m - 1];
-    X[0] = t;
-    xs[(long)k * sc.ss] = t;
+        for (int m = 0; m < NB; m++) ov[r][m] = k >= 0 ? o_at(m, k) : 0.f;
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int k = n1 - 1 - (j0 + r);
+        if (k >= 0) {
+          float v = __fdiv_rn(t[r], dv[r]);
+#pragma unroll
+          for (int m = 0; m < NB; m++) v = __fsub_rn(v, __fmul_rn(ov[r][m], X[m]));
+#pragma unroll
+          for (int m = NB - 1; m > 0; m--) X[m] = X[m - 1];
+          X[0] = v;
+          y[(long)k * yss] = v;
+        }
+      }
+    }
   }
-  const float b0 = xs[0], b1 = xs[sc.ss], b2 = xs[(long)(n1 - 2) * sc.ss],
-              b3 = xs[(long)(n1 - 1) * sc.ss];
+  const float b0 = y[0], b1 = y[yss], b2 = y[(long)(n1 - 2) * yss], b3 = y[(long)(n1 - 1) * yss];
   // pass 3: adjoint pwd_set.  tmp[k] = sum_{j=NA-1..0} a[j][k] x[k+NW-j]
   // (k in [NW, n1-NW)), then out[q] = sum_{j=NA-1..0} a[j][i] tmp[i] with
   // i = q+NW-j in [NW, n1-NW); both in the reference's accumulation order.
   FilterWin<NW> w;
-  float tw[NA];  // tw[c] = tmp[q-NW+c], aligned with the filter window
+  float tw[NA];
 #pragma unroll
   for (int cc = 0; cc < NA; cc++) {
     tw[cc] = 0.f;
 #pragma unroll
     for (int j = 0; j < NA; j++) w.a[cc][j] = 0.f;
   }
+  auto column = [&](int cn, float* col) {
+#pragma unroll
+    for (int j = 0; j < NA; j++) col[j] = taps[((long)(forw ? NA - 1 - j : j) * n1 + cn) * fss];
+  };
 #pragma unroll
   for (int cc = 0; cc < NW; cc++)
-    if (cc < n1) filter_column<NW>(c, pp[cc], forw, w.a[NW + 1 + cc]);
+    if (cc < n1) column(cc, w.a[NW + 1 + cc]);
   for (int q = 0; q < n1; q++) {
     const int cn = q + NW;
     shift_win<NW>(w);
 #pragma unroll
     for (int cc = 0; cc < NA - 1; cc++) tw[cc] = tw[cc + 1];
     if (cn < n1)
-      filter_column<NW>(c, pp[cn], forw, w.a[2 * NW]);
+      column(cn, w.a[2 * NW]);
     else
 #pragma unroll
       for (int j = 0; j < NA; j++) w.a[2 * NW][j] = 0.f;
@@ -784,22 +790,22 @@ __device__ void predict_adj(int n1, float eps, float eps2, const ApCoef& c, floa
     if (cn >= NW && cn < n1 - NW) {
 #pragma unroll
       for (int j = NA - 1; j >= 0; j--) {
-        int ii = cn + NW - j;
-        if (ii >= 0 && ii < n1) tk = __fadd_rn(tk, __fmul_rn(w.a[2 * NW][j], xs[(long)ii * sc.ss]));
+        const int ii = cn + NW - j;
+        if (ii >= 0 && ii < n1) tk = __fadd_rn(tk, __fmul_rn(w.a[2 * NW][j], y[(long)ii * yss]));
       }
     }
     tw[NA - 1] = tk;
     float o = 0.f;
 #pragma unroll
     for (int j = NA - 1; j >= 0; j--) {
-      int ii = q + NW - j;  // window slot of column ii is ii - (q - NW) = 2NW - j
+      const int ii = q + NW - j;
       if (ii >= NW && ii < n1 - NW) o = __fadd_rn(o, __fmul_rn(w.a[2 * NW - j][j], tw[2 * NW - j]));
     }
     if (q == 0) o = __fadd_rn(o, __fmul_rn(eps2, b0));
     if (q == 1) o = __fadd_rn(o, __fmul_rn(eps2, b1));
     if (q == n1 - 2) o = __fadd_rn(o, __fmul_rn(eps2, b2));
     if (q == n1 - 1) o = __fadd_rn(o, __fmul_rn(eps2, b3));
-    tr[q] = o;
+    tr[(long)q * yss] = o;
   }
 }
 

@@ -22,7 +22,8 @@ namespace pwd {
 
 size_t smooth2_workspace(int n1, int n2, int n3, int ns, int order);
 int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int n3, int ns,
-                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st);
+                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st,
+                int reuse);
 
 namespace {
 
@@ -160,11 +161,19 @@ struct GpuOps {
   int conj(float a) { return pass(kConj, a); }
   int step(float a) { return pass(kStep, a); }
   // primitives of the 3-D sequence
+  // The 2-D smoothing calls all use one slope field: after the first, each
+  // reuses the factor store and w1 it left in the smoothing workspace.  The
+  // 3-D sequence alternates two slope fields in that workspace, so every
+  // call there factors afresh.
+  bool factored = false;
   int inline_(int mode, float* in, float* out) {
-    return smooth2_run(in, dipi, out, n1, n2, n3, ns1, order1, eps, mode, sws, swsb, st);
+    const int rc = smooth2_run(in, dipi, out, n1, n2, n3, ns1, order1, eps, mode, sws, swsb, st,
+                               !three && factored ? 1 : 0);
+    if (rc == PWD_OK) factored = true;
+    return rc;
   }
   int crossline(int mode, float* in, float* out) {
-    return smooth2_run(in, xd, out, n1, n3, n2, ns2, order2, eps, mode, sws, swsb, st);
+    return smooth2_run(in, xd, out, n1, n3, n2, ns2, order2, eps, mode, sws, swsb, st, 0);
   }
   int cross(const float* a, float* b, int to, int sum) {
     PWD_KERNEL(PWD_FAM_CG, st,

@@ -35,29 +35,8 @@ struct SprayBufs {
   float* u;     // data panels [trace][np][n1] per section
   float* u1;    // ones panels (mean only)
   float* w1;    // normalisation weights, one per sample (adjoint mean only)
-  float* scr;   // per-chain prediction scratch
-  float* tbuf;  // adjoint chain traces
+  float* scr;   // factor store and chain scratch
 };
-
-__device__ __forceinline__ const SecDesc& trace_section(const SprayB& b, long g, long& q) {
-  const int si = find_section(b.nsec, g, [&](int k) { return b.secs[k].tr0; });
-  q = g - b.secs[si].tr0;
-  return b.secs[si];
-}
-
-// Per-thread prediction scratch of the adjoint chains (thread-interleaved).
-template <int NB>
-__device__ __forceinline__ PredictScratch chain_scratch(float* scr, const SecDesc& s, long tl,
-                                                        long nthr_s) {
-  PredictScratch my;
-  float* base = scr + s.sc0;
-  const long stride = (long)s.n1 * nthr_s;
-  my.o = base + tl;
-  my.d = base + NB * stride + tl;
-  my.y = base + (NB + 1) * stride + tl;
-  my.ss = nthr_s;
-  return my;
-}
 
 // Factor-once form of the forward spray.  The factor store of a section
 // (at scr + sc0, 128-byte aligned) holds, for every trace k, the
@@ -204,6 +183,7 @@ __device__ __forceinline__ TileRange tile_range(const SprayB& b, int t) {
 
 // pwsmooth_set :1102-1122 and pwsmooth_lop forward :1088-1098: w1 = 1 /
 // (weighted spray of ones) (0 where 0), smooth = sum_is u*w[is]*w1.
+// store_w1: 0 compute w1, 1 compute and store it, 2 read the stored w1.
 __global__ void k_weighted_mean(SprayBufs bf, float* __restrict__ out, SprayB b, int store_w1,
                                 int mean) {
   const TileRange tr = tile_range(b, blockIdx.x);
@@ -213,13 +193,18 @@ __global__ void k_weighted_mean(SprayBufs bf, float* __restrict__ out, SprayB b,
     const long trc = jj / (unsigned)s.n1;
     const int i1 = (int)(jj % (unsigned)s.n1);
     const long po = s.u0 + trc * b.np * (long)s.n1 + i1;
-    float acc = 0.f;
-    for (int is = 0; is < b.np; is++)
-      acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(bf.u1[po + (long)is * s.n1], tri_weight(is, b.ns)),
-                                     1.0f));
-    // 1.0/t in double rounded to float equals the float quotient
-    const float ws = (acc != 0.f) ? __fdiv_rn(1.0f, acc) : 0.f;
-    if (store_w1) bf.w1[s.off + j] = ws;
+    float ws;
+    if (store_w1 == 2) {
+      ws = bf.w1[s.off + j];
+    } else {
+      float acc = 0.f;
+      for (int is = 0; is < b.np; is++)
+        acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(bf.u1[po + (long)is * s.n1],
+                                                 tri_weight(is, b.ns)), 1.0f));
+      // 1.0/t in double rounded to float equals the float quotient
+      ws = (acc != 0.f) ? __fdiv_rn(1.0f, acc) : 0.f;
+      if (store_w1) bf.w1[s.off + j] = ws;
+    }
     if (mean) {
       float m = 0.f;
       for (int is = 0; is < b.np; is++)
@@ -255,58 +240,74 @@ __global__ void k_median_tiles(const float* __restrict__ u, float* __restrict__ 
 }
 
 // Adjoint of the weighted mean (pwsmooth_lop adjoint :1072-1086 with
-// pwspray_lop adjoint :957-989).  Thread per output trace; chain traces in a
-// per-thread buffer.  add != 0: the terms are added into `out` as it stands
-// (the adjoint with add = true, as the sparse-data interpolation's CG applies
-// it, soint2d_cfuns.c:2194-2220) instead of into zeros.
+// pwspray_lop adjoint :957-989) on the stored factors.  For output trace i
+// the reference runs two chains: over ip = i+ns .. i+1 (slot ns + is + 1,
+// the prediction with the slopes of ip - 1, forw = true) and over ip = i-ns
+// .. i-1 (slot ns - is - 1, slopes of ip, forw = false), each adding x w[slot]
+// w1 of trace ip to its running trace and then applying the adjoint
+// prediction.  Here a thread runs one chain (direction 1 the first, 0 the
+// second), numbered as the forward chains (a warp holds 32 consecutive traces
+// of one direction, so the interleaved factor, trace and scratch accesses are
+// whole lines), and leaves its trace in its column of the yb scratch;
+// k_somean2d_adj_sum then adds the two and the centre term in the
+// reference's order.
 template <int NW>
-__global__ void k_somean2d_adj(const float* __restrict__ x, const float* __restrict__ dip,
-                               float* __restrict__ out, SprayBufs bf, SprayB b, ApCoef c,
-                               int add) {
-  long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (g >= b.ntr) return;
+__global__ void __launch_bounds__(64) k_somean2d_adj_chains(const float* __restrict__ x,
+                                                            SprayBufs bf, SprayB b) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int dir = (int)((t >> 5) & 1);
+  const long g = (t >> 6) * 32 + (t & 31);
+  if (g >= b.ntp) return;
   long q;
-  const SecDesc& s = trace_section(b, g, q);
+  const SecDesc& s = padded_section(b, g, q);
+  if (q >= (long)s.n2 * s.n3) return;
   const int n1 = s.n1, n2 = s.n2;
   const int i = (int)(q % n2);
   const long i3 = q / n2;
   const long n12 = (long)n1 * n2;
-  const float* pp = dip + s.off + i3 * n12;
   const float* X = x + s.off + i3 * n12;
   const float* W = bf.w1 + s.off + i3 * n12;
-  float* tr = bf.tbuf + s.off + q * n1;
-  const long nthr_s = 2L * n2 * s.n3;
-  PredictScratch my = chain_scratch<2 * NW>(bf.scr, s, q, nthr_s);
-  float* o = out + s.pout + i3 * n12 + (long)i * n1;
-  auto add_slot = [&](int ip, int sl) {
-    const float wv = tri_weight(sl, b.ns);
+  const FactorLayout f = factor_layout<NW>(bf, s);
+  const long cl = dir * f.ntp + q, yss = 2 * f.ntp;
+  float* tr = f.yb + cl;
+  float* ys = f.y + cl;
+  for (int i1 = 0; i1 < n1; i1++) tr[(long)i1 * yss] = 0.f;
+  for (int is = b.ns - 1; is >= 0; is--) {
+    const int ip = dir == 1 ? i + is + 1 : i - is - 1;
+    if (ip < 0 || ip >= n2) continue;
+    const float wv = tri_weight(dir == 1 ? b.ns + is + 1 : b.ns - is - 1, b.ns);
     for (int i1 = 0; i1 < n1; i1++) {
-      long e = (long)ip * n1 + i1;
-      tr[i1] = __fadd_rn(tr[i1], __fmul_rn(__fmul_rn(X[e], wv), W[e]));
+      const long e = (long)ip * n1 + i1;
+      tr[(long)i1 * yss] =
+          __fadd_rn(tr[(long)i1 * yss], __fmul_rn(__fmul_rn(X[e], wv), W[e]));
     }
-  };
-  for (int i1 = 0; i1 < n1; i1++) tr[i1] = 0.f;
-  for (int is = b.ns - 1; is >= 0; is--) {
-    int ip = i + is + 1;
-    if (ip >= n2) continue;
-    add_slot(ip, b.ns + is + 1);
-    predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)(ip - 1) * n1, true, my, my.y);
+    const long tk = i3 * n2 + (dir == 1 ? ip - 1 : ip);
+    predict_adj_stored<NW>(n1, b.eps2, f.taps + tk, (dir == 1 ? f.f1 : f.f0) + tk, f.ntp,
+                           dir == 1, tr, ys, yss);
   }
-  for (int i1 = 0; i1 < n1; i1++) {
-    o[i1] = __fadd_rn(add ? o[i1] : 0.f, tr[i1]);
-    tr[i1] = 0.f;
-  }
-  for (int is = b.ns - 1; is >= 0; is--) {
-    int ip = i - is - 1;
-    if (ip < 0) continue;
-    add_slot(ip, b.ns - is - 1);
-    predict_adj<NW>(n1, b.eps, b.eps2, c, tr, pp + (long)ip * n1, false, my, my.y);
-  }
+}
+
+// out = ((add ? out : 0) + adjoint of direction 1) + adjoint of direction
+// 0, then the centre term x w[ns] w1, per sample (the reference's order).
+// add != 0: the terms are added into `out` as it stands (the adjoint with
+// add = true, as the sparse-data interpolation's CG applies it,
+// soint2d_cfuns.c:2194-2220) instead of into zeros.
+template <int NW>
+__global__ void k_somean2d_adj_sum(const float* __restrict__ x, float* __restrict__ out,
+                                   SprayBufs bf, SprayB b, int add) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  const FactorLayout f = factor_layout<NW>(bf, s);
+  const long yss = 2 * f.ntp;
   const float wc = tri_weight(b.ns, b.ns);
-  for (int i1 = 0; i1 < n1; i1++) {
-    long e = (long)i * n1 + i1;
-    float v = __fadd_rn(o[i1], tr[i1]);
-    o[i1] = __fadd_rn(v, __fmul_rn(__fmul_rn(X[e], wc), W[e]));
+  for (long j = tr.lo + threadIdx.x; j < tr.hi; j += blockDim.x) {
+    const unsigned jj = (unsigned)j;  // sections hold fewer than 2^31 samples
+    const long q = jj / (unsigned)s.n1;
+    const int i1 = (int)(jj % (unsigned)s.n1);
+    const float t1 = f.yb[(long)i1 * yss + f.ntp + q], t0 = f.yb[(long)i1 * yss + q];
+    float* o = out + s.pout + j;
+    const float v = __fadd_rn(__fadd_rn(add ? *o : 0.f, t1), t0);
+    *o = __fadd_rn(v, __fmul_rn(__fmul_rn(x[s.off + j], wc), bf.w1[s.off + j]));
   }
 }
 
@@ -348,13 +349,10 @@ SprayLayout layout2(std::vector<SecDesc>& secs, int ns, int order) {
     s.u0 = u;
     u += s.n * np;
     s.sc0 = sc;
-    const long plane = (long)s.n1 * s.n2 * s.n3;
     const long pplane = (long)s.n1 * padded_traces((long)s.n2 * s.n3);
-    // factor store + chain scratch (padded traces), or the adjoint mean's
-    // per-chain scratch (o, d, y for 2 n2 n3 chains), whichever is larger;
-    // every section's store starts on a 128-byte boundary
-    sc += std::max((long)(nb + 2) * 2 * plane,
-                   (long)(2 * order + 1 + 2 * (nb + 1)) * pplane + 4 * pplane);
+    // factor store + chain scratch (padded traces); every section's store
+    // starts on a 128-byte boundary
+    sc += (long)(2 * order + 1 + 2 * (nb + 1)) * pplane + 4 * pplane;
     sc = (sc + 31) / 32 * 32;
     samp = std::max(samp, s.off + s.n);
     L.n1max = std::max(L.n1max, (long)s.n1);
@@ -387,17 +385,20 @@ struct SprayWork {
   int* tile_sec;
 };
 
+// shared: the layout of the smoothing calls of the sparse-data
+// interpolation, the same for the forward and the adjoint mean, so that the
+// factor store and the normalisation w1 one call leaves in the workspace
+// serve the next calls on the same slopes.
 SprayWork carve2(void* ws, const SprayLayout& L, int nsec, int filter, int option,
-                 size_t* total) {
+                 size_t* total, bool shared = false) {
   Carver cv(ws);
   SprayWork w{};
   const bool adj = filter == kMeanAdj || filter == kMeanAdjAdd;
   const bool mean = filter == kMean || adj;
-  w.bf.u = adj ? nullptr : cv.take<float>(L.nu);
-  w.bf.u1 = mean ? cv.take<float>(L.nu) : nullptr;
-  w.bf.w1 = adj ? cv.take<float>(L.nsamp) : nullptr;
   w.bf.scr = cv.take<float>(std::max(L.nscr, 1L));
-  w.bf.tbuf = adj ? cv.take<float>(L.nsamp) : nullptr;
+  w.bf.w1 = adj || (shared && mean) ? cv.take<float>(L.nsamp) : nullptr;
+  w.bf.u = adj && !shared ? nullptr : cv.take<float>(L.nu);
+  w.bf.u1 = mean ? cv.take<float>(L.nu) : nullptr;
   w.ones = cv.take<float>(L.n1max);
   const bool svmf = filter == kMedian && option != 1;
   w.v2 = svmf ? cv.take<float>(L.nu) : nullptr;
@@ -408,10 +409,13 @@ SprayWork carve2(void* ws, const SprayLayout& L, int nsec, int filter, int optio
   return w;
 }
 
+// reuse (the shared layout only): bit 0, the factor store is in place (the
+// previous call factored the same slopes in this workspace); bit 1, so is
+// w1, the normalisation of the mean (1 / the weighted spray of ones).
 template <int NW>
 int spray2_run(const float* data, const float* dip, float* out, int filter, int option, int nmf,
                const std::vector<SecDesc>& secs, const SprayLayout& L, const SprayWork& w,
-               int ns, float eps, cudaStream_t st) {
+               int ns, float eps, cudaStream_t st, int reuse = 0) {
   const int nsec = (int)secs.size();
   const ApCoef c = make_apcoef(NW);
   SprayB b{w.secs, w.tile_sec, nsec, L.ntiles, L.ntr, L.ntp, ns, 2 * ns + 1, eps * eps, eps * eps};
@@ -427,11 +431,11 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   PWD_KERNEL(PWD_FAM_OTHER, st,
              k_fill<<<(unsigned)((L.n1max + 255) / 256), 256, 0, st>>>(w.ones, 1.0f, L.n1max));
   // slots whose source lies outside the section stay 0 (pwspray_lop :995)
+  const bool have_w1 = (reuse & 2) && w.bf.w1;
   if (w.bf.u && cudaMemsetAsync(w.bf.u, 0, sizeof(float) * L.nu, st) != cudaSuccess)
     return PWD_ECUDA;
-  if (w.bf.u1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
+  if (w.bf.u1 && !have_w1 && cudaMemsetAsync(w.bf.u1, 0, sizeof(float) * L.nu, st) != cudaSuccess)
     return PWD_ECUDA;
-  const unsigned gtr = (unsigned)((L.ntr + bs - 1) / bs);
   const unsigned gap = (unsigned)((2 * L.ntp + bs - 1) / bs);
   const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
   // a thread per filter orientation when even then the factor launch fills
@@ -441,7 +445,9 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spray2_factor<NW, true>, bs, 0);
-  if (split == 1 || (split < 0 && 2 * L.ntp <= (long)sms * per * bs)) {
+  if (reuse & 1) {
+    // the factor store of the previous call on these slopes is in place
+  } else if (split == 1 || (split < 0 && 2 * L.ntp <= (long)sms * per * bs)) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                (k_spray2_factor<NW, true><<<(unsigned)((2 * L.ntp + bs - 1) / bs), bs, 0, st>>>(
                    dip, w.bf, b, c)));
@@ -450,20 +456,34 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                (k_spray2_factor<NW, false><<<(unsigned)((L.ntp + bs - 1) / bs), bs, 0, st>>>(
                    dip, w.bf, b, c)));
   }
-  if (filter == kMean) {
+  if (filter == kMean && have_w1) {
+    // the data alone, normalised by the stored w1
+    PWD_KERNEL(PWD_FAM_SPRAY, st,
+               k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+    PWD_KERNEL(PWD_FAM_FILTER, st,
+               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 2, 1));
+  } else if (filter == kMean) {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
-               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 0, 1));
+               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(
+                   w.bf, out, b, w.bf.w1 ? 1 : 0, 1));
   } else if (filter == kMeanAdj || filter == kMeanAdjAdd) {
+    if (!have_w1) {
+      PWD_KERNEL(PWD_FAM_SPRAY, st,
+                 k_spray2_apply<NW, 2><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+      PWD_KERNEL(PWD_FAM_FILTER, st,
+                 k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1,
+                                                                               0));
+    }
+    // the adjoint chains on the stored factors, their traces and scratch in
+    // the chain scratch of the factor store, then the per-sample sum
     PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 2><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+               k_somean2d_adj_chains<NW><<<(unsigned)((2 * L.ntp + 63) / 64), 64, 0, st>>>(
+                   data, w.bf, b));
     PWD_KERNEL(PWD_FAM_FILTER, st,
-               k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1, 0));
-    // the adjoint chains reuse the scratch region as their per-chain scratch
-    PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_somean2d_adj<NW><<<gtr, bs, 0, st>>>(data, dip, out, w.bf, b, c,
-                                                      filter == kMeanAdjAdd ? 1 : 0));
+               k_somean2d_adj_sum<NW><<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(
+                   data, out, w.bf, b, filter == kMeanAdjAdd ? 1 : 0));
   } else {
     PWD_KERNEL(PWD_FAM_SPRAY, st,
                k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
@@ -487,12 +507,12 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
 
 int spray2_dispatch(int order, const float* data, const float* dip, float* out, int filter,
                     int option, int nmf, const std::vector<SecDesc>& secs, const SprayLayout& L,
-                    const SprayWork& w, int ns, float eps, cudaStream_t st) {
+                    const SprayWork& w, int ns, float eps, cudaStream_t st, int reuse = 0) {
   switch (order) {
-    case 1: return spray2_run<1>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
-    case 2: return spray2_run<2>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
-    case 3: return spray2_run<3>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
-    case 4: return spray2_run<4>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+    case 1: return spray2_run<1>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st, reuse);
+    case 2: return spray2_run<2>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st, reuse);
+    case 3: return spray2_run<3>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st, reuse);
+    case 4: return spray2_run<4>(data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st, reuse);
   }
   return PWD_ENOTSUP;
 }
@@ -512,25 +532,27 @@ std::vector<SecDesc> single(int n1, int n2, int n3) {
   return v;
 }
 
-size_t need_single(int n1, int n2, int n3, int ns, int order, int filter, int option) {
+size_t need_single(int n1, int n2, int n3, int ns, int order, int filter, int option,
+                   bool shared = false) {
   std::vector<SecDesc> secs = single(n1, n2, n3);
   SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
-  carve2(nullptr, L, 1, filter, option, &need);
+  carve2(nullptr, L, 1, filter, option, &need, shared);
   return need;
 }
 
 int run_single(const float* data, const float* dip, float* out, int n1, int n2, int n3, int ns,
                int order, float eps, int filter, int option, int nmf, void* ws, size_t wsb,
-               cudaStream_t st) {
+               cudaStream_t st, bool shared = false, int reuse = 0) {
   std::vector<SecDesc> secs = single(n1, n2, n3);
   SprayLayout L = layout2(secs, ns, order);
   size_t need = 0;
-  carve2(nullptr, L, 1, filter, option, &need);
+  carve2(nullptr, L, 1, filter, option, &need, shared);
   if (!ws || wsb < need || ((uintptr_t)ws & 255)) return PWD_EWORKSPACE;
-  SprayWork w = carve2(ws, L, 1, filter, option, &need);
+  SprayWork w = carve2(ws, L, 1, filter, option, &need, shared);
   PWD_KERNEL(PWD_FAM_OTHER, st, k_put_single<<<1, 1, 0, st>>>(w.secs, secs[0]));
-  return spray2_dispatch(order, data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st);
+  return spray2_dispatch(order, data, dip, out, filter, option, nmf, secs, L, w, ns, eps, st,
+                         shared ? reuse : 0);
 }
 
 int batch_table2(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
@@ -556,18 +578,23 @@ int batch_table2(const pwd_section* in, int nsec, std::vector<SecDesc>& secs) {
 // weighted spray mean, as pwd_somean2d), mode 1 gives out += S' in, the
 // adjoint adding its terms into out in the reference's order, and mode 2
 // out = S' in (pwd_somean2d's adjoint).  `in` and `out` must not overlap.
+// Every call leaves the slopes' factor store and w1 in the workspace.
 size_t smooth2_workspace(int n1, int n2, int n3, int ns, int order) {
   if (check2(n1, n2, n3, ns, order) != PWD_OK) return 0;
-  return std::max(need_single(n1, n2, n3, ns, order, kMean, 1),
-                  need_single(n1, n2, n3, ns, order, kMeanAdjAdd, 1));
+  return std::max(need_single(n1, n2, n3, ns, order, kMean, 1, true),
+                  need_single(n1, n2, n3, ns, order, kMeanAdjAdd, 1, true));
 }
 
+// reuse != 0: the previous smooth2_run call in this workspace was on the
+// same slopes and sizes, so its factor store and w1 are used again.
 int smooth2_run(const float* in, const float* dip, float* out, int n1, int n2, int n3, int ns,
-                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st) {
+                int order, float eps, int mode, void* ws, size_t wsb, cudaStream_t st,
+                int reuse) {
   int rc = check2(n1, n2, n3, ns, order);
   if (rc != PWD_OK) return rc;
   const int filter = mode == 1 ? kMeanAdjAdd : (mode == 2 ? kMeanAdj : kMean);
-  return run_single(in, dip, out, n1, n2, n3, ns, order, eps, filter, 1, 0, ws, wsb, st);
+  return run_single(in, dip, out, n1, n2, n3, ns, order, eps, filter, 1, 0, ws, wsb, st, true,
+                    reuse ? 3 : 0);
 }
 
 }  // namespace pwd

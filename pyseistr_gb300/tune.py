@@ -6,14 +6,17 @@ The kernels read a few tuning knobs from the environment at every call:
                    array (1, default) or element by element with cp.async (0)
   PWD_CG_STRIP     rows of an axis-1 strip of the mixed CG: 32, 64, 128
                    (default) or 256
+  PWD_CONV1_PAIR   axis-1 passes of the mixed CG with one column per thread
+                   (0, default) or two on packed FP32 pairs (1)
   PWD_SPRAY_BLOCK  threads per block of the spray's chain kernels: 32 or 64
                    (default)
   PWD_SPRAY_SPLIT  spray factor kernel: a thread per filter orientation (1),
                    per trace (0), or chosen by the wave count (unset)
 
 None of them changes what is computed: the spray and the axis-0 staging
-give the same bits whatever the setting, and the strip height only changes
-the order in which the mixed CG's FP64 dot products are summed.
+give the same bits whatever the setting, and the strip height and the
+column pairing only change the order in which the mixed CG's FP64 dot
+products are summed.
 
 `autotune` times the workload's step (slope estimation and filter) under
 candidate settings, one knob at a time from the defaults (coordinate
@@ -34,6 +37,7 @@ from typing import Callable, Dict, List, Optional, Sequence, Tuple
 KNOBS: Dict[str, List[Optional[str]]] = {
     "PWD_CONV0_TMA": ["1", "0"],
     "PWD_CG_STRIP": ["128", "64", "256", "32"],
+    "PWD_CONV1_PAIR": ["0", "1"],
     "PWD_SPRAY_BLOCK": ["64", "32"],
     "PWD_SPRAY_SPLIT": [None, "1", "0"],
 }

@@ -1,7 +1,7 @@
 """The tuning knobs leave the results as they are: the spray's block size
-and factor form give the same bits, the mixed CG's axis-1 strip height only
-reorders its FP64 dot products (slopes within 1e-5 of the default, each
-setting deterministic)."""
+and factor form give the same bits, the mixed CG's axis-1 strip height and
+its paired-column kernel only reorder its FP64 dot products (slopes within
+1e-5 of the default, each setting deterministic)."""
 import os
 
 import numpy as np
@@ -66,6 +66,37 @@ def test_strip_height_reorders_sums_only(D, strip):
         a = D.dip_batch(d, shapes, 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
         b = D.dip_batch(d, shapes, 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
     assert np.array_equal(a, b)
+    assert rel_l2(a, base) <= 1e-5
+
+
+def test_paired_columns_reorder_sums_only(D):
+    """Axis-1 passes with two columns per thread on packed FP32 pairs
+    (PWD_CONV1_PAIR=1) against one column per thread (the default): the
+    smoothed values are the same per column, only the CG's dot products
+    accumulate in another order."""
+    secs = _secs() + [np.ascontiguousarray(_secs()[0][:, :37])]  # an odd trace count
+    shapes = [s.shape for s in secs]
+    d = _pack(secs)
+    with _Env(PWD_CONV1_PAIR=None):
+        base = D.dip_batch(d, shapes, 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
+    with _Env(PWD_CONV1_PAIR="1"):
+        a = D.dip_batch(d, shapes, 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
+        b = D.dip_batch(d, shapes, 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
+    assert np.array_equal(a, b)
+    assert rel_l2(a, base) <= 1e-5
+
+
+def test_paired_columns_odd_trace_length(D):
+    """n1 odd: every other row of a strip is not 8-byte aligned and the last
+    column pair has one column; the paired kernel agrees with the one-column
+    kernel."""
+    import workloads
+
+    s = workloads.das2d(n1=333, n2=91, nev=4, seed=9)
+    d = _pack([s])
+    base = D.dip_batch(d, [s.shape], 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
+    with _Env(PWD_CONV1_PAIR="1"):
+        a = D.dip_batch(d, [s.shape], 3, 6, 2, (10, 10, 1), mixed=True).cpu().numpy()
     assert rel_l2(a, base) <= 1e-5
 
 

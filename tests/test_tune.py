@@ -22,8 +22,8 @@ def test_search_picks_fastest_per_knob_and_prefers_earlier_on_ties():
              ("PWD_SPRAY_SPLIT", "1"): -0.01}
     calls = []
     choice, seen = tune.search(_timer(table, calls))
-    assert choice == {"PWD_CONV0_TMA": "1", "PWD_CG_STRIP": "64", "PWD_SPRAY_BLOCK": "64",
-                      "PWD_SPRAY_SPLIT": "1"}
+    assert choice == {"PWD_CONV0_TMA": "1", "PWD_CG_STRIP": "64", "PWD_CONV1_PAIR": "0",
+                      "PWD_SPRAY_BLOCK": "64", "PWD_SPRAY_SPLIT": "1"}
     # every distinct candidate timed once
     keys = [",".join(f"{k}={c[k]}" for k in sorted(c)) for c in calls]
     assert len(keys) == len(set(keys)) == len(seen)
