@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <cstdlib>
 #include <vector>
 
 #include "pwd_common.cuh"
@@ -21,6 +22,9 @@ namespace pwd {
 namespace {
 
 constexpr int kFkThreads = 256;
+// one transform per block in shared memory while its two buffers fit
+constexpr int kFkSmemThreads = 512;
+constexpr size_t kFkSmemMax = 200 * 1024;
 
 unsigned fk_grid(long n) {
   const long b = (n + kFkThreads - 1) / kFkThreads;
@@ -67,11 +71,54 @@ __global__ void __launch_bounds__(kFkThreads) k_fk_out(const fk::Cx<double>* dd,
   PWD_FK_LOOP(n) fk::out_sample(dd, out, n1, nf, idx, inv_nf);
 }
 
+// All log2(len) Stockham passes of one transform per block in shared
+// memory (two buffers of len elements): the transform crosses HBM once each
+// way instead of once per pass, with the same butterflies in the same
+// order as the per-pass kernel, so the same results.
+template <class R>
+__global__ void __launch_bounds__(kFkSmemThreads) k_fk_fft_smem(const fk::Cx<R>* x,
+                                                                fk::Cx<R>* y, int len,
+                                                                const fk::Cx<R>* tw,
+                                                                int inverse) {
+  extern __shared__ __align__(16) unsigned char fk_sm[];
+  fk::Cx<R>* a = reinterpret_cast<fk::Cx<R>*>(fk_sm);
+  fk::Cx<R>* b = a + len;
+  const fk::Cx<R>* xg = x + (long)blockIdx.x * len;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) a[i] = xg[i];
+  __syncthreads();
+  for (int ns = 1; ns < len; ns *= 2) {
+    for (int j = threadIdx.x; j < len / 2; j += blockDim.x)
+      fk::stockham_pass<R>(a, b, len, ns, j, tw, inverse != 0);
+    __syncthreads();
+    fk::Cx<R>* t = a;
+    a = b;
+    b = t;
+  }
+  fk::Cx<R>* yg = y + (long)blockIdx.x * len;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) yg[i] = a[i];
+}
+
 // log2(len) Stockham passes over `batch` transforms; returns the buffer
-// holding the result (x or y).
+// holding the result (x or y).  Transforms whose two buffers fit in shared
+// memory run in one launch (k_fk_fft_smem), longer ones pass by pass.
 template <class R>
 fk::Cx<R>* fft_batch(fk::Cx<R>* x, fk::Cx<R>* y, int len, long batch, const fk::Cx<R>* tw,
                      bool inverse, cudaStream_t st, int* rc) {
+  const size_t smem = 2 * sizeof(fk::Cx<R>) * (size_t)len;
+  const char* env = getenv("PWD_FK_SMEM");  // 0: every transform pass by pass
+  const bool allow = !(env && atoi(env) == 0);
+  if (allow && len >= 2 && smem <= kFkSmemMax && batch <= 0x7fffffffL) {
+    *rc = cuda_status(cudaFuncSetAttribute(k_fk_fft_smem<R>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+    if (*rc != PWD_OK) return x;
+    const int threads = len / 2 < kFkSmemThreads ? len / 2 : kFkSmemThreads;
+    PWD_KERNEL(PWD_FAM_OTHER, st,
+               (k_fk_fft_smem<R><<<(unsigned)batch, threads, smem, st>>>(x, y, len, tw,
+                                                                          inverse ? 1 : 0)));
+    *rc = cuda_status(cudaGetLastError());
+    return y;
+  }
   const long nbf = batch * (len / 2);
   for (int ns = 1; ns < len; ns *= 2) {
     PWD_KERNEL(PWD_FAM_OTHER, st,

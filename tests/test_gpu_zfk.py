@@ -74,6 +74,22 @@ def test_fkdip_device_tensors_and_linearity(ps):
     assert rel_l2(both, 2 * a - 3 * ps.fkdip(e, 0.05)) <= 1e-5
 
 
+def test_fkdip_shared_memory_transforms_equal_the_passes(ps, monkeypatch):
+    """The transforms run in shared memory (one launch each) give the bits
+    of the pass-by-pass kernels; a section wide enough that its complex128
+    space transforms (nk = 8192) exceed shared memory mixes both forms."""
+    from oracle import fk_oracle as F
+
+    for shape in ((300, 97), (64, 5000)):
+        d = np.random.default_rng(31).standard_normal(shape).astype(np.float32)
+        a = ps.fkdip(d, 0.05)
+        monkeypatch.setenv("PWD_FK_SMEM", "0")
+        b = ps.fkdip(d, 0.05)
+        monkeypatch.delenv("PWD_FK_SMEM")
+        assert np.array_equal(a, b)
+        assert rel_l2(a, F.fkdip(d, 0.05)) <= TOL32
+
+
 def test_fkdip_zero_width_raises_like_the_reference(ps):
     with pytest.raises(ZeroDivisionError):
         ps.fkdip(np.zeros((8, 8), np.float32), 0.0)
