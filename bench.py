@@ -1405,6 +1405,20 @@ def main():
                               "unit": "TFLOP/s", "frac": ach / fpk,
                               "flops_per_sample": spray_flops_per_sample(wl),
                               "peak_source": "measured: pwd_fp32_fma_probe"}
+        # the same family against HBM: the DRAM bytes its launches move (the
+        # ncu capture's per-sample traffic, profiles/traffic.json) per second
+        try:
+            with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+                ent = json.load(fh).get(wl.name, {}).get(args.precision, {}).get("spray")
+        except (OSError, ValueError):
+            ent = None
+        if ent:
+            gbs = (ent["bytes_per_sample"] * fam_n["spray"] * wl.samples()
+                   / (fam_ms["spray"] / 1e3) / 1e9)
+            line["spray_fp32"]["dram_traffic"] = {
+                "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                "bytes_per_sample_per_launch": ent["bytes_per_sample"],
+                "source": "profiles/traffic.json (ncu DRAM bytes of the 128-section case)"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         kind = (None if wl.name in ("plain3d", "patches3d") else _ref_modules()) or "port"
         sample, desc = cpu_sample(wl, args.cpu_budget)

@@ -16,9 +16,9 @@
  *     a fixed device array of the library (below);
  *   - work is enqueued on `stream` (NULL = legacy default stream) and the
  *     call returns without synchronising; results are ready once the
- *     stream has been synchronised (pwd_sint2d, pwd_sint3d and
- *     pwd_soint2d_prec read values back and synchronise `stream` before
- *     they return);
+ *     stream has been synchronised (pwd_sint2d, pwd_sint3d,
+ *     pwd_soint2d_prec and pwd_soint2d_prec_batch read values back and
+ *     synchronise `stream` before they return);
  *   - results depend only on the arguments: calls on different streams
  *     with different workspaces may run concurrently.  The library's own
  *     process-wide state is limited to pwd_dip_static's scratch array
@@ -255,6 +255,18 @@ int pwd_soint2d_prec(const float *data, const float *mask, const float *dip1, co
                      float *out, int n1, int n2, int order, int niter, int hasmask,
                      int twoplane, void *workspace, size_t workspace_bytes,
                      pwd_stream_t stream);
+/* Many 2-D sections of uneven size (n3 = 1) at once, one CTA each: a loop
+ * of csoint2d(prec = 1) calls.  sections[k].offset places section k in
+ * data, mask and out, sections[k].out_offset its slopes in dip1 (and dip2)
+ * as pwd_dip_batch writes them; at most 65535 sections.  Every section
+ * gets the results of its own pwd_soint2d_prec call.  Synchronises
+ * `stream`. */
+size_t pwd_soint2d_prec_batch_workspace_size(const pwd_section *sections, int nsec, int order,
+                                             int twoplane);
+int pwd_soint2d_prec_batch(const float *data, const float *mask, const float *dip1,
+                           const float *dip2, float *out, const pwd_section *sections,
+                           int nsec, int order, int niter, int hasmask, int twoplane,
+                           void *workspace, size_t workspace_bytes, pwd_stream_t stream);
 
 /* Many patches of uneven size in one launch sequence (the batched
  * interpolation workflow): a loop of csoint3d calls over patches without

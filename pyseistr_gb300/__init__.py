@@ -8,6 +8,9 @@ sm_103a kernels of libpwd_gb300.so:
     somean3dc, somf3dc             3-D structure-oriented mean / median
     soint3dc                       3-D structure-oriented interpolation
     soint2dc                       2-D structure-oriented interpolation
+                                   (prec=1: preconditioned by plane-wave
+                                   integration; soint2dc_batch for many
+                                   sections at once)
     dipc, csomean2d, csomf2d,      the reference's low-level positional
     csomean3d, csomf3d, csoint3d,  entries
     csoint2d
@@ -64,6 +67,7 @@ from .api import (  # noqa: F401
     sint2dc,
     sint3dc,
     soint2dc,
+    soint2dc_batch,
     soint3dc,
     somean2dc,
     somean2dc_batch,

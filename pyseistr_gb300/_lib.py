@@ -66,6 +66,8 @@ SIGNATURES = {
     "pwd_soint3d": ([_P, _P, _P, _P, _P] + [_I] * 10 + [_F, _P, _S, _P], _I),
     "pwd_soint2d_prec_workspace_size": ([_I, _I, _I, _I], _S),
     "pwd_soint2d_prec": ([_P, _P, _P, _P, _P] + [_I] * 6 + [_P, _S, _P], _I),
+    "pwd_soint2d_prec_batch_workspace_size": ([_P, _I, _I, _I], _S),
+    "pwd_soint2d_prec_batch": ([_P, _P, _P, _P, _P, _P] + [_I] * 5 + [_P, _S, _P], _I),
     "pwd_soint3d_batch_workspace_size": ([_P, _I, _I], _S),
     "pwd_soint3d_batch": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P, _S, _P], _I),
 }

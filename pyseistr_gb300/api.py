@@ -365,6 +365,18 @@ def somf2dc_batch(sections, dips, ns, order, eps, option=1):
     return _unpack(out, shapes)
 
 
+def soint2dc_batch(sections, masks, dips, order=1, niter=100, hasmask=1, twoplane=0):
+    """soint2dc(..., prec=1) over a list of 2-D sections, their masks and
+    slopes ([n1, n2], or [n1, n2, 2] when twoplane), one CTA per section;
+    returns the list of results (each equal to its own call's)."""
+    shapes = [tuple(s.shape[:2]) for s in sections]
+    d1 = [d if not twoplane else d[:, :, 0] for d in dips]
+    d2 = _pack([d[:, :, 1] for d in dips]) if twoplane else None
+    out = D.soint2d_prec_batch(_pack(sections), _pack(masks), _pack(d1), d2, shapes, order,
+                               niter, hasmask, twoplane)
+    return _unpack(out, shapes)
+
+
 def dip_somean2d_batch(sections, niter=5, liter=10, order=2, rect=[10, 10, 1], ns=6, eps=0.01,
                        median=False, mixed=False):
     """Slope estimation followed by the structure-oriented mean (or median)

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
+#include <vector>
 
 #include "pwd_common.cuh"
 #include "pwd_gb300.h"
@@ -88,8 +89,9 @@ __host__ __device__ inline FacLayout fac_layout(int order, int n1) {
 // predict_lop uses) of every trace of both slope fields, then the factor
 // rearranged into the substitutions' row order.
 template <int NW>
-__global__ void k_prec_factor(PrecArgs a, ApCoef c) {
+__global__ void k_prec_factor(const PrecArgs* __restrict__ args, ApCoef c) {
   constexpr int NB = 2 * NW, RS = row_stride(NB);
+  const PrecArgs& a = args[blockIdx.y];  // one section per grid row
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (t >= (long)a.planes * a.n2) return;
   const int plane = (int)(t / a.n2), i2 = (int)(t % a.n2), n1 = a.n1;
@@ -435,7 +437,8 @@ __device__ bool scan(Cta& C, bool adj, ScanIo io, const float* in, float* outv) 
 
 // ps_solver_prec + ps_cgstep for one section per CTA.
 template <int NW>
-__global__ void __launch_bounds__(kPrecThreads) k_soint2d_prec(PrecArgs a) {
+__global__ void __launch_bounds__(kPrecThreads) k_soint2d_prec(const PrecArgs* __restrict__ args) {
+  const PrecArgs a = args[blockIdx.x];
   extern __shared__ __align__(16) float sm[];
   __shared__ __align__(8) unsigned long long bars[2];
   __shared__ double s_scal[4];  // alfa, beta (as floats), skip, stop
@@ -618,12 +621,78 @@ PrecLayout prec_layout(int n1, int n2, int order, int planes, size_t smem_cap) {
   return L;
 }
 
+// The sections of a call (one for pwd_soint2d_prec) and the shared-memory
+// plan of the longest traces, which serves every section.
+struct PrecBatch {
+  std::vector<pwd_section> secs;
+  int planes, order;
+  PrecLayout big;  // the plan of the largest n1
+};
+
+// Workspace: the per-section argument array, the failure flag, then every
+// section's factor store, vectors and scratch.  ws = nullptr only sizes it.
+size_t carve_prec(void* ws, const PrecBatch& B, std::vector<PrecArgs>* args, PrecArgs** dargs,
+                  int** status) {
+  Carver cv(ws);
+  const int nsec = (int)B.secs.size();
+  PrecArgs* da = cv.take<PrecArgs>(nsec);
+  int* st = cv.take<int>(1);
+  if (dargs) *dargs = da;
+  if (status) *status = st;
+  for (int k = 0; k < nsec; k++) {
+    const pwd_section& sc = B.secs[k];
+    const PrecLayout L = prec_layout(sc.n1, sc.n2, B.order, B.planes, smem_limit());
+    const long n = (long)sc.n1 * sc.n2;
+    PrecArgs a{};
+    a.fac = cv.take<float>(L.fac_floats);
+    a.p = cv.take<float>(n);
+    a.g = cv.take<float>(n);
+    a.rr = cv.take<float>(n);
+    a.gg = cv.take<float>(n);
+    a.S = cv.take<float>(n);
+    a.Ss = cv.take<float>(n);
+    a.vec = cv.take<float>((size_t)3 * B.planes * L.n1r);
+    a.known = cv.take<uint8_t>(n);
+    a.status = st;
+    a.n1 = sc.n1;
+    a.n2 = sc.n2;
+    a.planes = B.planes;
+    a.blk = L.blk;
+    a.cpy = L.cpy;
+    a.n1r = L.n1r;
+    a.smem_fac = B.big.nbuf;
+    a.smem_vec = B.big.smem_vec;
+    if (args) args->push_back(a);
+  }
+  return cv.size();
+}
+
+int prec_batch_make(const pwd_section* sections, int nsec, int order, int twoplane,
+                    PrecBatch& B) {
+  // (the factor launch takes a grid row per section: at most 65535)
+  if (!sections || nsec < 1 || nsec > 65535 || order < 1) return PWD_EINVAL;
+  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
+  B.secs.assign(sections, sections + nsec);
+  B.planes = twoplane ? 2 : 1;
+  B.order = order;
+  int n1max = 0, n2max = 0;
+  for (const pwd_section& s : B.secs) {
+    if (s.n1 < 2 || s.n2 < 1 || s.n3 != 1 || s.offset < 0 || s.out_offset < 0 ||
+        (long)s.n1 * s.n2 >= (1L << 31))
+      return PWD_EINVAL;
+    if (s.n1 > n1max) n1max = s.n1, n2max = s.n2;
+  }
+  B.big = prec_layout(n1max, n2max, order, B.planes, smem_limit());
+  return PWD_OK;
+}
+
 template <int NW>
-int prec_run(PrecArgs a, const PrecLayout& L, cudaStream_t st) {
+int prec_run(const PrecArgs* dargs, int nsec, int maxtr, const PrecLayout& L,
+             cudaStream_t st) {
   const ApCoef c = make_apcoef(NW);
-  const long nt = (long)a.planes * a.n2;
   PWD_KERNEL(PWD_FAM_SOINT, st,
-             (k_prec_factor<NW><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, c)));
+             (k_prec_factor<NW><<<dim3((unsigned)((maxtr + 127) / 128), (unsigned)nsec), 128, 0,
+                                  st>>>(dargs, c)));
   int rc = cuda_status(cudaGetLastError());
   if (rc != PWD_OK) return rc;
   rc = cuda_status(cudaFuncSetAttribute(k_soint2d_prec<NW>,
@@ -631,76 +700,97 @@ int prec_run(PrecArgs a, const PrecLayout& L, cudaStream_t st) {
                                         (int)L.smem_bytes));
   if (rc != PWD_OK) return rc;
   PWD_KERNEL(PWD_FAM_SOINT, st,
-             (k_soint2d_prec<NW><<<1, kPrecThreads, L.smem_bytes, st>>>(a)));
+             (k_soint2d_prec<NW><<<(unsigned)nsec, kPrecThreads, L.smem_bytes, st>>>(dargs)));
   return cuda_status(cudaGetLastError());
+}
+
+// Enqueues the batch, then reads back the failure flag (synchronising st).
+int prec_enqueue(const PrecBatch& B, const float* data, const float* mask, const float* dip1,
+                 const float* dip2, float* out, int niter, int hasmask, void* ws, size_t wsb,
+                 cudaStream_t st) {
+  const size_t need = carve_prec(nullptr, B, nullptr, nullptr, nullptr);
+  if (!ws || wsb < need || ((uintptr_t)ws & 255)) return PWD_EWORKSPACE;
+  std::vector<PrecArgs> args;
+  PrecArgs* dargs = nullptr;
+  int* status = nullptr;
+  carve_prec(ws, B, &args, &dargs, &status);
+  int maxtr = 0;
+  for (size_t k = 0; k < args.size(); k++) {
+    const pwd_section& s = B.secs[k];
+    PrecArgs& a = args[k];
+    a.din = data + s.offset;
+    a.mask = mask ? mask + s.offset : nullptr;
+    a.dip[0] = dip1 + s.out_offset;
+    a.dip[1] = (B.planes == 2 ? dip2 : dip1) + s.out_offset;
+    a.out = out + s.offset;
+    a.niter = niter;
+    a.hasmask = hasmask;
+    maxtr = std::max(maxtr, a.planes * a.n2);
+  }
+  int rc = cuda_status(cudaMemcpyAsync(dargs, args.data(), sizeof(PrecArgs) * args.size(),
+                                       cudaMemcpyHostToDevice, st));
+  if (rc == PWD_OK) rc = cuda_status(cudaMemsetAsync(status, 0, sizeof(int), st));
+  if (rc != PWD_OK) return rc;
+  const int nsec = (int)args.size();
+  switch (B.order) {
+    case 1: rc = prec_run<1>(dargs, nsec, maxtr, B.big, st); break;
+    case 2: rc = prec_run<2>(dargs, nsec, maxtr, B.big, st); break;
+    case 3: rc = prec_run<3>(dargs, nsec, maxtr, B.big, st); break;
+    default: rc = prec_run<4>(dargs, nsec, maxtr, B.big, st); break;
+  }
+  if (rc != PWD_OK) return rc;
+  // a bulk copy that timed out leaves a result incomplete: fail loudly (the
+  // synchronisation also keeps `args` alive until its copy has run)
+  int flag = 0;
+  rc = cuda_status(cudaMemcpyAsync(&flag, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (rc == PWD_OK) rc = cuda_status(cudaStreamSynchronize(st));
+  if (rc != PWD_OK) return rc;
+  return flag ? PWD_ECUDA : PWD_OK;
 }
 
 }  // namespace
 }  // namespace pwd
 
 extern "C" size_t pwd_soint2d_prec_workspace_size(int n1, int n2, int order, int twoplane) {
-  if (n1 < 2 || n2 < 1 || order < 1 || order > PWD_MAX_ORDER || (long)n1 * n2 >= (1L << 31))
-    return 0;
-  return pwd::prec_layout(n1, n2, order, twoplane ? 2 : 1, pwd::smem_limit()).total;
+  pwd_section sec{0, 0, n1, n2, 1};
+  pwd::PrecBatch B;
+  if (pwd::prec_batch_make(&sec, 1, order, twoplane, B) != PWD_OK) return 0;
+  return pwd::carve_prec(nullptr, B, nullptr, nullptr, nullptr);
 }
 
 extern "C" int pwd_soint2d_prec(const float* din, const float* mask, const float* dip1,
                                 const float* dip2, float* out, int n1, int n2, int order,
                                 int niter, int hasmask, int twoplane, void* workspace,
                                 size_t workspace_bytes, pwd_stream_t stream) {
-  using namespace pwd;
-  if (!din || !dip1 || !out || n1 < 2 || n2 < 1 || order < 1 || niter < 0 ||
-      (long)n1 * n2 >= (1L << 31))
-    return PWD_EINVAL;
+  if (!din || !dip1 || !out || niter < 0) return PWD_EINVAL;
   if (hasmask == 1 && !mask) return PWD_EINVAL;
   if (twoplane && !dip2) return PWD_EINVAL;
-  if (order > PWD_MAX_ORDER) return PWD_ENOTSUP;
-  const int planes = twoplane ? 2 : 1;
-  const PrecLayout L = prec_layout(n1, n2, order, planes, smem_limit());
-  if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255))
-    return PWD_EWORKSPACE;
-  cudaStream_t st = (cudaStream_t)stream;
-  const long n = (long)n1 * n2;
-  Carver cv(workspace);
-  PrecArgs a{};
-  a.din = din;
-  a.mask = mask;
-  a.dip[0] = dip1;
-  a.dip[1] = twoplane ? dip2 : dip1;
-  a.out = out;
-  a.fac = cv.take<float>(L.fac_floats);
-  a.p = cv.take<float>(n);
-  a.g = cv.take<float>(n);
-  a.rr = cv.take<float>(n);
-  a.gg = cv.take<float>(n);
-  a.S = cv.take<float>(n);
-  a.Ss = cv.take<float>(n);
-  a.vec = cv.take<float>((size_t)3 * planes * L.n1r);
-  a.known = cv.take<uint8_t>(n);
-  a.status = cv.take<int>(1);
-  a.n1 = n1;
-  a.n2 = n2;
-  a.niter = niter;
-  a.hasmask = hasmask;
-  a.planes = planes;
-  a.blk = L.blk;
-  a.cpy = L.cpy;
-  a.n1r = L.n1r;
-  a.smem_fac = L.nbuf;
-  a.smem_vec = L.smem_vec;
-  int rc = cuda_status(cudaMemsetAsync(a.status, 0, sizeof(int), st));
+  pwd_section sec{0, 0, n1, n2, 1};
+  pwd::PrecBatch B;
+  const int rc = pwd::prec_batch_make(&sec, 1, order, twoplane, B);
   if (rc != PWD_OK) return rc;
-  switch (order) {
-    case 1: rc = prec_run<1>(a, L, st); break;
-    case 2: rc = prec_run<2>(a, L, st); break;
-    case 3: rc = prec_run<3>(a, L, st); break;
-    default: rc = prec_run<4>(a, L, st); break;
-  }
+  return pwd::prec_enqueue(B, din, mask, dip1, dip2, out, niter, hasmask, workspace,
+                           workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t pwd_soint2d_prec_batch_workspace_size(const pwd_section* sections, int nsec,
+                                                        int order, int twoplane) {
+  pwd::PrecBatch B;
+  if (pwd::prec_batch_make(sections, nsec, order, twoplane, B) != PWD_OK) return 0;
+  return pwd::carve_prec(nullptr, B, nullptr, nullptr, nullptr);
+}
+
+extern "C" int pwd_soint2d_prec_batch(const float* data, const float* mask, const float* dip1,
+                                      const float* dip2, float* out,
+                                      const pwd_section* sections, int nsec, int order,
+                                      int niter, int hasmask, int twoplane, void* workspace,
+                                      size_t workspace_bytes, pwd_stream_t stream) {
+  if (!data || !dip1 || !out || niter < 0) return PWD_EINVAL;
+  if (hasmask == 1 && !mask) return PWD_EINVAL;
+  if (twoplane && !dip2) return PWD_EINVAL;
+  pwd::PrecBatch B;
+  const int rc = pwd::prec_batch_make(sections, nsec, order, twoplane, B);
   if (rc != PWD_OK) return rc;
-  // a bulk copy that timed out leaves the result incomplete: fail loudly
-  int flag = 0;
-  rc = cuda_status(cudaMemcpyAsync(&flag, a.status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  if (rc == PWD_OK) rc = cuda_status(cudaStreamSynchronize(st));
-  if (rc != PWD_OK) return rc;
-  return flag ? PWD_ECUDA : PWD_OK;
+  return pwd::prec_enqueue(B, data, mask, dip1, dip2, out, niter, hasmask, workspace,
+                           workspace_bytes, (cudaStream_t)stream);
 }

@@ -284,6 +284,28 @@ def soint3d_batch(data, mask, dips, shapes, order=1, niter=100, nj1=1, nj2=1, dr
     return out
 
 
+def soint2d_prec_batch(data, mask, dip1, dip2, shapes, order=1, niter=100, hasmask=1,
+                       twoplane=0, out=None, workspace=None):
+    """csoint2d(prec=1) of many 2-D sections packed one after another in
+    `data`, `mask` and `out`, their slopes `dip1` (and, when twoplane, the
+    second planes' `dip2`) packed the same way, as dip_batch returns them:
+    one CTA per section.  Synchronises the current stream."""
+    L = _lib.load()
+    tab, ntot, nout = section_table(shapes)
+    data = _as_flat(data, ntot, "data")
+    mask = _as_flat(mask, ntot, "mask") if mask is not None else None
+    dip1 = _as_flat(dip1, nout, "dip1")
+    dip2 = _as_flat(dip2, nout, "dip2") if twoplane else None
+    tp = int(bool(twoplane))
+    ws = _workspace(L.pwd_soint2d_prec_batch_workspace_size(tab, len(shapes), order, tp),
+                    data.device, workspace)
+    out = torch.empty_like(data) if out is None else out
+    _lib.check(L.pwd_soint2d_prec_batch(_ptr(data), _ptr(mask), _ptr(dip1), _ptr(dip2), _ptr(out),
+                                        tab, len(shapes), order, niter, int(hasmask), tp,
+                                        _ptr(ws), ws.numel(), _stream()), "soint2d_prec_batch")
+    return out
+
+
 FILTER_MEAN, FILTER_MEAN_ADJ, FILTER_MEDIAN = 1, 2, 3
 
 

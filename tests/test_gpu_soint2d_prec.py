@@ -108,3 +108,39 @@ def test_device_tensors(ps):
                     torch.from_numpy(dip).cuda(), order=m["order"], niter=m["niter"], prec=1,
                     verb=0)
     assert t.is_cuda and np.array_equal(t.cpu().numpy(), want)
+
+
+def test_batch_equals_one_call_per_section(ps):
+    """Sections of uneven size in one batch (the shared-memory plan of the
+    longest traces serves every section): every section gets its own call's
+    bits, for one and two slope planes."""
+    import torch
+    from pyseistr_gb300 import device as D
+
+    shapes = [(120, 30), (77, 19), (501, 40), (64, 64), (2, 9), (250, 12)]
+    for two in (0, 1):
+        secs = [_section(n1, n2, 40 + k, two) for k, (n1, n2) in enumerate(shapes)]
+        f = lambda a: torch.from_numpy(  # noqa: E731
+            np.concatenate([np.float32(x).reshape(-1, order="F") for x in a])).cuda()
+        data, mask = f([s[0] for s in secs]), f([s[1] for s in secs])
+        d1 = f([s[2][:, :, 0] if two else s[2] for s in secs])
+        d2 = f([s[2][:, :, 1] for s in secs]) if two else None
+        got = D.soint2d_prec_batch(data, mask, d1, d2, shapes, order=2, niter=15,
+                                   twoplane=two).cpu().numpy()
+        k = 0
+        for (din, m, dip), (n1, n2) in zip(secs, shapes):
+            want = ps.soint2dc(din, m, dip, order=2, niter=15, twoplane=two, prec=1, verb=0)
+            assert np.array_equal(got[k:k + n1 * n2], np.float32(want).reshape(-1, order="F"))
+            k += n1 * n2
+
+
+def test_soint2dc_batch_api(ps):
+    """The list form against the golden fixtures of one and two planes."""
+    for two in (0, 1):
+        cases = [c for c in CASES if c[0]["twoplane"] == two and c[0]["order"] == 2]
+        got = ps.soint2dc_batch([c[1] for c in cases], [c[2] for c in cases],
+                                [c[3] for c in cases], order=2,
+                                niter=cases[0][0]["niter"], twoplane=two)
+        for c, g in zip(cases, got):
+            if c[0]["niter"] == cases[0][0]["niter"] and c[0]["hasmask"] == 1:
+                assert np.array_equal(g, c[4])
