@@ -129,24 +129,6 @@ struct TraceFac {
   }
 };
 
-template <int NB>
-__device__ __forceinline__ void load_row(const float* __restrict__ p, float (&v)[NB]) {
-  if constexpr (NB == 2) {
-    const float2 x = *reinterpret_cast<const float2*>(p);
-    v[0] = x.x;
-    v[1] = x.y;
-  } else {
-#pragma unroll
-    for (int q = 0; q < (NB + 3) / 4; q++) {
-      const float4 x = reinterpret_cast<const float4*>(p)[q];
-      const float xs[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-      for (int e = 0; e < 4; e++)
-        if (4 * q + e < NB) v[4 * q + e] = xs[e];
-    }
-  }
-}
-
 // One substitution row: t -= ov[m] * W[m] for m = 0..NB-1 in order, then
 // the window of solved values shifts.  Rows whose band is shorter than NB
 // carry zero operands against the zero-initialised window, which leaves t
@@ -171,10 +153,78 @@ __device__ __forceinline__ float subst_row(float t, const float (&ov)[NB], float
 // row at NB = 4 on the GB300, against 52 with a load and a store per row).
 constexpr int kRows = 8;
 
-template <int NB>
-__device__ __forceinline__ void subst_pass(const float* __restrict__ ops, float* __restrict__ v,
-                                           int n1, bool down) {
+// Operand access of the substitution thread: generic loads and stores, or,
+// when the factor rows and the trace vectors are in shared memory (SH),
+// shared-space ones (about a third fewer cycles a row: a generic access
+// pays for the address-space check).  The volatile forms keep program
+// order, which already loads a block before solving and storing it.
+template <bool SH>
+struct SubMem {
+  const float* base;
+  unsigned sbase;
+  __device__ __forceinline__ explicit SubMem(const float* p)
+      : base(p), sbase(SH ? (unsigned)__cvta_generic_to_shared(p) : 0u) {}
+  __device__ __forceinline__ float ld(long k) const {
+    if constexpr (SH) {
+      float x;
+      asm volatile("ld.shared.f32 %0, [%1];" : "=f"(x) : "r"(sbase + (unsigned)k * 4u));
+      return x;
+    } else {
+      return base[k];
+    }
+  }
+  __device__ __forceinline__ float2 ld2(long k) const {
+    if constexpr (SH) {
+      float2 x;
+      asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(x.x), "=f"(x.y)
+                   : "r"(sbase + (unsigned)k * 4u));
+      return x;
+    } else {
+      return *reinterpret_cast<const float2*>(base + k);
+    }
+  }
+  __device__ __forceinline__ float4 ld4(long k) const {
+    if constexpr (SH) {
+      float4 x;
+      asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                   : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w)
+                   : "r"(sbase + (unsigned)k * 4u));
+      return x;
+    } else {
+      return *reinterpret_cast<const float4*>(base + k);
+    }
+  }
+  __device__ __forceinline__ void st(long k, float x) const {
+    if constexpr (SH) {
+      asm volatile("st.shared.f32 [%0], %1;" ::"r"(sbase + (unsigned)k * 4u), "f"(x) : "memory");
+    } else {
+      const_cast<float*>(base)[k] = x;
+    }
+  }
+};
+
+template <int NB, bool SH>
+__device__ __forceinline__ void load_row_m(const SubMem<SH>& m, long k, float (&v)[NB]) {
+  if constexpr (NB == 2) {
+    const float2 x = m.ld2(k);
+    v[0] = x.x;
+    v[1] = x.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < (NB + 3) / 4; q++) {
+      const float4 x = m.ld4(k + 4 * q);
+      const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (4 * q + e < NB) v[4 * q + e] = xs[e];
+    }
+  }
+}
+
+template <int NB, bool DOWN, bool SH>
+__device__ __forceinline__ void subst_pass(const float* ops_p, float* v_p, int n1) {
   constexpr int RS = row_stride(NB);
+  const SubMem<SH> ops(ops_p), v(v_p);
   float W[NB];
 #pragma unroll
   for (int m = 0; m < NB; m++) W[m] = 0.f;
@@ -183,34 +233,45 @@ __device__ __forceinline__ void subst_pass(const float* __restrict__ ops, float*
     float ov[kRows][NB], t[kRows];
 #pragma unroll
     for (int r = 0; r < kRows; r++) {
-      const int k = down ? n1 - 1 - (q * kRows + r) : q * kRows + r;
-      load_row<NB>(ops + (long)k * RS, ov[r]);
-      t[r] = v[k];
+      const int k = DOWN ? n1 - 1 - (q * kRows + r) : q * kRows + r;
+      load_row_m<NB, SH>(ops, (long)k * RS, ov[r]);
+      t[r] = v.ld(k);
     }
 #pragma unroll
     for (int r = 0; r < kRows; r++) t[r] = subst_row<NB>(t[r], ov[r], W);
 #pragma unroll
-    for (int r = 0; r < kRows; r++) v[down ? n1 - 1 - (q * kRows + r) : q * kRows + r] = t[r];
+    for (int r = 0; r < kRows; r++) v.st(DOWN ? n1 - 1 - (q * kRows + r) : q * kRows + r, t[r]);
   }
   for (int j = nblk * kRows; j < n1; j++) {
-    const int k = down ? n1 - 1 - j : j;
+    const int k = DOWN ? n1 - 1 - j : j;
     float ov[NB];
-    load_row<NB>(ops + (long)k * RS, ov);
-    v[k] = subst_row<NB>(v[k], ov, W);
+    load_row_m<NB, SH>(ops, (long)k * RS, ov);
+    v.st(k, subst_row<NB>(v.ld(k), ov, W));
   }
 }
 
+// sh: the factor rows and the trace vectors are in shared memory.
 template <int NB>
-__device__ void banded_solve_all(const TraceFac* f, float* const* b, int P) {
+__device__ void banded_solve_all(const TraceFac* f, float* const* b, int P, bool sh) {
   const int n1 = f[0].n1;
   const bool solver = (threadIdx.x & 31) == 0 && (int)(threadIdx.x >> 5) < P;
   const int pl = threadIdx.x >> 5;
-  if (solver) subst_pass<NB>(f[pl].fo, b[pl], n1, false);
+  if (solver) {
+    if (sh)
+      subst_pass<NB, false, true>(f[pl].fo, b[pl], n1);
+    else
+      subst_pass<NB, false, false>(f[pl].fo, b[pl], n1);
+  }
   __syncthreads();
   for (int q = 0; q < P; q++)
     for (int k = threadIdx.x; k < n1; k += blockDim.x) b[q][k] = __fdiv_rn(b[q][k], f[q].d[k]);
   __syncthreads();
-  if (solver) subst_pass<NB>(f[pl].bo, b[pl], n1, true);
+  if (solver) {
+    if (sh)
+      subst_pass<NB, true, true>(f[pl].bo, b[pl], n1);
+    else
+      subst_pass<NB, true, false>(f[pl].bo, b[pl], n1);
+  }
 }
 
 // pwd_set forward (:1139-1157) into tv: tmp[i] = sum_j a[j][i] tt[i+j-nw]
@@ -398,7 +459,7 @@ __device__ bool scan(Cta& C, bool adj, ScanIo io, const float* in, float* outv) 
         __syncthreads();
         for (int pl = 0; pl < P; pl++) set_fwd_out<NW>(f[pl], C.tt[pl], C.tv[pl], C.rhs[pl]);
         __syncthreads();
-        banded_solve_all<NB>(f, C.rhs, P);
+        banded_solve_all<NB>(f, C.rhs, P, C.nbuf > 0 && a.smem_vec);
         // the solved trace is the next step's tt
         for (int pl = 0; pl < P; pl++) {
           float* t = C.tt[pl];
@@ -409,7 +470,7 @@ __device__ bool scan(Cta& C, bool adj, ScanIo io, const float* in, float* outv) 
     } else {
       // tt = predict_step'(tt) per plane, then tt2 += y; tmp = 0 + tt2;
       // tt1 += tmp; x = 0 + tt1 (one plane: tt += y; x = 0 + tt)
-      banded_solve_all<NB>(f, C.tt, P);
+      banded_solve_all<NB>(f, C.tt, P, C.nbuf > 0 && a.smem_vec);
       __syncthreads();
       for (int pl = 0; pl < P; pl++) set_adj_tmp<NW>(f[pl], C.tt[pl], C.tv[pl]);
       __syncthreads();
