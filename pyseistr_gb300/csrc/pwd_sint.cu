@@ -98,24 +98,24 @@ __global__ void __launch_bounds__(kSintThreads) k_sint_cross(const float* __rest
 }
 
 struct SintLayout {
-  size_t vec_bytes, part_bytes, smooth_bytes, total;
+  size_t vec_bytes, part_bytes, smooth_bytes, cross_bytes, total;
 };
 
 // 8 CG vectors, for csint3d 4 more (itmp, itmp2, xtmp and the transposed
-// crossline slope), the dot partials and the smoothing's workspace.
+// crossline slope), the dot partials and the smoothing's workspaces: one
+// for the inline smoothing and, in 3-D, one for the crossline smoothing, so
+// that each keeps the factor store of its own slope field across calls.
 SintLayout sint_layout(int n1, int n2, int n3, int ns1, int ns2, int order1, int order2,
                        bool three) {
   SintLayout l{};
   const long n = (long)n1 * n2 * n3;
   l.vec_bytes = ((sizeof(float) * (size_t)n + 255) & ~(size_t)255);
   l.part_bytes = ((sizeof(double) * kSintDotBlocks + 255) & ~(size_t)255);
-  l.smooth_bytes = smooth2_workspace(n1, n2, n3, ns1, order1);
-  if (three && l.smooth_bytes) {
-    const size_t c = smooth2_workspace(n1, n3, n2, ns2, order2);
-    l.smooth_bytes = c ? (c > l.smooth_bytes ? c : l.smooth_bytes) : 0;
-  }
+  l.smooth_bytes = (smooth2_workspace(n1, n2, n3, ns1, order1) + 255) & ~(size_t)255;
+  l.cross_bytes = three ? (smooth2_workspace(n1, n3, n2, ns2, order2) + 255) & ~(size_t)255 : 0;
+  const bool ok = l.smooth_bytes && (!three || l.cross_bytes);
   const int nvec = three ? 12 : 8;
-  l.total = l.smooth_bytes ? nvec * l.vec_bytes + l.part_bytes + l.smooth_bytes : 0;
+  l.total = ok ? nvec * l.vec_bytes + l.part_bytes + l.smooth_bytes + l.cross_bytes : 0;
   return l;
 }
 
@@ -129,8 +129,10 @@ struct GpuOps {
   int ns1, ns2, order1, order2;
   float eps;                // the smoothing's eps (csint2d's / csint3d's eps argument)
   float *itmp, *itmp2, *xtmp;
-  void* sws;
+  void* sws;  // inline smoothing workspace
   size_t swsb;
+  void* cws;  // crossline smoothing workspace (3-D)
+  size_t cwsb;
   double* part;
   std::vector<double> host;
   cudaStream_t st;
@@ -161,19 +163,21 @@ struct GpuOps {
   int conj(float a) { return pass(kConj, a); }
   int step(float a) { return pass(kStep, a); }
   // primitives of the 3-D sequence
-  // The 2-D smoothing calls all use one slope field: after the first, each
-  // reuses the factor store and w1 it left in the smoothing workspace.  The
-  // 3-D sequence alternates two slope fields in that workspace, so every
-  // call there factors afresh.
-  bool factored = false;
+  // Each smoothing (inline, and crossline in 3-D) always runs on one slope
+  // field in its own workspace: after its first call, each call reuses the
+  // factor store and w1 the previous one left there.
+  bool factored = false, cfactored = false;
   int inline_(int mode, float* in, float* out) {
     const int rc = smooth2_run(in, dipi, out, n1, n2, n3, ns1, order1, eps, mode, sws, swsb, st,
-                               !three && factored ? 1 : 0);
+                               factored ? 1 : 0);
     if (rc == PWD_OK) factored = true;
     return rc;
   }
   int crossline(int mode, float* in, float* out) {
-    return smooth2_run(in, xd, out, n1, n3, n2, ns2, order2, eps, mode, sws, swsb, st, 0);
+    const int rc = smooth2_run(in, xd, out, n1, n3, n2, ns2, order2, eps, mode, cws, cwsb, st,
+                               cfactored ? 1 : 0);
+    if (rc == PWD_OK) cfactored = true;
+    return rc;
   }
   int cross(const float* a, float* b, int to, int sum) {
     PWD_KERNEL(PWD_FAM_CG, st,
@@ -259,6 +263,8 @@ int sint_run(const float* din, const float* dipi, const float* dipx, const float
   ops.part = (double*)(base + nvec * l.vec_bytes);
   ops.sws = base + nvec * l.vec_bytes + l.part_bytes;
   ops.swsb = l.smooth_bytes;
+  ops.cws = three ? base + nvec * l.vec_bytes + l.part_bytes + l.smooth_bytes : nullptr;
+  ops.cwsb = l.cross_bytes;
   ops.host.assign(kSintDotBlocks, 0.);
   const long blocks = (n + kSintThreads - 1) / kSintThreads;
   ops.grid = (unsigned)(blocks < 152L * 8 * 16 ? blocks : 152L * 8 * 16);
