@@ -157,19 +157,33 @@ __global__ void k_ap3_coef(SoArrays A, SoBatch b, ApCoef c) {
   }
 }
 
+__device__ void cg3_scalars(SolveScalars* S, const dvec<6>& tt, int iter);
+
 // yy (+)= L xx, yy = [inline residual ; crossline residual] (allpass3_lop
-// forward, :662-695).
-template <int NW>
-__global__ void k_ap3_fwd(const float* __restrict__ xxb, float* __restrict__ yyb, SoArrays A,
-                          SoBatch b, int add, int use_done) {
-  const TileRange tr = tile_range(b, blockIdx.x);
+// forward, :662-695).  With DOTS (yy = gg = L g inside the CG loop) the
+// kernel also accumulates gg.gg, Ss.Ss, gg.Ss, gg.rr, Ss.rr, rr.rr over the
+// patch's 2n data space, and the last tile of the patch runs the tolerance
+// test of ps_solver (:1086-1100) and ps_cgstep's scalar part (:835-866).
+// The dot products are float-float per thread (exact products, ~2^-45 sums),
+// double across threads and tiles: no per-sample FP64 arithmetic.
+template <int NW, bool DOTS>
+__global__ void __launch_bounds__(kTileThreads, 4) k_ap3_fwd(const float* __restrict__ xxb,
+                                                          float* __restrict__ yyb, SoArrays A,
+                                                          SoBatch b, int add, int use_done,
+                                                          int iter) {
+  const int t = blockIdx.x;
+  const TileRange tr = tile_range(b, t);
   const SecDesc& s = b.secs[tr.sec];
   if (use_done && b.S[tr.sec].done) return;
   const Op3 g = geometry(b, s);
   constexpr int NA = 2 * NW + 1;
   const float* xx = xxb + s.off;
   float* yy = yyb + 2 * s.off;
+  ffacc c0, c1, c2, c3, c4, c5;
+  const float *Ssv = A.Ss + 2 * s.off, *rrv = A.rr + 2 * s.off;
   for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+    float yo[2];
+#pragma unroll 1
     for (int part = 0; part < 2; part++) {
       float* y = yy + (part == 0 ? 0 : g.n);
       float acc = add ? y[i] : 0.f;
@@ -196,7 +210,28 @@ __global__ void k_ap3_fwd(const float* __restrict__ xxb, float* __restrict__ yyb
           acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(xa[iw], xb[iw]), fv[iw]));
       }
       y[i] = acc;
+      yo[part] = acc;
     }
+    if (DOTS) {
+#pragma unroll
+      for (int part = 0; part < 2; part++) {
+        const long k = i + part * s.n;
+        const float a = yo[part], sv = Ssv[k], r = rrv[k];
+        c0.add_prod(a, a);
+        c1.add_prod(sv, sv);
+        c2.add_prod(a, sv);
+        c3.add_prod(a, r);
+        c4.add_prod(sv, r);
+        c5.add_prod(r, r);
+      }
+    }
+  }
+  if (DOTS) {
+    SolveScalars* S = b.S + tr.sec;
+    dvec<6> acc = {{c0.value(), c1.value(), c2.value(), c3.value(), c4.value(), c5.value()}};
+    dvec<6> tt;
+    if (so_sum_last<6>(acc, b, t, s, &S->cnt[1], tt) && threadIdx.x == 0)
+      cg3_scalars(S, tt, iter);
   }
 }
 
@@ -335,34 +370,9 @@ __global__ void k_max_shift(SoArrays A, SoBatch b) {
   atomicMax(&b.S[tr.sec].dmax, best);
 }
 
-// gg.gg, Ss.Ss, gg.Ss, gg.rr, Ss.rr, rr.rr over the patch's 2n data space;
-// the last tile runs the tolerance test of ps_solver (:1086-1100) and
-// ps_cgstep's scalar part (:835-866).
-__global__ void k_cg3_dots(SoArrays A, SoBatch b, int iter) {
-  const int t = blockIdx.x;
-  const TileRange tr = tile_range(b, t);
-  const SecDesc& s = b.secs[tr.sec];
-  SolveScalars* S = b.S + tr.sec;
-  if (S->done) return;
-  // float-float per-thread accumulation (exact products, ~2^-45 sums),
-  // double across threads and tiles: no per-sample FP64 arithmetic
-  ffacc c0, c1, c2, c3, c4, c5;
-  const float *gg = A.gg + 2 * s.off, *Ss = A.Ss + 2 * s.off, *rr = A.rr + 2 * s.off;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
-#pragma unroll
-    for (int part = 0; part < 2; part++) {
-      const long k = i + part * s.n;
-      const float a = gg[k], sv = Ss[k], r = rr[k];
-      c0.add_prod(a, a);
-      c1.add_prod(sv, sv);
-      c2.add_prod(a, sv);
-      c3.add_prod(a, r);
-      c4.add_prod(sv, r);
-      c5.add_prod(r, r);
-    }
-  dvec<6> acc = {{c0.value(), c1.value(), c2.value(), c3.value(), c4.value(), c5.value()}};
-  dvec<6> tt;
-  if (!(so_sum_last<6>(acc, b, t, s, &S->cnt[1], tt) && threadIdx.x == 0)) return;
+// The tolerance test of ps_solver (:1086-1100) and ps_cgstep's scalar part
+// (:835-866) from the patch's six dot products.
+__device__ void cg3_scalars(SolveScalars* S, const dvec<6>& tt, int iter) {
   const float TOL = 1.e-12f, EPS = 1.e-12f;
   float dpr, dpg;
   if (iter == 0) {
@@ -604,15 +614,16 @@ int soint3_run(const SoArrays& A, const SoBatch& b, int niter, cudaStream_t st) 
   PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_coef<NW><<<gt, bs, 0, st>>>(A, b, make_apcoef(NW)));
   if (b.drift) PWD_KERNEL(PWD_FAM_SOINT, st, k_max_shift<<<gt, bs, 0, st>>>(A, b));
   PWD_KERNEL(PWD_FAM_SOINT, st, k_init<<<gt, bs, 0, st>>>(A, b));
-  PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.x, A.rr, A, b, 1, 0));
+  PWD_KERNEL(PWD_FAM_SOINT, st,
+             (k_ap3_fwd<NW, false><<<gt, bs, 0, st>>>(A.x, A.rr, A, b, 1, 0, 0)));
   PWD_KERNEL(PWD_FAM_SOINT, st, k_rr0<<<gt, bs, 0, st>>>(A, b));
   for (int iter = 0; iter < niter; iter++) {
     if (b.drift)
       PWD_KERNEL(PWD_FAM_SOINT, st, (k_ap3_adj<NW, true><<<gt, bs, 0, st>>>(A, b)));
     else
       PWD_KERNEL(PWD_FAM_SOINT, st, (k_ap3_adj<NW, false><<<gt, bs, 0, st>>>(A, b)));
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_ap3_fwd<NW><<<gt, bs, 0, st>>>(A.g, A.gg, A, b, 0, 1));
-    PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_dots<<<gt, bs, 0, st>>>(A, b, iter));
+    PWD_KERNEL(PWD_FAM_SOINT, st,
+               (k_ap3_fwd<NW, true><<<gt, bs, 0, st>>>(A.g, A.gg, A, b, 0, 1, iter)));
     PWD_KERNEL(PWD_FAM_SOINT, st, k_cg3_update<<<gt, bs, 0, st>>>(A, b, iter));
   }
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
