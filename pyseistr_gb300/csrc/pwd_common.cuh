@@ -471,7 +471,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 
 // ---------------------------------------------------------------------------
 // Packed FP32 pairs (add / mul / fma .rn.f32x2): two independent IEEE
-// operations per instruction, each rounded as its scalar form.
+// operations per instruction, each rounded as its scalar form.  A packed
+// multiply whose result feeds a packed add can be contracted into a packed
+// FMA by the compiler in spite of the .rn qualifiers and -fmad=false
+// (measured: a float-float dot product accumulated on packed pairs came out
+// as the FMA-accumulated sum), so these are used only where no product
+// feeds an addition directly; the scalar __fmul_rn / __fadd_rn are never
+// contracted.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long f2_bits(float2 a) {
   return ((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x);
@@ -494,32 +500,6 @@ __device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
   return f2_from(d);
 }
-__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
-  unsigned long long d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_from(d);
-}
-
-// Two ffacc accumulators in the lanes of packed pairs: the x and y lanes
-// accumulate two streams of products with ffacc's operations (exact
-// product error by FMA, TwoSum), at half the instructions.
-struct ffacc2 {
-  float2 h = {0.f, 0.f}, l = {0.f, 0.f};
-  __device__ __forceinline__ void add_prod(float2 a, float2 b) {
-    const float2 p = mul2_rn(a, b);
-    const float2 pe = fma2_rn(a, b, sub2_rn(make_float2(0.f, 0.f), p));
-    const float2 s = add2_rn(h, p);
-    const float2 bb = sub2_rn(s, h);
-    const float2 e = add2_rn(sub2_rn(h, sub2_rn(s, bb)), sub2_rn(p, bb));
-    h = s;
-    l = add2_rn(l, add2_rn(e, pe));
-  }
-  // both lanes' sums
-  __device__ __forceinline__ double value() const {
-    return ((double)h.x + (double)l.x) + ((double)h.y + (double)l.y);
-  }
-};
-
 // ---------------------------------------------------------------------------
 // Workspace carving (256-byte aligned slices of the caller's buffer).
 // ---------------------------------------------------------------------------

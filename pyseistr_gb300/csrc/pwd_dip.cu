@@ -763,7 +763,7 @@ struct SmParams {
   const float* gpc;  // gp, read at the output sample by SM_OUT_CG2 of axis 2
   const float* xo;  // x before the iteration (read) and after it (written):
   float* xn;        // double-buffered, a segment's halo reads other tiles' x
-  const int4* c0map;  // axis-0 tiles: section, first trace, first sample, lines << 16 | length
+  const int4* c0map;  // axis-0 tiles, two entries each (k_conv0_map)
   int c0buf;          // floats per axis-0 staging buffer
   int tma;            // axis-0 tiles staged by bulk copies (else 4-byte cp.async)
   int b2;             // rows of an axis-1 strip
@@ -935,7 +935,11 @@ __host__ __device__ inline int conv0_tiles(int n1, long ntr, int h0) {
 // last window's float4 reads run up to 10 floats past its line.
 __host__ __device__ inline int conv0_buffer(int h0) { return (kC0Seg + 2 * h0 + 24 + 3) & ~3; }
 
-// The tile table of the axis-0 pass (one thread per tile).
+// The tile table of the axis-0 pass (one thread per tile): two int4 per
+// tile, {section, n1, first sample, lines << 16 | length} and {first element
+// of the tile's first trace (64 bits, low word first), section is 2-D, 0},
+// so that a block finds everything it needs to start its copies in one
+// 32-byte load.
 __global__ void k_conv0_map(const SecDesc* secs, int nsec, int ntiles, int h0, int4* map) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
@@ -956,7 +960,21 @@ __global__ void k_conv0_map(const SecDesc* secs, int nsec, int ntiles, int h0, i
     o1 = 0;
     len = n1;
   }
-  map[t] = make_int4(si, tr0, o1, (nl << 16) | len);
+  const unsigned long long so = (unsigned long long)(s.off + (long)tr0 * n1);
+  map[2 * t] = make_int4(si, n1, o1, (nl << 16) | len);
+  map[2 * t + 1] = make_int4((int)(unsigned)so, (int)(unsigned)(so >> 32), s.n3 == 1, 0);
+}
+
+// A stopped section keeps its x and r: the CG input pass carries x to the
+// new buffer.
+template <int NT>
+__device__ __noinline__ void conv0_carry(const SmParams& q, long so, int n1, int o1, int nl,
+                                         int len) {
+  for (int k = 0; k < nl; k++)
+    for (int i = threadIdx.x; i < len; i += NT) {
+      const long e = so + (long)k * n1 + o1 + i;
+      q.xn[e] = q.xo[e];
+    }
 }
 
 template <int IN, int NB0>
@@ -967,25 +985,21 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
   // num, sx (SM_IN_CG1); with bulk staging the lines come first, then one
   // staging buffer per array
   extern __shared__ __align__(16) float buf[];
-  const int4 tm = q.c0map[blockIdx.x];
-  const SecDesc& s = b.secs[tm.x];
-  if (!sm_selected(q.sel, s)) return;
+  const int4 tm = q.c0map[2 * blockIdx.x], tx = q.c0map[2 * blockIdx.x + 1];
+  if (!(q.sel == 0 || (q.sel == 1) == (tx.z != 0))) return;  // sm_selected
   DipScalars* S = b.S + tm.x;
-  const int n1 = s.n1;
+  const int n1 = tm.y;
   const int h0 = (NB0 > 0 ? NB0 : q.nb0) - 1;
   const int stride = conv0_stride(n1, h0);
   const int o1 = tm.z, nl = tm.w >> 16, len = tm.w & 0xffff;
   // indices below are relative to the tile's first trace (a section holds
   // fewer than 2^31 samples)
-  const long so = s.off + (long)tm.y * n1;
-  if (S->cg_done) {
-    // a stopped section keeps its x and r: carry them to the new buffers
-    if (IN == SM_IN_CG1)
-      for (int k = 0; k < nl; k++)
-        for (int i = threadIdx.x; i < len; i += NT) {
-          const long e = so + k * n1 + o1 + i;
-          q.xn[e] = q.xo[e];
-        }
+  const long so = (long)(((unsigned long long)(unsigned)tx.y << 32) | (unsigned)tx.x);
+  // the section's stop flag: with bulk staging it is tested once the
+  // copies are under way, so that its load and theirs overlap
+  const int done = S->cg_done;
+  if (!q.tma && done) {
+    if (IN == SM_IN_CG1) conv0_carry<NT>(q, so, n1, o1, nl, len);
     return;
   }
   const int w = len + 2 * h0;  // staged samples per line
@@ -1032,6 +1046,10 @@ __global__ void __launch_bounds__(conv0_threads<IN>()) k_conv0(DipArrays a, DipB
       s_ok = ok;
     }
     __syncthreads();
+    if (done) {
+      if (IN == SM_IN_CG1) conv0_carry<NT>(q, so, n1, o1, nl, len);
+      return;
+    }
     if (!s_ok) return;
     const float st = stepped ? __double2float_rn(S->step) : 0.f;
     for (int k = 0; k < nl; k++) {
@@ -1517,7 +1535,7 @@ DipWork carve_dip(void* ws, const DipLayout& L, int nsec, bool has_mask, size_t*
   w.a.tri = mixed ? nullptr : cv.take<float>(L.scr_total);
   w.a.x2 = mixed ? cv.take<float>(n) : nullptr;
   w.a.t2 = mixed && L.any3d ? cv.take<float>(n) : nullptr;
-  w.a.c0map = mixed ? cv.take<int4>(L.nctiles) : nullptr;
+  w.a.c0map = mixed ? cv.take<int4>(2 * (size_t)L.nctiles) : nullptr;
   w.m0 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.m1 = has_mask ? cv.take<uint8_t>(n) : nullptr;
   w.secs = cv.take<SecDesc>(nsec);
