@@ -409,11 +409,16 @@ def family_bytes(wl, launches, mixed=False):
         elif fam == "cg" and mixed and d["rect"][2] > 1 and wl.name in ("plain3d", "patches3d"):
             # cubes, per CG iteration: axis 0 with the step and gradient 24
             # (read x, W, num, sx; write x, t; 20 first), axis 1 8, axis 2
-            # with gp 20 (12 first), axis 0 8, axis 1 8, axis 2 with the
+            # with gp 20 (12 first), axes 0 and 1 of gp 8 in one pass (two
+            # passes of 8 where the fused pass is not used), axis 2 with the
             # update 28 (read t, gp, W, sp, sx; write sp, sx; 20 first);
             # scale 28 and final step 12 per Gauss-Newton iteration
-            per_outer = 28 + (20 + 8 + 12 + 8 + 8 + 20) + (liter - 1) * 96 + 12
-            bps = per_outer / (2.0 + 6.0 * liter)
+            r0, r1 = d["rect"][0], d["rect"][1]
+            fused = (r0 == r1 and r0 in (5, 10) and os.environ.get("PWD_CONV01") != "0"
+                     and os.environ.get("PWD_CONV1_PAIR") != "1")
+            gp01, k = (8, 5) if fused else (16, 6)
+            per_outer = 28 + (20 + 8 + 12 + gp01 + 20) + (liter - 1) * (80 + gp01) + 12
+            bps = per_outer / (2.0 + k * liter)
         elif fam == "cg" and mixed:
             # per CG iteration: axis 0 with the step and gradient 24 (read
             # x, W, num, sx; write x, t; 20 first), axis 1 with gp 20 (12

@@ -1305,6 +1305,101 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
   }
 }
 
+// Cubes: the axis-0 pass of gp fused into the axis-1 pass that consumes it
+// (gp -> tmp -> t2, k_conv0<SM_IN_ARR> then k_conv1<SM_OUT_ARR>), for radii
+// compiled on both axes.  Each staged row of the strip is the input's row
+// segment of kSmStrip + 2 (NB0 - 1) samples (the strip's columns and the
+// axis-0 halo, mirrored at the trace ends); each thread forms its column's
+// axis-0 value from the segment in k_conv0's order of operations, so the
+// outputs are those of the two separate passes, without the intermediate
+// array's write and read.  The block waits for every row (threads read one
+// another's copies), and a slot is refilled only after the barrier that
+// follows its last reads.  (The same fusion into the conjugate-update pass
+// of 2-D sections measured slower than the separate passes.)
+template <int NB0>
+__host__ __device__ constexpr int conv01_seg() {
+  return (kSmStrip + 2 * (NB0 - 1) + 3) & ~3;
+}
+template <int NB0, int NB1>
+__global__ void __launch_bounds__(kSmStrip, 16) k_conv01(DipArrays a, DipBatch b, SmParams q) {
+  extern __shared__ float sm[];
+  constexpr int H0 = NB0 - 1, H1 = NB1 - 1, RING = 2 * H1 + 1, SEG = conv01_seg<NB0>();
+  const int t = blockIdx.x;
+  const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
+  const SecDesc& s = b.secs[si];
+  if (!sm_selected(q.sel, s)) return;
+  if (b.S[si].cg_done) return;
+  const int n1 = s.n1, n2 = s.n2;
+  const int b2 = q.b2;
+  const int nt1 = (n1 + kSmStrip - 1) / kSmStrip, nt2 = (n2 + b2 - 1) / b2;
+  const int lt = t - s.ftile0;
+  const int t1 = lt % nt1, t2 = (lt / nt1) % nt2, i3 = lt / (nt1 * nt2);
+  const int o2 = t2 * b2;
+  const int rows = min(b2, n2 - o2);
+  const long so = s.off + (long)i3 * n1 * n2;
+  const int j = threadIdx.x;
+  const int c0 = t1 * kSmStrip;  // the strip's first column
+  const int g1 = c0 + j;
+  const bool colok = g1 < n1;
+  // this thread's samples of the row segment: c0 - H0 + j and, for the
+  // halo, c0 - H0 + kSmStrip + j (mirrored into the trace)
+  const int e0 = mirror_idx(c0 - H0 + j, n1);
+  const bool two = j < 2 * H0;
+  const int e1 = two ? mirror_idx(c0 - H0 + kSmStrip + j, n1) : 0;
+  const int nsteps = rows + 2 * H1;
+  auto issue = [&](int step) {
+    if (step < nsteps) {
+      float* sg = sm + (step % kSmStages) * SEG;
+      const float* row = q.in + so + (long)mirror_idx(o2 - H1 + step, n2) * n1;
+      cp_async4(sg + j, row + e0);
+      if (two) cp_async4(sg + kSmStrip + j, row + e1);
+    }
+    cp_async_commit();
+  };
+  // the axis-0 value of this thread's column on the step's row
+  auto take = [&](int step) -> float {
+    cp_async_wait<kSmStages - 2>();
+    __syncthreads();
+    issue(step + kSmStages - 1);
+    const float* v = sm + (step % kSmStages) * SEG + j + H0;  // centred on the column
+    float acc = __fmul_rn(tri_tap_c<NB0>(0), v[0]), acc2 = 0.f;
+#pragma unroll
+    for (int kk = 1; kk <= H0; kk++) {
+      const float pr = __fadd_rn(v[-kk], v[kk]);
+      if (kk & 1)
+        acc2 = __fmaf_rn(tri_tap_c<NB0>(kk), pr, acc2);
+      else
+        acc = __fmaf_rn(tri_tap_c<NB0>(kk), pr, acc);
+    }
+    return __fadd_rn(acc, acc2);
+  };
+  for (int k = 0; k < kSmStages - 1; k++) issue(k);
+  float rg[RING];
+  for (int step0 = 0; step0 < nsteps; step0 += RING) {
+#pragma unroll
+    for (int u = 0; u < RING; u++) {
+      const int step = step0 + u;
+      if (step < nsteps) {
+        rg[u] = take(step);
+        if (step >= 2 * H1) {
+          float acc = __fmul_rn(tri_tap_c<NB1>(0), rg[(u - H1 + RING) % RING]), acc2 = 0.f;
+#pragma unroll
+          for (int k = 1; k <= H1; k++) {
+            const float pr = __fadd_rn(rg[(u - H1 - k + 2 * RING) % RING],
+                                       rg[(u - H1 + k + RING) % RING]);
+            if (k & 1)
+              acc2 = __fmaf_rn(tri_tap_c<NB1>(k), pr, acc2);
+            else
+              acc = __fmaf_rn(tri_tap_c<NB1>(k), pr, acc);
+          }
+          if (colok) q.out[so + (long)(o2 + step - 2 * H1) * n1 + g1] = __fadd_rn(acc, acc2);
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();
+}
+
 // The same pass with two adjacent columns per thread (kSmStrip / 2 threads
 // per strip), for the compiled radii: the convolution runs on packed FP32
 // pairs (add / mul / fma .rn.f32x2, each lane rounded as the scalar form, so
@@ -1616,6 +1711,19 @@ SmKernel conv1_kernel(int nb, bool pair) {
   if (nb == 5) return pair ? k_conv1p<OUT, 5, AX> : k_conv1<OUT, 5, AX>;
   return k_conv1<OUT, 0, AX>;
 }
+// The cubes' fused axis-0 + axis-1 pass of gp for radii compiled on both
+// axes (5 and 5, or 10 and 10), unless PWD_CONV01=0 in the environment or
+// the paired-column kernels are chosen; null otherwise.
+SmKernel conv01_kernel(int nb0, int nb1, bool pair) {
+  const char* e = getenv("PWD_CONV01");
+  if (pair || (e && atoi(e) == 0)) return nullptr;
+  if (nb0 == 5 && nb1 == 5) return k_conv01<5, 5>;
+  if (nb0 == 10 && nb1 == 10) return k_conv01<10, 10>;
+  return nullptr;
+}
+size_t conv01_smem(int nb0) {
+  return sizeof(float) * kSmStages * ((kSmStrip + 2 * (nb0 - 1) + 3) & ~3);
+}
 // Threads of an axis-1 (or axis-2) launch: paired columns for the compiled
 // radii when PWD_CONV1_PAIR=1 (a tuning knob: on the batched workload the
 // paired kernel measured 4 % slower, 137.0 against 132.9 ms of CG a step).
@@ -1661,6 +1769,9 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
   cudaFuncSetAttribute(c0_arr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0);
   for (SmKernel k : {c1_cg1, c1_cg2, c1_arr})
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  const SmKernel c01_arr = conv01_kernel(q.nb0, q.nb1, p1);
+  const size_t smem01 = conv01_smem(q.nb0);
+  if (c01_arr) cudaFuncSetAttribute(c01_arr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem01);
   // axis 2 of cubes: the axis-1 kernel on the (n1 n2) x n3 view
   const bool ring2 = !(q.nb2 == 10 || q.nb2 == 5);
   const size_t smem2 = sizeof(float) * (kSmStages * 6 * kSmStrip +
@@ -1706,12 +1817,19 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
         PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, c1t, smem1, st>>>(a, b, q)));
         q.in = a.t2;
         PWD_KERNEL(PWD_FAM_CG, st, (c2_cg1<<<gg, c2t, smem2, st>>>(a, b, q)));
-        q.in = a.gp;
-        q.out = a.tmp;
-        PWD_KERNEL(PWD_FAM_CG, st, (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
-        q.in = a.tmp;
-        q.out = a.t2;
-        PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, c1t, smem1, st>>>(a, b, q)));
+        if (c01_arr) {  // axis 0 of gp inside the axis-1 pass
+          q.in = a.gp;
+          q.out = a.t2;
+          PWD_KERNEL(PWD_FAM_CG, st, (c01_arr<<<gf, kSmStrip, smem01, st>>>(a, b, q)));
+        } else {
+          q.in = a.gp;
+          q.out = a.tmp;
+          PWD_KERNEL(PWD_FAM_CG, st,
+                     (c0_arr<<<gc, conv0_threads<SM_IN_ARR>(), smem0, st>>>(a, b, q)));
+          q.in = a.tmp;
+          q.out = a.t2;
+          PWD_KERNEL(PWD_FAM_CG, st, (c1_arr<<<gf, c1t, smem1, st>>>(a, b, q)));
+        }
         q.in = a.t2;
         q.gpc = a.gp;
         PWD_KERNEL(PWD_FAM_CG, st, (c2_cg2<<<gg, c2t, smem2, st>>>(a, b, q)));

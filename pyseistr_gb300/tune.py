@@ -13,6 +13,9 @@ The kernels read a few tuning knobs from the environment at every call:
   PWD_SPRAY_SPLIT  spray factor kernel: a thread per filter orientation (1),
                    per trace (0), or chosen by the wave count (unset)
 
+and one switch that is not searched: PWD_CONV01=0 runs the cubes' axis-0
+and axis-1 passes of gp as two kernels instead of one (the same bits).
+
 None of them changes what is computed: the spray and the axis-0 staging
 give the same bits whatever the setting, and the strip height and the
 column pairing only change the order in which the mixed CG's FP64 dot
