@@ -147,7 +147,9 @@ int pwd_dip_batch_run(const float *data, const float *mask, float *dip_out,
  * updates, and the dot products stay in FP64 as in the plain path.  The
  * slopes agree with an FP64 evaluation of the reference algorithm to about
  * the accuracy of the plain FP32 path.  No reference counterpart: it is an
- * alternative arithmetic for the same dipc computation.
+ * alternative arithmetic for the same dipc computation.  Its tile copies
+ * wait at most 50 ms each; a section whose copy did not complete in time
+ * (a fault of the device, not of the input) gets NaN slopes.
  */
 size_t pwd_dip_batch_mixed_workspace_size(const pwd_section *sections, int nsec, int order,
                                           const int rect[3], int has_mask);

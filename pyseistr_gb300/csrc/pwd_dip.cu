@@ -658,6 +658,16 @@ __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
   }
 }
 
+// Slopes of a section whose staged tile copy in the mixed CG timed out (the
+// bounded wait gave up, the tile's CG values are missing) are set to NaN.
+__global__ void k_mark_lost(DipArrays a, DipBatch b, int dip) {
+  const TileRange tr = tile_range(b, blockIdx.x);
+  const SecDesc& s = b.secs[tr.sec];
+  if (!b.S[tr.sec].stage_timeout || no_pass(s, dip)) return;
+  float* p = a.p + pout_of(s, dip);
+  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) p[i] = __int_as_float(0x7fc00000);
+}
+
 // mask32 (dip_cfuns.c:914-997, both=false, nj=1): flags samples whose PWD
 // stencil touches a zero of the mask data.  m0 inline, m1 crossline.
 __global__ void k_mask32(const float* __restrict__ mdata, uint8_t* __restrict__ m0,
@@ -1842,6 +1852,7 @@ int dip3_run_mixed(DipArrays a, int dip, int niter, int liter, const int rect[3]
       PWD_KERNEL(PWD_FAM_PWD, st,
                  k_ls_trial<NW, true><<<gt, kTileThreads, 0, st>>>(af, b, c, dip, k));
   }
+  PWD_KERNEL(PWD_FAM_OTHER, st, k_mark_lost<<<gt, kTileThreads, 0, st>>>(a, b, dip));
   return cudaGetLastError() == cudaSuccess ? PWD_OK : PWD_ECUDA;
 }
 
