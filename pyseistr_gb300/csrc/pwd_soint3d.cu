@@ -181,14 +181,16 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_ap3_fwd(const float* __rest
   float* yy = yyb + 2 * s.off;
   ffacc c0, c1, c2, c3, c4, c5;
   const float *Ssv = A.Ss + 2 * s.off, *rrv = A.rr + 2 * s.off;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+  // 32-bit indices within the patch (fewer than 2^31 samples)
+  const int n = (int)g.n, hi = (int)tr.hi;
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x) {
     float yo[2];
 #pragma unroll 1
     for (int part = 0; part < 2; part++) {
-      float* y = yy + (part == 0 ? 0 : g.n);
+      float* y = yy + (part == 0 ? 0 : n);
       float acc = add ? y[i] : 0.f;
       const uint8_t ok = (part == 0 ? A.v1 : A.v2)[s.off + i];
-      const long st = part == 0 ? g.nx : (long)g.nx * g.ny;
+      const int st = part == 0 ? g.nx : g.nx * g.ny;
       const int nj = part == 0 ? g.nj1 : g.nj2;
       // the shifts are all 0 without drift
       const int id = g.drift ? (part == 0 ? A.id1 : A.id2)[s.off + i] : 0;
@@ -198,11 +200,11 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_ap3_fwd(const float* __rest
       float xa[NA], xb[NA], fv[NA];
 #pragma unroll
       for (int iw = 0; iw < NA; iw++) {
-        const long is = (long)(iw - NW) * nj;
-        const long ia = i + st + is, ib = i - is - id;
-        xa[iw] = xx[ia < 0 ? 0 : (ia >= g.n ? g.n - 1 : ia)];
-        xb[iw] = xx[ib < 0 ? 0 : (ib >= g.n ? g.n - 1 : ib)];
-        fv[iw] = f[iw * g.n + i];
+        const int is = (iw - NW) * nj;
+        const int ia = i + st + is, ib = i - is - id;
+        xa[iw] = xx[ia < 0 ? 0 : (ia >= n ? n - 1 : ia)];
+        xb[iw] = xx[ib < 0 ? 0 : (ib >= n ? n - 1 : ib)];
+        fv[iw] = f[(long)iw * n + i];
       }
       if (ok) {
 #pragma unroll
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_ap3_fwd(const float* __rest
     if (DOTS) {
 #pragma unroll
       for (int part = 0; part < 2; part++) {
-        const long k = i + part * s.n;
+        const int k = i + part * n;
         const float a = yo[part], sv = Ssv[k], r = rrv[k];
         c0.add_prod(a, a);
         c1.add_prod(sv, sv);
@@ -239,49 +241,51 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_ap3_fwd(const float* __rest
 // i = m - st - is and the "-" terms from rows i with i - is - id_i = m, all
 // added in the reference's scatter order (row i ascending, iw ascending,
 // "+" before "-"), part 1 before part 2.
+// Indices are 32-bit within a patch (a patch holds fewer than 2^31
+// samples); a tap plane is n floats, so plane iw starts at f + iw n (64-bit).
 template <int NW>
-__device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, long m, long st, int nj,
+__device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, int m, int st, int nj,
                                               const float* __restrict__ f,
                                               const int* __restrict__ idv,
-                                              const uint8_t* __restrict__ v, long n, int drift,
+                                              const uint8_t* __restrict__ v, int n, int drift,
                                               int dmax, float acc) {
   constexpr int NA = 2 * NW + 1;
   // "+" list: iw = NA-1 .. 0 gives ascending rows
-  long ip[NA];
+  int ip[NA];
   int wp[NA];
   int np_ = 0;
   for (int iw = NA - 1; iw >= 0; iw--) {
-    long i = m - st - (long)(iw - NW) * nj;
-    if (i >= 0 && i < n && v[i]) {
+    const int i = m - st - (iw - NW) * nj;
+    if ((unsigned)i < (unsigned)n && v[i]) {
       ip[np_] = i;
       wp[np_] = iw;
       np_++;
     }
   }
   int a = 0;
-  auto emit_plus_upto = [&](long ilim, int iwlim, bool strict) {
+  auto emit_plus_upto = [&](int ilim, int iwlim, bool strict) {
     while (a < np_ && (ip[a] < ilim || (ip[a] == ilim && (strict ? wp[a] <= iwlim : false)))) {
-      acc = __fadd_rn(acc, __fmul_rn(y[ip[a]], f[wp[a] * n + ip[a]]));
+      acc = __fadd_rn(acc, __fmul_rn(y[ip[a]], f[(long)wp[a] * n + ip[a]]));
       a++;
     }
   };
   if (!drift) {
     for (int iw = 0; iw < NA; iw++) {
-      long i = m + (long)(iw - NW) * nj;
-      if (i < 0 || i >= n || !v[i]) continue;
+      const int i = m + (iw - NW) * nj;
+      if ((unsigned)i >= (unsigned)n || !v[i]) continue;
       emit_plus_upto(i, iw, true);
-      acc = __fsub_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
+      acc = __fsub_rn(acc, __fmul_rn(y[i], f[(long)iw * n + i]));
     }
   } else {
-    const long lo = m - (long)NW * nj - dmax, hi = m + (long)NW * nj + dmax;
-    for (long i = lo; i <= hi; i++) {
-      if (i < 0 || i >= n || !v[i]) continue;
-      long q = i - m - idv[i];
+    const int lo = m - NW * nj - dmax, hi = m + NW * nj + dmax;
+    for (int i = lo; i <= hi; i++) {
+      if ((unsigned)i >= (unsigned)n || !v[i]) continue;
+      const int q = i - m - idv[i];
       if (q % nj) continue;
-      long iw = q / nj + NW;
+      const int iw = q / nj + NW;
       if (iw < 0 || iw >= NA) continue;
-      emit_plus_upto(i, (int)iw, true);
-      acc = __fsub_rn(acc, __fmul_rn(y[i], f[iw * n + i]));
+      emit_plus_upto(i, iw, true);
+      acc = __fsub_rn(acc, __fmul_rn(y[i], f[(long)iw * n + i]));
     }
   }
   emit_plus_upto(n, 0, false);
@@ -295,10 +299,9 @@ __device__ __forceinline__ float ap3_adj_part(const float* __restrict__ y, long 
 // into the patch), then the valid terms are added in that order: the same
 // additions as a loop that tests each row before loading it.
 template <int NW>
-__device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ y, long m,
-                                                      long st, int nj,
-                                                      const float* __restrict__ f,
-                                                      const uint8_t* __restrict__ v, long n,
+__device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ y, int m, int st,
+                                                      int nj, const float* __restrict__ f,
+                                                      const uint8_t* __restrict__ v, int n,
                                                       float acc) {
   constexpr int NA = 2 * NW + 1;
   float yv[2 * NA], fv[2 * NA];
@@ -307,13 +310,13 @@ __device__ __forceinline__ float ap3_adj_part_nodrift(const float* __restrict__ 
   for (int k = 0; k < 2 * NA; k++) {
     // k < NA: "+" term iw = NA-1-k at row m - st - is; else "-" term iw = k-NA at m + is
     const int iw = k < NA ? NA - 1 - k : k - NA;
-    const long is = (long)(iw - NW) * nj;
-    const long i = k < NA ? m - st - is : m + is;
-    const bool in = i >= 0 && i < n;
-    const long ic = in ? i : m;
+    const int is = (iw - NW) * nj;
+    const int i = k < NA ? m - st - is : m + is;
+    const bool in = (unsigned)i < (unsigned)n;
+    const int ic = in ? i : m;
     ok[k] = in && v[ic];
     yv[k] = y[ic];
-    fv[k] = f[iw * n + ic];
+    fv[k] = f[(long)iw * n + ic];
   }
 #pragma unroll
   for (int k = 0; k < NA; k++)
@@ -338,20 +341,22 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_ap3_adj(SoArrays A, SoBatch
   const int dm = g.drift ? S->dmax : 0;
   const float* yy = A.rr + 2 * s.off;
   const float *f1 = A.f1 + NA * s.off, *f2 = A.f2 + NA * s.off;
+  const uint8_t *v1 = A.v1 + s.off, *v2 = A.v2 + s.off, *known = A.known + s.off;
+  float* gout = A.g + s.off;
+  // 32-bit indices within the patch (fewer than 2^31 samples)
+  const int n = (int)g.n, st2 = g.nx * g.ny, hi = (int)tr.hi;
   ffacc a0;
-  for (long m = tr.lo + threadIdx.x; m < tr.hi; m += blockDim.x) {
+  for (int m = (int)tr.lo + threadIdx.x; m < hi; m += blockDim.x) {
     float a = 0.f;
     if (DRIFT) {
-      a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, f1, A.id1 + s.off, A.v1 + s.off, g.n, 1, dm, a);
-      a = ap3_adj_part<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.id2 + s.off,
-                           A.v2 + s.off, g.n, 1, dm, a);
+      a = ap3_adj_part<NW>(yy, m, g.nx, g.nj1, f1, A.id1 + s.off, v1, n, 1, dm, a);
+      a = ap3_adj_part<NW>(yy + n, m, st2, g.nj2, f2, A.id2 + s.off, v2, n, 1, dm, a);
     } else {
-      a = ap3_adj_part_nodrift<NW>(yy, m, g.nx, g.nj1, f1, A.v1 + s.off, g.n, a);
-      a = ap3_adj_part_nodrift<NW>(yy + g.n, m, (long)g.nx * g.ny, g.nj2, f2, A.v2 + s.off,
-                                   g.n, a);
+      a = ap3_adj_part_nodrift<NW>(yy, m, g.nx, g.nj1, f1, v1, n, a);
+      a = ap3_adj_part_nodrift<NW>(yy + n, m, st2, g.nj2, f2, v2, n, a);
     }
-    if (A.known[s.off + m]) a = 0.f;
-    A.g[s.off + m] = a;
+    if (known[m]) a = 0.f;
+    gout[m] = a;
     a0.add_prod(a, a);
   }
   dvec<1> acc = {{a0.value()}};
@@ -425,14 +430,16 @@ __global__ void k_cg3_update(SoArrays A, SoBatch b, int iter) {
   const float al = S->alfa, be = S->beta;
   float *x = A.x + s.off, *Sv = A.S + s.off, *rr = A.rr + 2 * s.off, *Ss = A.Ss + 2 * s.off;
   const float *g = A.g + s.off, *gg = A.gg + 2 * s.off;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+  // 32-bit indices within the patch (fewer than 2^31 samples)
+  const int n = (int)s.n, hi = (int)tr.hi;
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x) {
     float sv = iter == 0 ? 0.f : Sv[i];
     sv = __fadd_rn(__fmul_rn(sv, be), __fmul_rn(al, g[i]));
     Sv[i] = sv;
     x[i] = __fadd_rn(x[i], sv);
 #pragma unroll
     for (int part = 0; part < 2; part++) {
-      const long k = i + part * s.n;
+      const int k = i + part * n;
       float s2 = iter == 0 ? 0.f : Ss[k];
       s2 = __fadd_rn(__fmul_rn(s2, be), __fmul_rn(al, gg[k]));
       Ss[k] = s2;
