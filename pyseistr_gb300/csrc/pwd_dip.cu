@@ -859,17 +859,8 @@ __device__ __forceinline__ void cg2_finish(DipScalars* S, const dvec<3>& tot, in
 // Output operation at one sample given the smoothed value v.
 struct CgOut {
   ffacc a0, a1, a2;
-  __device__ __forceinline__ void cg1(const DipArrays& a, long i, float v, float st, int iter) {
-    float p = a.pcg[i];
-    if (iter > 0) {
-      p = __fmaf_rn(st, a.sp[i], p);
-      a.pcg[i] = p;
-    }
-    const float g = __fadd_rn(p, v);  // gp = eps p + S' gx, eps = 1
-    a.gp[i] = g;
-    a0.add_prod(g, g);
-  }
-  // the same with the operands already loaded: pc = pcg, sv = sp
+  // p = pcg (+ step sp after the first iteration), gp = eps p + S' gx with
+  // eps = 1, gp.gp; the operands arrive staged: pc = pcg, sv = sp
   __device__ __forceinline__ void cg1v(const DipArrays& a, long i, float v, float st, int iter,
                                        float pc, float sv) {
     float p = pc;
@@ -1326,14 +1317,13 @@ __global__ void __launch_bounds__(kSmStrip, 16) k_conv1(DipArrays a, DipBatch b,
 // another's copies), and a slot is refilled only after the barrier that
 // follows its last reads.  (The same fusion into the conjugate-update pass
 // of 2-D sections measured slower than the separate passes.)
-template <int NB0>
-__host__ __device__ constexpr int conv01_seg() {
-  return (kSmStrip + 2 * (NB0 - 1) + 3) & ~3;
+__host__ __device__ constexpr int conv01_seg(int nb0) {
+  return (kSmStrip + 2 * (nb0 - 1) + 3) & ~3;
 }
 template <int NB0, int NB1>
 __global__ void __launch_bounds__(kSmStrip, 16) k_conv01(DipArrays a, DipBatch b, SmParams q) {
   extern __shared__ float sm[];
-  constexpr int H0 = NB0 - 1, H1 = NB1 - 1, RING = 2 * H1 + 1, SEG = conv01_seg<NB0>();
+  constexpr int H0 = NB0 - 1, H1 = NB1 - 1, RING = 2 * H1 + 1, SEG = conv01_seg(NB0);
   const int t = blockIdx.x;
   const int si = find_section(b.nsec, (long)t, [&](int k) { return (long)b.secs[k].ftile0; });
   const SecDesc& s = b.secs[si];
@@ -1731,9 +1721,7 @@ SmKernel conv01_kernel(int nb0, int nb1, bool pair) {
   if (nb0 == 10 && nb1 == 10) return k_conv01<10, 10>;
   return nullptr;
 }
-size_t conv01_smem(int nb0) {
-  return sizeof(float) * kSmStages * ((kSmStrip + 2 * (nb0 - 1) + 3) & ~3);
-}
+size_t conv01_smem(int nb0) { return sizeof(float) * kSmStages * conv01_seg(nb0); }
 // Threads of an axis-1 (or axis-2) launch: paired columns for the compiled
 // radii when PWD_CONV1_PAIR=1 (a tuning knob: on the batched workload the
 // paired kernel measured 4 % slower, 137.0 against 132.9 ms of CG a step).
