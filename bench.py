@@ -323,7 +323,7 @@ def api_step(wl, mixed=False, host=None):
     if wl.name == "plain3d":
         c = wl.sections[0]
         pi, px = ps.dip3dc(c, d["niter"], d["liter"], d["order"], eps_dv=0.01, eps_cg=1,
-                           tol_cg=1e-6, rect=list(d["rect"]))
+                           tol_cg=1e-6, rect=list(d["rect"]), mixed=mixed)
         ps.somean3dc(c, pi, px, f["r1"], f["r2"], f["eps"], f["order"])
         ps.somf3dc(c, pi, px, f["r1"], f["r2"], f["eps"], f["order"])
         return 7 * nbytes, 4 * nbytes

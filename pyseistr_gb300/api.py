@@ -151,8 +151,11 @@ def csoint2d(din, mask, dip1, dip2, n1, n2, nw, nj1, nj2, niter, drift, hasmask,
 # high-level entries
 # --------------------------------------------------------------------------
 def dip2dc(din, niter=5, liter=20, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.000001,
-           rect=[10, 10, 1], verb=1, mask=None):
-    """2-D slope by shaping-regularised PWD (dip2d.py:115)."""
+           rect=[10, 10, 1], verb=1, mask=None, mixed=False):
+    """2-D slope by shaping-regularised PWD (dip2d.py:115).  mixed=True (not
+    in the reference) estimates it in the mixed mode: FP32 taps, the
+    smoothing as a fused direct convolution, FP64 reductions; about 1e-7
+    from an FP64 evaluation instead of the reference's bits."""
     n1, n2 = din.shape[0], din.shape[1]
     d, as_t = _to_dev_flat(din)
     m = None
@@ -160,13 +163,17 @@ def dip2dc(din, niter=5, liter=20, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.0000
         if int(np.prod(mask.shape)) != n1 * n2:
             raise ValueError("Mask and Data should have the same dimension")
         m, _ = _to_dev_flat(mask)
-    out = D.dip(d, n1, n2, 1, niter, liter, order, rect, m)
+    if mixed:
+        out = D.dip_batch(d, [(n1, n2)], niter, liter, order, rect, mask=m, mixed=True)
+    else:
+        out = D.dip(d, n1, n2, 1, niter, liter, order, rect, m)
     return _from_dev_flat(out, (n1, n2), as_t)
 
 
 def dip3dc(din, niter=5, liter=10, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.000001,
-           rect=[5, 5, 5], verb=1, runc=1, mask=None):
-    """3-D inline and crossline slopes (dip3d.py:59)."""
+           rect=[5, 5, 5], verb=1, runc=1, mask=None, mixed=False):
+    """3-D inline and crossline slopes (dip3d.py:59); mixed=True as in
+    dip2dc."""
     n1, n2, n3 = din.shape
     d, as_t = _to_dev_flat(din)
     m = None
@@ -174,7 +181,10 @@ def dip3dc(din, niter=5, liter=10, order=2, eps_dv=0.01, eps_cg=1, tol_cg=0.0000
         if int(np.prod(mask.shape)) != n1 * n2 * n3:
             raise ValueError("Mask and Data should have the same dimension")
         m, _ = _to_dev_flat(mask)
-    out = D.dip(d, n1, n2, n3, niter, liter, order, rect, m)
+    if mixed:
+        out = D.dip_batch(d, [(n1, n2, n3)], niter, liter, order, rect, mask=m, mixed=True)
+    else:
+        out = D.dip(d, n1, n2, n3, niter, liter, order, rect, m)
     n = n1 * n2 * n3
     return (_from_dev_flat(out[:n], (n1, n2, n3), as_t),
             _from_dev_flat(out[n:], (n1, n2, n3), as_t))

@@ -225,6 +225,26 @@ def test_dip_graph_replay_equals_direct_call(D, mixed):
         assert np.array_equal(got, want)
 
 
+def test_dipc_mixed_keyword_equals_batch(D, O):
+    """dip2dc / dip3dc with mixed=True give the mixed batch's slopes for
+    their one section (within the bar of FP64); the default stays the
+    bit-faithful path."""
+    import workloads
+    import pyseistr_gb300 as ps
+
+    d2 = workloads.plain2d()[:200, :60].copy()
+    got = ps.dip2dc(d2, 3, 6, 2, rect=[10, 10, 1], mixed=True)
+    assert np.array_equal(got, _batch(D, [d2], 3, 6, 2, (10, 10, 1))[0])
+    plain = ps.dip2dc(d2, 3, 6, 2, rect=[10, 10, 1])
+    assert np.array_equal(plain, _batch(D, [d2], 3, 6, 2, (10, 10, 1), mixed=False)[0])
+    c = workloads.plain3d()[:60, :14, :11].copy()
+    pi, px = ps.dip3dc(c, 2, 4, 2, rect=[5, 5, 5], mixed=True)
+    wi, wx = _batch(D, [c], 2, 4, 2, (5, 5, 5))[0]
+    assert np.array_equal(pi, wi) and np.array_equal(px, wx)
+    fi, fx = O.dip3d(c, 2, 4, 2, (5, 5, 5), precision="f64")
+    assert rel_l2(pi, fi) <= MIXED_TOL and rel_l2(px, fx) <= MIXED_TOL
+
+
 def test_packed_host_api_equals_list_api(D):
     """dip_somean2d_packed on a pinned packed tensor returns the list API's
     slopes and filtered sections."""
