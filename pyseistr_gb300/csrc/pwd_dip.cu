@@ -103,7 +103,7 @@ __device__ __forceinline__ bool sec_sum_last(dvec<K> x, const DipBatch& b, int t
 }
 
 // Sections hold fewer than 2^31 samples, so 32-bit index arithmetic is used.
-__device__ __forceinline__ bool pwd_valid(const SecDesc& s, long i, int nw, int dip) {
+__device__ __forceinline__ bool pwd_valid(const SecDesc& s, int i, int nw, int dip) {
   const unsigned ii = (unsigned)i, n1 = (unsigned)s.n1, n2 = (unsigned)s.n2;
   const int i1 = (int)(ii % n1);
   const unsigned r = ii / n1;
@@ -114,7 +114,7 @@ __device__ __forceinline__ bool pwd_valid(const SecDesc& s, long i, int nw, int 
 
 // allpass1/allpass2 at one sample (dip_cfuns.c:1135-1200, :1399-1465).
 template <int NW, bool DER, bool FAST = false>
-__device__ __forceinline__ float pwd_at(const float* __restrict__ u, long i, long ip,
+__device__ __forceinline__ float pwd_at(const float* __restrict__ u, int i, int ip,
                                         const ApCoef& c, float p) {
   float f[2 * NW + 1];
   if (FAST) {
@@ -136,8 +136,8 @@ __device__ __forceinline__ float pwd_at(const float* __restrict__ u, long i, lon
   return y;
 }
 
-__device__ __forceinline__ long nb_offset(const SecDesc& s, int dip) {
-  return dip == 1 ? (long)s.n1 : (long)s.n1 * s.n2;
+__device__ __forceinline__ int nb_offset(const SecDesc& s, int dip) {
+  return dip == 1 ? s.n1 : s.n1 * s.n2;
 }
 
 // 2-D sections of a batch that also holds cubes have no crossline slope.
@@ -151,8 +151,8 @@ __global__ void k_residual(DipArrays a, DipBatch b, ApCoef c, int dip) {
   const float* u = a.u + s.off;
   const float* p = a.p + pout_of(s, dip);
   float* u2 = a.u2 + s.off;
-  const long ip = nb_offset(s, dip);
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
+  const int ip = nb_offset(s, dip), hi = (int)tr.hi;
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x)
     u2[i] = pwd_valid(s, i, NW, dip) ? pwd_at<NW, false, FAST>(u, i, ip, c, p[i]) : 0.f;
 }
 
@@ -169,9 +169,9 @@ __global__ void k_prep(DipArrays a, DipBatch b, ApCoef c, int dip) {
   const float* p = a.p + pout_of(s, dip);
   float *u2 = a.u2 + s.off, *u1 = a.u1 + s.off, *p0 = a.p0 + s.off;
   const uint8_t* mask = a.mask ? a.mask + s.off : nullptr;
-  const long ip = nb_offset(s, dip);
+  const int ip = nb_offset(s, dip), hi = (int)tr.hi;
   ffacc a0, a1;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x) {
     float pi = p[i];
     float d = pwd_valid(s, i, NW, dip) ? pwd_at<NW, true, FAST>(u, i, ip, c, pi) : 0.f;
     float r = u2[i];
@@ -638,9 +638,9 @@ __global__ void k_ls_trial(DipArrays a, DipBatch b, ApCoef c, int dip, int k) {
   const float pmin = -FLT_MAX, pmax = FLT_MAX;
   const float *u = a.u + s.off, *p0 = a.p0 + s.off, *dp = a.dp + s.off;
   float *p = a.p + pout_of(s, dip), *u2 = a.u2 + s.off;
-  const long ip = nb_offset(s, dip);
+  const int ip = nb_offset(s, dip), hi = (int)tr.hi;
   ffacc a0;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x) {
     float pi = __fadd_rn(p0[i], __fmul_rn(lam, dp[i]));
     if (pi < pmin) pi = pmin;
     if (pi > pmax) pi = pmax;
