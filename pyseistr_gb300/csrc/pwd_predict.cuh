@@ -470,19 +470,21 @@ __device__ void predict_factor(int n1, float eps, float eps2, const ApCoef& c,
 // sample (taps, factor elements, input, y) is staged kApplyStages - 1
 // samples ahead by cp.async into the thread's ring in shared memory: ring
 // element e of slot q at ring[(q*apply_elems(NW) + e)*rs] (rs = threads of the
-// block, so consecutive threads hit consecutive banks).
+// block, so consecutive threads hit consecutive banks).  IX is the type of
+// the element offsets: int where every offset of the section's factor store
+// fits in 32 bits (fewer integer instructions a sample), long otherwise.
 #ifndef PWD_APPLY_STAGES
 #define PWD_APPLY_STAGES 4
 #endif
 constexpr int kApplyStages = PWD_APPLY_STAGES;
 __host__ __device__ constexpr int apply_elems(int nw) { return 4 * nw + 3; }  // NA + NB + 2
 
-template <int NW, bool RHS2>
+template <int NW, bool RHS2, typename IX = long>
 __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps,
-                              const float* __restrict__ fac, long fss, bool forw,
-                              const float* in1, long ins, float* __restrict__ out, float* ys,
-                              float* ysb, long yss, float* ring, int rs,
-                              const float* in1b = nullptr, long insb = 1,
+                              const float* __restrict__ fac, IX fss, bool forw,
+                              const float* in1, IX ins, float* __restrict__ out, float* ys,
+                              float* ysb, IX yss, float* ring, int rs,
+                              const float* in1b = nullptr, IX insb = 1,
                               float* __restrict__ outb = nullptr) {
   constexpr int NA = 2 * NW + 1, NB = 2 * NW, P = kApplyStages, NE = apply_elems(NW);
   // the input trace (the previous step's output) and, below, the y scratch
@@ -513,7 +515,7 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     if (cc < n1) {
       float v[NA];
 #pragma unroll
-      for (int j = 0; j < NA; j++) v[j] = taps[((long)j * n1 + cc) * fss];
+      for (int j = 0; j < NA; j++) v[j] = taps[((IX)j * n1 + cc) * fss];
       set_col(v, w1.a[NW + 1 + cc]);
     }
 #pragma unroll
@@ -536,10 +538,10 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
       const int q = i % P, cn = i + NW, ln = i + 2 * NW;
       if (cn < n1)
 #pragma unroll
-        for (int j = 0; j < NA; j++) cp_async4(R(q, j), taps + ((long)j * n1 + cn) * fss);
+        for (int j = 0; j < NA; j++) cp_async4(R(q, j), taps + ((IX)j * n1 + cn) * fss);
 #pragma unroll
       for (int m = 0; m < NB; m++)
-        if (m < i) cp_async4(R(q, NA + m), fac + ((long)m * n1 + (i - 1 - m)) * fss);
+        if (m < i) cp_async4(R(q, NA + m), fac + ((IX)m * n1 + (i - 1 - m)) * fss);
       if (ln < n1) {
         cp_async4(R(q, NA + NB), in1 + ln * ins);
         if (RHS2) cp_async4(R(q, NA + NB + 1), in1b + ln * insb);
@@ -615,8 +617,8 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
         y = __fsub_rn(y, __fmul_rn(om, Y[m]));
         if (RHS2) y2 = __fsub_rn(y2, __fmul_rn(om, YB[m]));
       }
-    ys[(long)i * yss] = y;
-    if (RHS2) ysb[(long)i * yss] = y2;
+    ys[(IX)i * yss] = y;
+    if (RHS2) ysb[(IX)i * yss] = y2;
 #pragma unroll
     for (int m = NB - 1; m > 0; m--) {
       Y[m] = Y[m - 1];
@@ -635,10 +637,10 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
       const int k = n1 - 1 - step, q = step % P;
 #pragma unroll
       for (int m = 0; m < NB; m++)
-        if (m < n1 - k - 1) cp_async4(R(q, m), fac + ((long)m * n1 + k) * fss);
-      cp_async4(R(q, NB), fac + ((long)NB * n1 + k) * fss);
-      cp_async4(R(q, NB + 1), ys + (long)k * yss);
-      if (RHS2) cp_async4(R(q, NB + 2), ysb + (long)k * yss);
+        if (m < n1 - k - 1) cp_async4(R(q, m), fac + ((IX)m * n1 + k) * fss);
+      cp_async4(R(q, NB), fac + ((IX)NB * n1 + k) * fss);
+      cp_async4(R(q, NB + 1), ys + (IX)k * yss);
+      if (RHS2) cp_async4(R(q, NB + 2), ysb + (IX)k * yss);
     }
     cp_async_commit();
   };
@@ -671,11 +673,11 @@ __device__ void predict_apply(int n1, float eps2, const float* __restrict__ taps
     }
     X[0] = t;
     out[k] = t;
-    ys[(long)k * yss] = t;  // y[k] is consumed: the slot carries the output
+    ys[(IX)k * yss] = t;  // y[k] is consumed: the slot carries the output
     if (RHS2) {
       XB[0] = tb2;
       outb[k] = tb2;
-      ysb[(long)k * yss] = tb2;
+      ysb[(IX)k * yss] = tb2;
     }
   }
   cp_async_wait<0>();

@@ -9,6 +9,7 @@
 // predicted through the same factorisation in the same chain.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "pwd_batch.cuh"
@@ -102,7 +103,7 @@ __global__ void k_spray2_factor(const float* __restrict__ dip, SprayBufs bf, Spr
 // warp holds 32 consecutive (padded) source traces of one section and one
 // direction (whole-line factor and scratch accesses).  MODE 0: data only into u; MODE 1: data and
 // the trace of ones together (u and u1); MODE 2: ones only into u1.
-template <int NW, int MODE>
+template <int NW, int MODE, typename IX = long>
 __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict__ in, const float* __restrict__ ones,
                                SprayBufs bf, SprayB b) {
   extern __shared__ float apply_ring[];  // kApplyStages x apply_elems(NW) per thread
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict
   // the previous prediction from the chain's interleaved scratch
   const float* prev = src;
   const float* prevb = ones;
-  long ps = 1;
+  IX ps = 1;
   for (int is = 0; is < ns; is++) {
     // dir 0 predicts forward to trace i-is-1 with its own slopes (forw=false);
     // dir 1 predicts backward to trace i+is+1 with the slopes of ip-1.
@@ -149,16 +150,17 @@ __global__ void __launch_bounds__(64, 10) k_spray2_apply(const float* __restrict
     float* out = slot(U, ip, sl);
     if (MODE == 1) {
       float* outb = slot(U1, ip, sl);
-      predict_apply<NW, true>(n1, b.eps2, f.taps + tk, fac, f.ntp, dir == 1, prev, ps, out,
-                              f.y + cl, f.yb + cl, yss, apply_ring + threadIdx.x, blockDim.x,
-                              prevb, ps, outb);
+      predict_apply<NW, true, IX>(n1, b.eps2, f.taps + tk, fac, (IX)f.ntp, dir == 1, prev, ps,
+                                  out, f.y + cl, f.yb + cl, (IX)yss, apply_ring + threadIdx.x,
+                                  blockDim.x, prevb, ps, outb);
       prevb = f.yb + cl;
     } else {
-      predict_apply<NW, false>(n1, b.eps2, f.taps + tk, fac, f.ntp, dir == 1, prev, ps, out,
-                               f.y + cl, nullptr, yss, apply_ring + threadIdx.x, blockDim.x);
+      predict_apply<NW, false, IX>(n1, b.eps2, f.taps + tk, fac, (IX)f.ntp, dir == 1, prev, ps,
+                                   out, f.y + cl, nullptr, (IX)yss, apply_ring + threadIdx.x,
+                                   blockDim.x);
     }
     prev = f.y + cl;
-    ps = yss;
+    ps = (IX)yss;
   }
 }
 
@@ -438,6 +440,20 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
     return PWD_ECUDA;
   const unsigned gap = (unsigned)((2 * L.ntp + bs - 1) / bs);
   const size_t ring = sizeof(float) * kApplyStages * apply_elems(NW) * bs;
+  // 32-bit element offsets in the chains when every section's factor store
+  // (2 NW + 1 planes of n1 x padded traces, the largest group) allows them
+  bool i32 = true;
+  for (const SecDesc& s : secs)
+    if ((long)(2 * NW + 1) * s.n1 * padded_traces((long)s.n2 * s.n3) >= (1L << 31)) i32 = false;
+  auto apply = [&](auto mode) {
+    constexpr int M = decltype(mode)::value;
+    if (i32)
+      PWD_KERNEL(PWD_FAM_SPRAY, st,
+                 (k_spray2_apply<NW, M, int><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b)));
+    else
+      PWD_KERNEL(PWD_FAM_SPRAY, st,
+                 (k_spray2_apply<NW, M, long><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b)));
+  };
   // a thread per filter orientation when even then the factor launch fills
   // less than one wave (a thread per trace then leaves SMs idle); otherwise
   // a thread per trace, its two factors sharing the taps
@@ -458,20 +474,17 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
   }
   if (filter == kMean && have_w1) {
     // the data alone, normalised by the stored w1
-    PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+    apply(std::integral_constant<int, 0>());
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 2, 1));
   } else if (filter == kMean) {
-    PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 1><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+    apply(std::integral_constant<int, 1>());
     PWD_KERNEL(PWD_FAM_FILTER, st,
                k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(
                    w.bf, out, b, w.bf.w1 ? 1 : 0, 1));
   } else if (filter == kMeanAdj || filter == kMeanAdjAdd) {
     if (!have_w1) {
-      PWD_KERNEL(PWD_FAM_SPRAY, st,
-                 k_spray2_apply<NW, 2><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+      apply(std::integral_constant<int, 2>());
       PWD_KERNEL(PWD_FAM_FILTER, st,
                  k_weighted_mean<<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(w.bf, out, b, 1,
                                                                                0));
@@ -485,8 +498,7 @@ int spray2_run(const float* data, const float* dip, float* out, int filter, int 
                k_somean2d_adj_sum<NW><<<(unsigned)L.ntiles, kTileThreads, 0, st>>>(
                    data, out, w.bf, b, filter == kMeanAdjAdd ? 1 : 0));
   } else {
-    PWD_KERNEL(PWD_FAM_SPRAY, st,
-               k_spray2_apply<NW, 0><<<gap, bs, ring, st>>>(data, w.ones, w.bf, b));
+    apply(std::integral_constant<int, 0>());
     if (option == 1) {
       if (nmf > kNetWin)
         PWD_KERNEL(PWD_FAM_FILTER, st,
