@@ -221,7 +221,8 @@ __global__ void k_scale(DipArrays a, DipBatch b, int dip) {
   const float nh = __double2float_rn(nrm);
   const float nl = __double2float_rn(nrm - (double)nh);
   ffacc a0;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x) {
+  const int hi = (int)tr.hi;  // a section holds fewer than 2^31 samples
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x) {
     x[i] = 0.f;
     if (zero) continue;
     float va = mul_by_double(num[i], nh, nl, nrm);
@@ -277,7 +278,8 @@ __global__ void k_cg_step(DipArrays a, DipBatch b) {
   const float st = __double2float_rn(S->step);
   float* x = a.dp + s.off;
   const float* sx = a.sx + s.off;
-  for (long i = tr.lo + threadIdx.x; i < tr.hi; i += blockDim.x)
+  const int hi = (int)tr.hi;  // a section holds fewer than 2^31 samples
+  for (int i = (int)tr.lo + threadIdx.x; i < hi; i += blockDim.x)
     x[i] = __fadd_rn(x[i], __fmul_rn(st, sx[i]));
 }
 
